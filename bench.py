@@ -1,0 +1,294 @@
+"""Benchmark of the TEMPO column step on GB300.
+
+Workload (default): 1024 x 1024 = 1,048,576 columns x 65 levels on the stretched
+20-km grid, 40 % clear columns, dt = 30 s (the batched FP32 forward configuration),
+synthetic seeded profiles generated on the device.  One "step" = one column step over
+all columns; the state is carried from step to step like a model integration.
+
+Prints ONE JSON line.  `value` is device-resident throughput (column-steps/s) of the
+mixed-precision (FP32 bulk, FP64 islands) path; `e2e` is the same metric through the
+host C ABI (tempo_run_f32_c: host arrays, host<->device copies inside the timed
+region).  `--impl reference` times the CPU restatement of the reference (the Fortran
+reference has no compiler here) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "column-steps/s @65 lev: FP32 vs FP64 GPU vs CPU at stated err; adjoint/fwd ratio"
+# algorithmic HBM bytes per column-step, hail off: read 15 3-D fields, write 12
+# prognostic + 4 diagnostic 3-D fields, plus 8 2-D diagnostics
+N_IN3, N_OUT3, N_OUT2 = 15, 16, 8
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ni", type=int, default=1024)
+    ap.add_argument("--nj", type=int, default=1024)
+    ap.add_argument("--nz", type=int, default=65)
+    ap.add_argument("--dt", type=float, default=30.0)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons)}
+
+
+def peaks():
+    try:
+        return json.loads((REPO / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return {}
+
+
+def traffic_from_profiles():
+    try:
+        d = json.loads((REPO / "profiles" / "roofline_traffic.json").read_text())
+        return d.get("dram_bytes_per_launch_full_size")
+    except Exception:
+        return None
+
+
+def cpu_baseline(seconds: float, nz: int, dt: float, sample_cols: int = 16384):
+    """The FP64 CPU restatement (oracle port) on all host cores, bounded sample."""
+    import oracle
+    from tempo_gb300 import workloads as W
+    oracle.build()
+    oracle.init(False, REPO / "tables" / "ccn_activate.bin")
+    oracle.build_big_tables()
+    wl = W.config1(seed=11, ni=sample_cols, nj=1, nz=nz, steps=1, dt=dt)
+    cfg = oracle.default_cfgs(hailaware_flag=0)
+    f = {k: v.copy() for k, v in wl.fields.items()}
+    nj, nk, ni = f["p"].shape
+    d = {"rain_precip": np.zeros((nj, ni)), "refl10cm": np.zeros((nj, nk, ni)),
+         "re_cloud": np.zeros((nj, nk, ni)), "re_ice": np.zeros((nj, nk, ni)),
+         "re_snow": np.zeros((nj, nk, ni))}
+    oracle.run(cfg, dt, 1, f, d)  # warm
+    n, t0 = 0, time.perf_counter()
+    while True:
+        oracle.run(cfg, dt, 2 + n, f, d)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    cores = os.cpu_count()
+    return {"value": sample_cols * n / el, "unit": "column-steps/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{n} steps x {sample_cols} columns x {nz} levels of the same generator, "
+                      f"FP64 CPU restatement, {cores} OpenMP threads, {el:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cb = cpu_baseline(max(5.0, args.cpu_seconds), args.nz, args.dt)
+    line = {"metric": METRIC, "impl": "reference", "value": cb["value"], "unit": "column-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * args.ni * args.nj / cb["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded config1 generator)",
+            "config": {"workload": f"config1: {args.ni * args.nj} columns x {args.nz} levels, "
+                                   f"dt={args.dt}s (timed on a bounded column sample)",
+                       "parallelism": "cpu-openmp"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "column-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import torch.distributed as dist
+    import tempo_gb300 as tg
+    from tempo_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    tg.build.build()
+    ctx = tg.TempoContext(build_tables=True, device=local, cfgs=tg.default_cfgs(hailaware_flag=0))
+    ctx.set_precision(tg.PREC_MIXED)
+    ni, nj, nz = args.ni, args.nj, args.nz
+    ncol = ni * nj
+    f32 = W.config1_torch(seed=rank, ni=ni, nj=nj, nz=nz, device=f"cuda:{local}",
+                          dtype=torch.float32)
+    diag = {n: torch.zeros((nj, ni), device=f"cuda:{local}", dtype=torch.float32) for n in tg.DIAG2}
+    diag.update({n: torch.zeros((nj, nz, ni), device=f"cuda:{local}", dtype=torch.float32)
+                 for n in ("refl10cm", "re_cloud", "re_ice", "re_snow")})
+    stream = torch.cuda.current_stream()
+    it = 1
+    for _ in range(args.warmup):
+        ctx.run_device(f32, args.dt, it, diags=diag)
+        it += 1
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            ctx.run_device(f32, args.dt, it, diags=diag)
+            it += 1
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    stats = ctx.stats()
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * ncol * args.steps / (ms / 1e3)
+
+    # FP64 drop-in on the same columns (a few steps; FP64 is 1/64 rate on GB300)
+    ctx.set_precision(tg.PREC_FP64)
+    f64 = {k: v.double() for k, v in f32.items()}
+    d64 = {k: v.double() for k, v in diag.items()}
+    ctx.run_device(f64, args.dt, 1, diags=d64)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for s in range(args.fp64_steps):
+        ctx.run_device(f64, args.dt, 2 + s, diags=d64)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / args.fp64_steps
+    del f64, d64
+    torch.cuda.empty_cache()
+
+    # end-to-end through the host C ABI (pinned host arrays, copies in the timed region)
+    ctx.set_precision(tg.PREC_MIXED)
+    host = {k: v.cpu().pin_memory().numpy() for k, v in f32.items()}
+    hdiag = {k: torch.zeros(v.shape, dtype=torch.float32).pin_memory().numpy() for k, v in diag.items()}
+    h2d = sum(a.nbytes for a in host.values())
+    d2h = sum(a.nbytes for k, a in host.items() if k not in ("p", "w", "dz")) + \
+        sum(a.nbytes for a in hdiag.values())
+    ctx.run(host, args.dt, 1, diags=hdiag)
+    t0 = time.perf_counter()
+    for s in range(args.e2e_steps):
+        ctx.run(host, args.dt, 2 + s, diags=hdiag)
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_value = world * ncol / e2e_s
+
+    pk = peaks()
+    hbm = pk.get("hbm_gbs")
+    peak_src = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    alg_bytes = ncol * (4 * nz * (N_IN3 + N_OUT3) + 4 * N_OUT2)
+    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    clocks = clk.summary()
+    out = {
+        "metric": METRIC, "value": value, "unit": "column-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded config1 generator on device)",
+        "config": {"workload": f"config1: {ncol} columns x {nz} levels, stretched 20 km grid, "
+                               f"40% clear, dt={args.dt}s, mixed precision (FP32 bulk, FP64 "
+                               f"islands), aerosol-aware, hail-aware off",
+                   "columns_per_gpu": ncol, "levels": nz, "dt": args.dt,
+                   "l2": "inputs (8.5 GB) larger than L2", "parallelism": f"replicas x{world}"},
+        "fp64_value": world * ncol / (ms64 / 1e3), "fp64_ms_per_step": ms64,
+        "fp32_over_fp64": ms64 / ms_step,
+        "e2e": {"value": e2e_value, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "path": "tempo_run_f32_c (host arrays)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic_from_profiles(),
+                     "kernel": "tempo_column_kernel<float,float>",
+                     "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src},
+        "gpu_launches": args.steps * stats.get("launches", 1),
+        "clocks": clocks,
+        "step_stats": stats,
+    }
+    if rank == 0 and not args.no_cpu:
+        try:
+            out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, nz, args.dt)
+        except Exception as e:  # the baseline is reported, never required
+            out["cpu_baseline"] = {"value": None, "error": str(e)}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,192 @@
+/*
+ * tempo_gb300.h -- C ABI of the GB300 (sm_103a) TEMPO column-microphysics step.
+ *
+ * This is the drop-in boundary for the host model's column loop.  Each entry point
+ * replaces one routine of the Fortran reference (NCAR/TEMPO v3.1.1) and keeps its
+ * argument list and argument meaning; a Fortran host binds it with ISO_C_BINDING
+ * (optional arguments map to NULL pointers, logical flags to int 0/1).
+ *
+ * Conventions
+ *   - Every entry point returns an int status: TEMPO_OK (0) or a negative
+ *     tempo_status_t code.  Nothing aborts the process (the reference `error stop`s).
+ *   - tempo_last_error() returns a thread-local message for the last failure.
+ *   - A context owns its device tables and buffers; calls on one context are not
+ *     thread-safe, distinct contexts are independent (one context per host thread or
+ *     per CUDA stream).
+ *   - 3-D arrays are (ims:ime, kms:kme, jms:jme) with i fastest, exactly as in
+ *     tempo_run; the step updates them in place on the tile its:ite, kts:kte,
+ *     jts:jte.  Diagnostic arrays are tile-shaped (its:ite, [kts:kte,] jts:jte).
+ */
+#ifndef TEMPO_GB300_H
+#define TEMPO_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TEMPO_OK = 0,
+  TEMPO_ERR_ARG = -1,         /* NULL required pointer, bad bounds, dt <= 0, ... */
+  TEMPO_ERR_UNSUPPORTED = -2, /* optional path outside this build (ML, semi-Lagrangian, melting radar) */
+  TEMPO_ERR_TABLE = -3,       /* missing, truncated or malformed lookup table */
+  TEMPO_ERR_CUDA = -4,        /* CUDA runtime failure (message has the CUDA error string) */
+  TEMPO_ERR_NOMEM = -5,       /* host or device allocation failed */
+  TEMPO_ERR_STATE = -6,       /* context not initialised / wrong precision for the call */
+  TEMPO_ERR_TIMEOUT = -7,     /* a bounded device wait gave up (status word set by the kernel) */
+  TEMPO_ERR_NONFINITE = -8    /* non-finite input detected by the validation pass */
+} tempo_status_t;
+
+/* ty_tempo_cfgs (src/module_mp_tempo_cfgs.F90:14-35); same field order and defaults
+ * as tempo_default_cfgs() returns.  Logicals are int 0/1. */
+typedef struct {
+  int aerosolaware_flag;          /* .true.  */
+  int hailaware_flag;             /* .true.  */
+  int ml_for_bl_nc_flag;          /* .false. */
+  int ml_for_nc_flag;             /* .false. */
+  int semi_sedi_flag;             /* .false. */
+  int refl10cm_from_melting_flag; /* .false. */
+  int turn_off_micro_flag;        /* .false. */
+  int cloud_condensation_flag;    /* .true.  */
+  int verbose;                    /* .false. */
+  int check_tables;               /* .false. */
+  char single_moment_nc_opt[32];  /* 'land' | 'ocean' | number in m^-3 */
+  int refl10cm_flag;              /* .true.  */
+  int re_cloud_flag;              /* .true.  */
+  int re_ice_flag;                /* .true.  */
+  int re_snow_flag;               /* .true.  */
+  int max_hail_diameter_flag;     /* .true.  */
+  int rain_med_vol_diam_flag;     /* .false. */
+  int graupel_med_vol_diam_flag;  /* .false. */
+  int cloud_number_mixing_ratio_flag; /* .false. */
+} tempo_cfgs_t;
+
+/* ty_tempo_driver_diags (src/module_mp_tempo_driver.F90:18-34).  Caller-owned,
+ * tile-shaped; NULL = not requested.  The element type follows the run call
+ * (double for *_c / *_dev_c, float for *_f32 variants); host pointers for the
+ * host-memory calls, device pointers for the *_dev_* calls. */
+typedef struct {
+  void *rain_precip, *ice_liquid_equiv_precip, *snow_liquid_equiv_precip,
+      *graupel_liquid_equiv_precip, *frozen_fraction, *frz_rain_precip,
+      *max_hail_diameter_sfc, *max_hail_diameter_column;           /* 2-D */
+  void *refl10cm, *re_cloud, *re_ice, *re_snow, *rain_med_vol_diam,
+      *graupel_med_vol_diam, *cloud_number_mixing_ratio;           /* 3-D */
+} tempo_diags_t;
+
+/* Arithmetic of the step kernels. */
+typedef enum {
+  TEMPO_PREC_FP64 = 0,  /* plain FP64 drop-in: every real is a double, no FMA contraction */
+  TEMPO_PREC_MIXED = 1  /* FP32 bulk; temperature/vapour state, saturation differences,
+                           sedimentation flux divergence and precipitation sums in FP64 */
+} tempo_precision_t;
+
+typedef struct tempo_ctx tempo_ctx_t;
+
+/* Library identification; never fails. */
+const char *tempo_version(void);
+/* Thread-local message of the last failing call ("" if none). */
+const char *tempo_last_error(void);
+/* Reference defaults of ty_tempo_cfgs (cfgs:15-34). */
+int tempo_default_cfgs(tempo_cfgs_t *cfgs);
+
+/* tempo_init (src/module_mp_tempo_driver.F90:42-182).  The eight flag arguments are
+ * the reference's optional logicals (NULL = not present); present ones are written
+ * into *tempo_cfgs.  table_dir holds ccn_activate.bin and, unless build_tables is
+ * nonzero, the three big-endian stream tables (qr_acr_qg_data_tempo_v3,
+ * qr_acr_qs_data_tempo_v3, freeze_water_data_tempo_v3).  build_tables != 0 builds
+ * the three tables on the GPU in FP64 instead of reading them (the reference builds
+ * them offline with tools/build_tables.F90).  device: CUDA ordinal.  On success
+ * *ctx receives a new context. */
+int tempo_init_c(const int *aerosolaware_flag, const int *hailaware_flag,
+                 const int *semi_sedi_flag, const int *cloud_condensation_flag,
+                 const int *refl10cm_from_melting_flag, const int *ml_for_bl_nc_flag,
+                 const int *ml_for_nc_flag, const int *force_init_flag,
+                 tempo_cfgs_t *tempo_cfgs, const char *table_dir, int build_tables,
+                 int device, tempo_ctx_t **ctx);
+
+/* Releases the context and its device memory. NULL is a no-op. */
+int tempo_ctx_destroy(tempo_ctx_t *ctx);
+
+/* Selects the kernel arithmetic for later run calls (default TEMPO_PREC_FP64). */
+int tempo_set_precision(tempo_ctx_t *ctx, int precision);
+
+/* tempo_run (src/module_mp_tempo_driver.F90:187-513) on host arrays of doubles (the
+ * reference's default kind_phys).  Copies the tile to the device, runs the step on
+ * the context's stream, copies results back and synchronises.  Optional arrays: t
+ * or (th and pii); nc, nwfa, nifa, ng, qb, land_input, qcfrac, qifrac and the *_bl /
+ * thten_* inputs (the latter are accepted and, as in the reference, unused).
+ * qc_bl with qcfrac_bl selects the reference's ML effective-radius path and returns
+ * TEMPO_ERR_UNSUPPORTED. */
+int tempo_run_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double dt, int itimestep,
+                double *t, double *th, const double *pii, const double *p, const double *w,
+                const double *dz, double *qv, double *qc, double *qr, double *qi, double *qs,
+                double *qg, double *ni, double *nr, double *nc, double *nwfa, double *nifa,
+                double *ng, double *qb, const double *qc_bl, const double *qcfrac_bl,
+                double *qcfrac, double *qifrac, const double *thten_bl, const double *qvten_bl,
+                const double *qcten_bl, const double *qiten_bl, const double *thten_lwrad,
+                const double *thten_swrad, const int *land_input, int ids, int ide, int jds,
+                int jde, int kds, int kde, int ims, int ime, int jms, int jme, int kms, int kme,
+                int its, int ite, int jts, int jte, int kts, int kte, tempo_diags_t *tempo_diags);
+
+/* Same as tempo_run_c for host arrays of floats (the reference built with
+ * -DSINGLE_PREC, src/machine.F90:13-17). */
+int tempo_run_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float dt, int itimestep,
+                    float *t, float *th, const float *pii, const float *p, const float *w,
+                    const float *dz, float *qv, float *qc, float *qr, float *qi, float *qs,
+                    float *qg, float *ni, float *nr, float *nc, float *nwfa, float *nifa,
+                    float *ng, float *qb, const int *land_input, int ims, int ime, int jms,
+                    int jme, int kms, int kme, int its, int ite, int jts, int jte, int kts,
+                    int kte, tempo_diags_t *tempo_diags);
+
+/* tempo_run on DEVICE arrays (doubles) already resident in HBM, enqueued on `stream`
+ * (a cudaStream_t); returns after enqueueing.  Same
+ * arguments as tempo_run_c minus the inert ones.  A NULL stream is the CUDA default
+ * stream, so the call orders with other work issued there. */
+int tempo_run_dev_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double dt,
+                    int itimestep, double *t, double *th, const double *pii, const double *p,
+                    const double *w, const double *dz, double *qv, double *qc, double *qr,
+                    double *qi, double *qs, double *qg, double *ni, double *nr, double *nc,
+                    double *nwfa, double *nifa, double *ng, double *qb, const int *land_input,
+                    int ims, int ime, int jms, int jme, int kms, int kme, int its, int ite,
+                    int jts, int jte, int kts, int kte, tempo_diags_t *tempo_diags,
+                    void *stream);
+
+/* tempo_run on DEVICE arrays of floats (FP32 storage). */
+int tempo_run_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float dt,
+                        int itimestep, float *t, float *th, const float *pii, const float *p,
+                        const float *w, const float *dz, float *qv, float *qc, float *qr,
+                        float *qi, float *qs, float *qg, float *ni, float *nr, float *nc,
+                        float *nwfa, float *nifa, float *ng, float *qb, const int *land_input,
+                        int ims, int ime, int jms, int jme, int kms, int kme, int its, int ite,
+                        int jts, int jte, int kts, int kte, tempo_diags_t *tempo_diags,
+                        void *stream);
+
+/* tempo_aerosol_surface_emissions (src/module_mp_tempo_driver.F90:516-529) on device
+ * arrays: nwfa(i,kts,j) += nwfa2d(i,j)*dt over the memory range. */
+int tempo_aerosol_surface_emissions_dev_c(tempo_ctx_t *ctx, double dt, double *nwfa,
+                                          const double *nwfa2d, int ims, int ime, int jms,
+                                          int jme, int kms, int kme, int kts, void *stream);
+
+/* Table export/import in the reference's file formats (big-endian stream FP64,
+ * src/module_mp_tempo_tables.F90:96-444, read back by driver:532-622).  name is one
+ * of "qr_acr_qg", "qr_acr_qs", "freezewater". */
+int tempo_write_table_c(tempo_ctx_t *ctx, const char *name, const char *path);
+
+/* Copies a lookup table or derived constant array from the context to host memory in
+ * the reference's Fortran order (e.g. "tcg_racg", "t_efrw", "tnc_wev", "tpi_ide").
+ * count is the element count of host_out (doubles); *needed receives the size. */
+int tempo_get_table_c(tempo_ctx_t *ctx, const char *name, double *host_out, long count,
+                      long *needed);
+
+/* Rebuilds the three large tables on the GPU in FP64 (tables.F90:493-805 semantics)
+ * and reports the device time in milliseconds. */
+int tempo_build_tables_c(tempo_ctx_t *ctx, float *elapsed_ms);
+
+/* Per-call counters of the last run on this context: [0] columns, [1] early-exit
+ * columns, [2..6] max sedimentation substeps rain/graupel/snow/ice/cloud, [7]
+ * kernel launches. */
+int tempo_last_stats_c(tempo_ctx_t *ctx, long out[8]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

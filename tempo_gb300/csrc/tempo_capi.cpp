@@ -1,0 +1,820 @@
+// tempo_capi.cpp -- the C ABI of libtempo_gb300 (declared in include/tempo_gb300.h).
+//
+// Host side of the drop-in: tempo_init (src/module_mp_tempo_driver.F90:42-182) builds a
+// context that owns the device lookup tables; tempo_run (driver:187-513) validates
+// the reference's argument list, sets up the column-step launch and, for host
+// arrays, stages the tile through HBM.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tempo_gb300.h"
+#include "tempo_internal.h"
+#include "tempo_types.h"
+
+using namespace tg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+#define CUDA_TRY(expr)                                                                    \
+  do {                                                                                    \
+    cudaError_t e_ = (expr);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(TEMPO_ERR_CUDA, "%s failed: %s", #expr, cudaGetErrorString(e_));      \
+  } while (0)
+
+template <class T>
+int dev_alloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) return TEMPO_OK;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fail(TEMPO_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T),
+                cudaGetErrorString(e));
+  }
+  return TEMPO_OK;
+}
+
+// host staging buffers reused across host-memory run calls
+struct Mirror {
+  void* d = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct tempo_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  tempo_cfgs_t cfgs{};
+  bool hail = true;
+  int precision = TEMPO_PREC_FP64;
+  TempoConsts<double> c64{};
+  TempoConsts<float> c32{};
+  TempoBins bins{};
+  DevTables64 t64{};
+  // FP32 copies for the mixed kernels
+  float *f_efrw = nullptr, *f_efsw = nullptr, *f_tnc_wev = nullptr, *f_tps = nullptr,
+        *f_tni = nullptr, *f_tpi = nullptr, *f_qg = nullptr, *f_qs = nullptr, *f_qrfz = nullptr,
+        *f_qcfz = nullptr;
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  unsigned long long* d_stats = nullptr;
+  long last_cols = 0;
+  long launches = 0;
+  std::vector<Mirror> mirrors;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+void free_tables(tempo_ctx* c) {
+  double* d[] = {c->t64.t_efrw, c->t64.t_efsw, c->t64.tpc_wev, c->t64.tnc_wev, c->t64.tps_iaus,
+                 c->t64.tni_iaus, c->t64.tpi_ide, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
+  for (double* p : d) cudaFree(p);
+  cudaFree(c->t64.tnccn);
+  float* f[] = {c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
+                c->f_qg,   c->f_qs,   c->f_qrfz,    c->f_qcfz};
+  for (float* p : f) cudaFree(p);
+  c->t64 = DevTables64{};
+}
+
+int alloc_tables(tempo_ctx* c) {
+  int rc;
+  DevTables64& t = c->t64;
+  if ((rc = dev_alloc(&t.t_efrw, (size_t)nbr * nbc))) return rc;
+  if ((rc = dev_alloc(&t.t_efsw, (size_t)nbs * nbc))) return rc;
+  if ((rc = dev_alloc(&t.tpc_wev, (size_t)nbc * ntb_c * nbc))) return rc;
+  if ((rc = dev_alloc(&t.tnc_wev, (size_t)nbc * ntb_c * nbc))) return rc;
+  if ((rc = dev_alloc(&t.tps_iaus, (size_t)ntb_i * ntb_i1))) return rc;
+  if ((rc = dev_alloc(&t.tni_iaus, (size_t)ntb_i * ntb_i1))) return rc;
+  if ((rc = dev_alloc(&t.tpi_ide, (size_t)ntb_i * ntb_i1))) return rc;
+  if ((rc = dev_alloc(&t.qg, (size_t)QG_COUNT * 5))) return rc;
+  if ((rc = dev_alloc(&t.qs, (size_t)QS_COUNT * 12))) return rc;
+  if ((rc = dev_alloc(&t.qrfz, (size_t)QRFZ_COUNT * 4))) return rc;
+  if ((rc = dev_alloc(&t.qcfz, (size_t)QCFZ_COUNT * 2))) return rc;
+  if ((rc = dev_alloc(&t.tnccn, (size_t)CCN_COUNT))) return rc;
+  return TEMPO_OK;
+}
+
+int make_f32_tables(tempo_ctx* c) {
+  struct P {
+    float** f;
+    const double* d;
+    long n;
+  } ps[] = {{&c->f_efrw, c->t64.t_efrw, (long)nbr * nbc},
+            {&c->f_efsw, c->t64.t_efsw, (long)nbs * nbc},
+            {&c->f_tnc_wev, c->t64.tnc_wev, (long)nbc * ntb_c * nbc},
+            {&c->f_tps, c->t64.tps_iaus, (long)ntb_i * ntb_i1},
+            {&c->f_tni, c->t64.tni_iaus, (long)ntb_i * ntb_i1},
+            {&c->f_tpi, c->t64.tpi_ide, (long)ntb_i * ntb_i1},
+            {&c->f_qg, c->t64.qg, QG_COUNT * 5},
+            {&c->f_qs, c->t64.qs, QS_COUNT * 12},
+            {&c->f_qrfz, c->t64.qrfz, QRFZ_COUNT * 4},
+            {&c->f_qcfz, c->t64.qcfz, QCFZ_COUNT * 2}};
+  for (auto& p : ps) {
+    if (!*p.f) {
+      int rc = dev_alloc(p.f, (size_t)p.n);
+      if (rc) return rc;
+    }
+    CUDA_TRY(narrow_copy(*p.f, p.d, p.n, c->stream));
+  }
+  return TEMPO_OK;
+}
+
+bool host_little() {
+  uint16_t x = 1;
+  return *(uint8_t*)&x == 1;
+}
+void bswap8(void* p, size_t n) {
+  uint8_t* b = (uint8_t*)p;
+  for (size_t i = 0; i < n; i++, b += 8)
+    for (int k = 0; k < 4; k++) {
+      uint8_t t = b[k];
+      b[k] = b[7 - k];
+      b[7 - k] = t;
+    }
+}
+
+std::string join(const char* dir, const char* name) {
+  std::string s = dir ? dir : ".";
+  if (!s.empty() && s.back() != '/') s += '/';
+  return s + name;
+}
+
+// read_table_ccn (driver:625-649): Fortran sequential unformatted, big-endian FP32,
+// one record of 8820 values between 4-byte length markers.
+int read_ccn(tempo_ctx* c, const char* dir) {
+  std::string path = join(dir, "ccn_activate.bin");
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return fail(TEMPO_ERR_TABLE, "cannot open %s", path.c_str());
+  std::vector<uint8_t> buf(CCN_COUNT * 4 + 8);
+  size_t got = std::fread(buf.data(), 1, buf.size(), f);
+  int extra = std::fgetc(f);
+  std::fclose(f);
+  if (got != buf.size() || extra != EOF)
+    return fail(TEMPO_ERR_TABLE, "%s has the wrong size (expected %zu bytes)", path.c_str(), buf.size());
+  uint32_t m0 = (uint32_t)buf[0] << 24 | (uint32_t)buf[1] << 16 | (uint32_t)buf[2] << 8 | buf[3];
+  if (m0 != (uint32_t)(CCN_COUNT * 4) || std::memcmp(buf.data(), buf.data() + buf.size() - 4, 4))
+    return fail(TEMPO_ERR_TABLE, "%s: bad record markers", path.c_str());
+  std::vector<float> v(CCN_COUNT);
+  for (long i = 0; i < CCN_COUNT; i++) {
+    const uint8_t* b = buf.data() + 4 + 4 * i;
+    uint32_t u = (uint32_t)b[0] << 24 | (uint32_t)b[1] << 16 | (uint32_t)b[2] << 8 | b[3];
+    std::memcpy(&v[i], &u, 4);
+    if (!std::isfinite(v[i]) || v[i] < 0.f || v[i] > 1.f)
+      return fail(TEMPO_ERR_TABLE, "%s: activated fraction out of [0,1] at %ld", path.c_str(), i);
+  }
+  CUDA_TRY(cudaMemcpy(c->t64.tnccn, v.data(), CCN_COUNT * 4, cudaMemcpyHostToDevice));
+  return TEMPO_OK;
+}
+
+// A big-endian FP64 stream table family: `narr` arrays of `counts[a]` doubles that
+// land in AoS family `fam` (nfam wide) at slot `slot[a]`.
+struct Family {
+  const char* file;
+  int narr;
+  const long* counts;
+  double** aos;  // per array: AoS destination base
+  const int* nfam;
+  const int* slot;
+};
+
+int read_stream_table(tempo_ctx* c, const std::string& path, int narr, const long* counts,
+                      double* const* aos, const int* nfam, const int* slot) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return fail(TEMPO_ERR_TABLE, "cannot open %s", path.c_str());
+  long total = 0;
+  for (int a = 0; a < narr; a++) total += counts[a];
+  std::fseek(f, 0, SEEK_END);
+  long size = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  if (size != total * 8) {
+    std::fclose(f);
+    return fail(TEMPO_ERR_TABLE, "%s has a size of %ld bytes but the table needs %ld bytes",
+                path.c_str(), size, total * 8);
+  }
+  std::vector<double> host;
+  double* dtmp = nullptr;
+  long maxc = 0;
+  for (int a = 0; a < narr; a++) maxc = counts[a] > maxc ? counts[a] : maxc;
+  if (int rc = dev_alloc(&dtmp, (size_t)maxc)) {
+    std::fclose(f);
+    return rc;
+  }
+  for (int a = 0; a < narr; a++) {
+    host.resize(counts[a]);
+    if ((long)std::fread(host.data(), 8, counts[a], f) != counts[a]) {
+      std::fclose(f);
+      cudaFree(dtmp);
+      return fail(TEMPO_ERR_TABLE, "%s: short read", path.c_str());
+    }
+    if (host_little()) bswap8(host.data(), counts[a]);
+    for (long i = 0; i < counts[a]; i++)
+      if (!std::isfinite(host[i]) || host[i] < 0.0) {
+        std::fclose(f);
+        cudaFree(dtmp);
+        return fail(TEMPO_ERR_TABLE, "%s: array %d entry %ld is negative or not finite",
+                    path.c_str(), a, i);
+      }
+    cudaError_t e = cudaMemcpy(dtmp, host.data(), counts[a] * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = aos_scatter(aos[a], dtmp, counts[a], nfam[a], slot[a], c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+      std::fclose(f);
+      cudaFree(dtmp);
+      return fail(TEMPO_ERR_CUDA, "table upload: %s", cudaGetErrorString(e));
+    }
+  }
+  std::fclose(f);
+  cudaFree(dtmp);
+  return TEMPO_OK;
+}
+
+// reference file order of each family (tables.F90:122-127, 298-309, 438-442)
+const long kFzCounts[6] = {QRFZ_COUNT, QRFZ_COUNT, QRFZ_COUNT, QRFZ_COUNT, QCFZ_COUNT, QCFZ_COUNT};
+const int kFzNfam[6] = {4, 4, 4, 4, 2, 2};
+const int kFzSlot[6] = {0, 1, 2, 3, 0, 1};  // tpi_qrfz tni_qrfz tpg_qrfz tnr_qrfz | tpi_qcfz tni_qcfz
+const long kQsCounts[12] = {QS_COUNT, QS_COUNT, QS_COUNT, QS_COUNT, QS_COUNT, QS_COUNT,
+                            QS_COUNT, QS_COUNT, QS_COUNT, QS_COUNT, QS_COUNT, QS_COUNT};
+const int kQsNfam[12] = {12, 12, 12, 12, 12, 12, 12, 12, 12, 12, 12, 12};
+const int kQsSlot[12] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11};
+const long kQgCounts[5] = {QG_COUNT, QG_COUNT, QG_COUNT, QG_COUNT, QG_COUNT};
+const int kQgNfam[5] = {5, 5, 5, 5, 5};
+const int kQgSlot[5] = {0, 1, 2, 3, 4};
+
+int read_big_tables(tempo_ctx* c, const char* dir) {
+  double* fz[6] = {c->t64.qrfz, c->t64.qrfz, c->t64.qrfz, c->t64.qrfz, c->t64.qcfz, c->t64.qcfz};
+  int rc = read_stream_table(c, join(dir, "freeze_water_data_tempo_v3"), 6, kFzCounts, fz, kFzNfam,
+                             kFzSlot);
+  if (rc) return rc;
+  double* qs[12];
+  for (int a = 0; a < 12; a++) qs[a] = c->t64.qs;
+  rc = read_stream_table(c, join(dir, "qr_acr_qs_data_tempo_v3"), 12, kQsCounts, qs, kQsNfam, kQsSlot);
+  if (rc) return rc;
+  double* qg[5];
+  for (int a = 0; a < 5; a++) qg[a] = c->t64.qg;
+  return read_stream_table(c, join(dir, "qr_acr_qg_data_tempo_v3"), 5, kQgCounts, qg, kQgNfam, kQgSlot);
+}
+
+int build_tables_gpu(tempo_ctx* c, float* ms) {
+  TempoConsts<double> hc;
+  make_consts(&hc, true);  // tables are always built hail-aware (tables.F90:31,50)
+  double* work = nullptr;
+  if (int rc = dev_alloc(&work, big_tables_work_bytes() / sizeof(double))) return rc;
+  CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+  cudaError_t e = build_big_tables(c->t64, c->bins, hc, work, big_tables_work_bytes(), c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(work);
+  if (e != cudaSuccess) return fail(TEMPO_ERR_CUDA, "table build: %s", cudaGetErrorString(e));
+  if (ms) cudaEventElapsedTime(ms, c->ev0, c->ev1);
+  return TEMPO_OK;
+}
+
+// single_moment_nc_opt (cfgs:50-73): 'land' | 'ocean' | a number; typos fall back to land
+double resolve_nc_value(const tempo_cfgs_t* cfg) {
+  char buf[33];
+  std::memcpy(buf, cfg->single_moment_nc_opt, 32);
+  buf[32] = 0;
+  char* s = buf;
+  while (*s == ' ') s++;
+  for (int i = (int)std::strlen(s) - 1; i >= 0 && (s[i] == ' ' || s[i] == 0); i--) s[i] = 0;
+  if (!std::strcmp(s, "land")) return nt_c_l;
+  if (!std::strcmp(s, "ocean")) return nt_c_o;
+  char* end = nullptr;
+  double v = std::strtod(s, &end);
+  if (end == s) return nt_c_l;
+  return v;
+}
+
+int ensure_scratch(tempo_ctx* c, size_t bytes) {
+  if (bytes <= c->scratch_bytes) return TEMPO_OK;
+  cudaFree(c->scratch);
+  c->scratch = nullptr;
+  c->scratch_bytes = 0;
+  cudaError_t e = cudaMalloc(&c->scratch, bytes);
+  if (e != cudaSuccess)
+    return fail(TEMPO_ERR_NOMEM, "scratch of %zu bytes: %s", bytes, cudaGetErrorString(e));
+  c->scratch_bytes = bytes;
+  return TEMPO_OK;
+}
+
+struct Bounds {
+  int ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte;
+};
+
+int check_bounds(const Bounds& b) {
+  if (b.ime < b.ims || b.jme < b.jms || b.kme < b.kms)
+    return fail(TEMPO_ERR_ARG, "empty memory bounds");
+  if (b.its < b.ims || b.ite > b.ime || b.jts < b.jms || b.jte > b.jme || b.kts < b.kms || b.kte > b.kme)
+    return fail(TEMPO_ERR_ARG, "tile (%d:%d,%d:%d,%d:%d) outside memory (%d:%d,%d:%d,%d:%d)", b.its,
+                b.ite, b.kts, b.kte, b.jts, b.jte, b.ims, b.ime, b.kms, b.kme, b.jms, b.jme);
+  if (b.kte - b.kts + 1 < 2) return fail(TEMPO_ERR_ARG, "a column needs at least 2 levels");
+  return TEMPO_OK;
+}
+
+template <class S>
+struct RunArrays {
+  S *t, *th;
+  const S *pii, *p, *w, *dz;
+  S *qv, *qc, *qr, *qi, *qs, *qg, *ni, *nr, *nc, *nwfa, *nifa, *ng, *qb;
+  const int* land;
+};
+
+// Validates the argument list and launches the step on device arrays.
+template <class S>
+int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, const RunArrays<S>& A,
+            const Bounds& b, const tempo_diags_t* dg, cudaStream_t s) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (!cfg) return fail(TEMPO_ERR_ARG, "NULL tempo_cfgs");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(TEMPO_ERR_ARG, "dt must be > 0 (got %g)", dt);
+  if (int rc = check_bounds(b)) return rc;
+  if (!A.p || !A.w || !A.dz || !A.qv || !A.qc || !A.qr || !A.qi || !A.qs || !A.qg || !A.ni || !A.nr)
+    return fail(TEMPO_ERR_ARG, "a required array (p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr) is NULL");
+  if (!A.t && !(A.th && A.pii))
+    return fail(TEMPO_ERR_ARG, "tempo_run requires either t or th and pii");
+  if (cfg->semi_sedi_flag)
+    return fail(TEMPO_ERR_UNSUPPORTED, "semi-Lagrangian sedimentation is not part of this build");
+  if (cfg->refl10cm_from_melting_flag)
+    return fail(TEMPO_ERR_UNSUPPORTED, "melting-layer reflectivity is not part of this build");
+  if (cfg->ml_for_nc_flag && !A.nc)
+    return fail(TEMPO_ERR_UNSUPPORTED, "ML cloud-number prediction is not part of this build");
+  uint32_t f = 0;
+  if (A.nc) f |= F_NC;
+  if (A.nwfa) f |= F_NWFA;
+  if (A.nifa) f |= F_NIFA;
+  if (A.ng && A.qb) f |= F_HAIL;
+  if (A.qb) f |= F_QB;
+  if (A.land) f |= F_LAND;
+  if (itimestep == 1) f |= F_FIRST;
+  if (cfg->turn_off_micro_flag) f |= F_NOMICRO;
+  if (cfg->cloud_condensation_flag) f |= F_COND;
+  if (cfg->refl10cm_flag) f |= F_REFL;
+  if (cfg->re_cloud_flag && cfg->re_ice_flag && cfg->re_snow_flag) f |= F_RE;
+  if (cfg->max_hail_diameter_flag) f |= F_MHD;
+  if (cfg->rain_med_vol_diam_flag) f |= F_MVDR;
+  if (cfg->graupel_med_vol_diam_flag) f |= F_MVDG;
+  if (cfg->cloud_number_mixing_ratio_flag) f |= F_NCMR;
+  if (A.t) f |= F_USE_T;
+  if (dt > timestep_conversion_rime_to_rain) f |= F_DT_RIME;
+
+  StepArgs<S> a{};
+  a.t = A.t;
+  a.th = A.th;
+  a.pii = A.pii;
+  a.p = A.p;
+  a.w = A.w;
+  a.dz = A.dz;
+  a.qv = A.qv;
+  a.qc = A.qc;
+  a.qr = A.qr;
+  a.qi = A.qi;
+  a.qs = A.qs;
+  a.qg = A.qg;
+  a.ni = A.ni;
+  a.nr = A.nr;
+  a.nc = A.nc;
+  a.nwfa = A.nwfa;
+  a.nifa = A.nifa;
+  a.ng = A.ng;
+  a.qb = A.qb;
+  a.land = A.land;
+  if (dg) {
+    a.rain_precip = (S*)dg->rain_precip;
+    a.ice_precip = (S*)dg->ice_liquid_equiv_precip;
+    a.snow_precip = (S*)dg->snow_liquid_equiv_precip;
+    a.graupel_precip = (S*)dg->graupel_liquid_equiv_precip;
+    a.frozen_fraction = (S*)dg->frozen_fraction;
+    a.frz_rain = (S*)dg->frz_rain_precip;
+    if (cfg->max_hail_diameter_flag) {
+      a.mhd_sfc = (S*)dg->max_hail_diameter_sfc;
+      a.mhd_col = (S*)dg->max_hail_diameter_column;
+    }
+    if (cfg->refl10cm_flag) a.refl10cm = (S*)dg->refl10cm;
+    if (cfg->re_cloud_flag) a.re_cloud = (S*)dg->re_cloud;
+    if (cfg->re_ice_flag) a.re_ice = (S*)dg->re_ice;
+    if (cfg->re_snow_flag) a.re_snow = (S*)dg->re_snow;
+    if (cfg->rain_med_vol_diam_flag) a.mvd_r = (S*)dg->rain_med_vol_diam;
+    if (cfg->graupel_med_vol_diam_flag) a.mvd_g = (S*)dg->graupel_med_vol_diam;
+    if (cfg->cloud_number_mixing_ratio_flag) a.ncmr = (S*)dg->cloud_number_mixing_ratio;
+  }
+  a.NI = (long)b.ime - b.ims + 1;
+  a.NK = (long)b.kme - b.kms + 1;
+  a.i0 = b.its - b.ims;
+  a.k0 = b.kts - b.kms;
+  a.j0 = b.jts - b.jms;
+  a.ti = b.ite - b.its + 1;
+  a.tj = b.jte - b.jts + 1;
+  a.nz = b.kte - b.kts + 1;
+  a.ncol = (long)a.ti * a.tj;
+  a.ncol_pad = (a.ncol + 31) / 32 * 32;
+  a.dt = dt;
+  a.nc_single = resolve_nc_value(cfg);
+  a.flags = f;
+  const bool mixed = c->precision == TEMPO_PREC_MIXED;
+  const size_t rsz = mixed ? sizeof(float) : sizeof(double);
+  const size_t sd_bytes = (size_t)SD_N * a.nz * a.ncol_pad * sizeof(double);
+  const size_t sr_bytes = (size_t)SR_N * a.nz * a.ncol_pad * rsz;
+  if (int rc = ensure_scratch(c, sd_bytes + sr_bytes + 256)) return rc;
+  a.sd = (double*)c->scratch;
+  a.sr = (void*)((char*)c->scratch + (sd_bytes + 255) / 256 * 256);
+  a.stats = c->d_stats;
+  CUDA_TRY(cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s));
+  c->last_cols = a.ncol;
+  c->launches = 1;
+  if (!mixed) {
+    if constexpr (sizeof(S) == sizeof(double)) {
+      Tables<double> T{c->t64.t_efrw, c->t64.t_efsw, c->t64.tnc_wev, c->t64.tps_iaus, c->t64.tni_iaus,
+                       c->t64.tpi_ide, c->t64.tnccn, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
+      CUDA_TRY(launch_step_f64(a, T, c->c64, s));
+      return TEMPO_OK;
+    } else {
+      return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
+    }
+  }
+  Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
+                  c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
+  if constexpr (sizeof(S) == sizeof(double))
+    CUDA_TRY(launch_step_mixed_f64(a, T, c->c32, c->c64, s));
+  else
+    CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->c64, s));
+  return TEMPO_OK;
+}
+
+// Stages host arrays through device mirrors (whole memory extent), runs, copies back.
+template <class S>
+int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, const RunArrays<S>& H,
+             const Bounds& b, tempo_diags_t* dg) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (int rc = check_bounds(b)) return rc;
+  const size_t n3 = (size_t)(b.ime - b.ims + 1) * (b.kme - b.kms + 1) * (b.jme - b.jms + 1);
+  const size_t n2 = (size_t)(b.ime - b.ims + 1) * (b.jme - b.jms + 1);
+  const size_t t2 = (size_t)(b.ite - b.its + 1) * (b.jte - b.jts + 1);
+  const size_t t3 = t2 * (b.kte - b.kts + 1);
+  struct Slot {
+    const void* h;
+    size_t bytes;
+    bool out;
+  };
+  const S* in3[] = {H.t, H.th, H.pii, H.p, H.w, H.dz, H.qv, H.qc, H.qr, H.qi, H.qs, H.qg,
+                    H.ni, H.nr, H.nc, H.nwfa, H.nifa, H.ng, H.qb};
+  const bool out3[] = {true, true, false, false, false, false, true, true, true, true, true,
+                       true, true, true, true, true, true, true, true};
+  const int n_in = 19;
+  void* dg_h[15] = {dg ? dg->rain_precip : nullptr, dg ? dg->ice_liquid_equiv_precip : nullptr,
+                    dg ? dg->snow_liquid_equiv_precip : nullptr,
+                    dg ? dg->graupel_liquid_equiv_precip : nullptr,
+                    dg ? dg->frozen_fraction : nullptr, dg ? dg->frz_rain_precip : nullptr,
+                    dg ? dg->max_hail_diameter_sfc : nullptr,
+                    dg ? dg->max_hail_diameter_column : nullptr, dg ? dg->refl10cm : nullptr,
+                    dg ? dg->re_cloud : nullptr, dg ? dg->re_ice : nullptr,
+                    dg ? dg->re_snow : nullptr, dg ? dg->rain_med_vol_diam : nullptr,
+                    dg ? dg->graupel_med_vol_diam : nullptr,
+                    dg ? dg->cloud_number_mixing_ratio : nullptr};
+  const int nslots = n_in + 1 + 15;
+  if (c->mirrors.size() < (size_t)nslots) c->mirrors.resize(nslots);
+  void* d[nslots];
+  for (int i = 0; i < nslots; i++) {
+    const void* h;
+    size_t bytes;
+    if (i < n_in) {
+      h = in3[i];
+      bytes = n3 * sizeof(S);
+    } else if (i == n_in) {
+      h = H.land;
+      bytes = n2 * sizeof(int);
+    } else {
+      h = dg_h[i - n_in - 1];
+      bytes = ((i - n_in - 1) < 8 ? t2 : t3) * sizeof(S);
+    }
+    d[i] = nullptr;
+    if (!h) continue;
+    Mirror& m = c->mirrors[i];
+    if (m.bytes < bytes) {
+      cudaFree(m.d);
+      m.d = nullptr;
+      m.bytes = 0;
+      cudaError_t e = cudaMalloc(&m.d, bytes);
+      if (e != cudaSuccess)
+        return fail(TEMPO_ERR_NOMEM, "device mirror of %zu bytes: %s", bytes, cudaGetErrorString(e));
+      m.bytes = bytes;
+    }
+    d[i] = m.d;
+    if (i <= n_in) CUDA_TRY(cudaMemcpyAsync(d[i], h, bytes, cudaMemcpyHostToDevice, c->stream));
+  }
+  RunArrays<S> D{(S*)d[0],  (S*)d[1],  (const S*)d[2], (const S*)d[3], (const S*)d[4],
+                 (const S*)d[5], (S*)d[6],  (S*)d[7],  (S*)d[8],  (S*)d[9],
+                 (S*)d[10], (S*)d[11], (S*)d[12], (S*)d[13], (S*)d[14],
+                 (S*)d[15], (S*)d[16], (S*)d[17], (S*)d[18], (const int*)d[n_in]};
+  tempo_diags_t ddg{};
+  void** ddp[15] = {&ddg.rain_precip, &ddg.ice_liquid_equiv_precip, &ddg.snow_liquid_equiv_precip,
+                    &ddg.graupel_liquid_equiv_precip, &ddg.frozen_fraction, &ddg.frz_rain_precip,
+                    &ddg.max_hail_diameter_sfc, &ddg.max_hail_diameter_column, &ddg.refl10cm,
+                    &ddg.re_cloud, &ddg.re_ice, &ddg.re_snow, &ddg.rain_med_vol_diam,
+                    &ddg.graupel_med_vol_diam, &ddg.cloud_number_mixing_ratio};
+  for (int i = 0; i < 15; i++) *ddp[i] = d[n_in + 1 + i];
+  int rc = run_dev(c, cfg, dt, itimestep, D, b, &ddg, c->stream);
+  if (rc) return rc;
+  for (int i = 0; i < n_in; i++)
+    if (d[i] && out3[i])
+      CUDA_TRY(cudaMemcpyAsync((void*)in3[i], d[i], n3 * sizeof(S), cudaMemcpyDeviceToHost, c->stream));
+  for (int i = 0; i < 15; i++)
+    if (d[n_in + 1 + i])
+      CUDA_TRY(cudaMemcpyAsync(dg_h[i], d[n_in + 1 + i], (i < 8 ? t2 : t3) * sizeof(S),
+                               cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return TEMPO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tempo_version(void) { return "tempo_gb300 1.0 (TEMPO v3.1.1 column step, sm_103a)"; }
+const char* tempo_last_error(void) { return g_err.c_str(); }
+
+int tempo_default_cfgs(tempo_cfgs_t* c) {
+  if (!c) return fail(TEMPO_ERR_ARG, "NULL cfgs");
+  std::memset(c, 0, sizeof *c);
+  c->aerosolaware_flag = 1;
+  c->hailaware_flag = 1;
+  c->cloud_condensation_flag = 1;
+  std::strcpy(c->single_moment_nc_opt, "land");
+  c->refl10cm_flag = 1;
+  c->re_cloud_flag = 1;
+  c->re_ice_flag = 1;
+  c->re_snow_flag = 1;
+  c->max_hail_diameter_flag = 1;
+  return TEMPO_OK;
+}
+
+int tempo_init_c(const int* aerosolaware_flag, const int* hailaware_flag, const int* semi_sedi_flag,
+                 const int* cloud_condensation_flag, const int* refl10cm_from_melting_flag,
+                 const int* ml_for_bl_nc_flag, const int* ml_for_nc_flag, const int* force_init_flag,
+                 tempo_cfgs_t* cfgs, const char* table_dir, int build_tables, int device,
+                 tempo_ctx_t** out) {
+  (void)force_init_flag;  // every context initialises its own tables
+  if (!cfgs || !out) return fail(TEMPO_ERR_ARG, "tempo_cfgs and ctx must not be NULL");
+  *out = nullptr;
+  if (aerosolaware_flag) cfgs->aerosolaware_flag = *aerosolaware_flag != 0;
+  if (hailaware_flag) cfgs->hailaware_flag = *hailaware_flag != 0;
+  if (ml_for_bl_nc_flag) cfgs->ml_for_bl_nc_flag = *ml_for_bl_nc_flag != 0;
+  if (ml_for_nc_flag) cfgs->ml_for_nc_flag = *ml_for_nc_flag != 0;
+  if (semi_sedi_flag) cfgs->semi_sedi_flag = *semi_sedi_flag != 0;
+  if (cloud_condensation_flag) cfgs->cloud_condensation_flag = *cloud_condensation_flag != 0;
+  if (refl10cm_from_melting_flag) cfgs->refl10cm_from_melting_flag = *refl10cm_from_melting_flag != 0;
+
+  tempo_ctx* c = new (std::nothrow) tempo_ctx();
+  if (!c) return fail(TEMPO_ERR_NOMEM, "context allocation failed");
+  auto bail = [&](int rc) {
+    tempo_ctx_destroy(c);
+    return rc;
+  };
+  c->device = device;
+  c->cfgs = *cfgs;
+  c->hail = cfgs->hailaware_flag != 0;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return bail(fail(TEMPO_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e)));
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess)
+    return bail(fail(TEMPO_ERR_CUDA, "stream/event creation: %s", cudaGetErrorString(e)));
+  make_consts(&c->c64, c->hail);
+  narrow_consts(c->c64, &c->c32);
+  make_bins(&c->bins);
+  int rc;
+  if ((rc = alloc_tables(c))) return bail(rc);
+  if ((rc = dev_alloc(&c->d_stats, 8))) return bail(rc);
+  e = build_small_tables(c->t64, c->bins, c->c64, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return bail(fail(TEMPO_ERR_CUDA, "small tables: %s", cudaGetErrorString(e)));
+  if ((rc = read_ccn(c, table_dir))) return bail(rc);
+  if (build_tables) {
+    if ((rc = build_tables_gpu(c, nullptr))) return bail(rc);
+  } else {
+    if ((rc = read_big_tables(c, table_dir))) return bail(rc);
+  }
+  if ((rc = make_f32_tables(c))) return bail(rc);
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return bail(fail(TEMPO_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
+  *out = c;
+  return TEMPO_OK;
+}
+
+int tempo_ctx_destroy(tempo_ctx_t* c) {
+  if (!c) return TEMPO_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_tables(c);
+  cudaFree(c->scratch);
+  cudaFree(c->d_stats);
+  for (auto& m : c->mirrors) cudaFree(m.d);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return TEMPO_OK;
+}
+
+int tempo_set_precision(tempo_ctx_t* c, int precision) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (precision != TEMPO_PREC_FP64 && precision != TEMPO_PREC_MIXED)
+    return fail(TEMPO_ERR_ARG, "unknown precision %d", precision);
+  c->precision = precision;
+  return TEMPO_OK;
+}
+
+int tempo_run_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, double dt, int itimestep, double* t,
+                double* th, const double* pii, const double* p, const double* w, const double* dz,
+                double* qv, double* qc, double* qr, double* qi, double* qs, double* qg, double* ni,
+                double* nr, double* nc, double* nwfa, double* nifa, double* ng, double* qb,
+                const double* qc_bl, const double* qcfrac_bl, double* qcfrac, double* qifrac,
+                const double* thten_bl, const double* qvten_bl, const double* qcten_bl,
+                const double* qiten_bl, const double* thten_lwrad, const double* thten_swrad,
+                const int* land_input, int ids, int ide, int jds, int jde, int kds, int kde, int ims,
+                int ime, int jms, int jme, int kms, int kme, int its, int ite, int jts, int jte,
+                int kts, int kte, tempo_diags_t* diags) {
+  (void)qcfrac; (void)qifrac; (void)thten_bl; (void)qvten_bl; (void)qcten_bl; (void)qiten_bl;
+  (void)thten_lwrad; (void)thten_swrad; (void)ids; (void)ide; (void)jds; (void)jde; (void)kds; (void)kde;
+  if (qc_bl && qcfrac_bl)
+    return fail(TEMPO_ERR_UNSUPPORTED, "the ML boundary-layer cloud path (qc_bl, qcfrac_bl) is not part of this build");
+  if (c && c->precision != TEMPO_PREC_FP64 && c->precision != TEMPO_PREC_MIXED)
+    return fail(TEMPO_ERR_STATE, "bad precision");
+  RunArrays<double> H{t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb, land_input};
+  return run_host(c, cfg, dt, itimestep, H, Bounds{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte}, diags);
+}
+
+int tempo_run_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, int itimestep, float* t,
+                    float* th, const float* pii, const float* p, const float* w, const float* dz,
+                    float* qv, float* qc, float* qr, float* qi, float* qs, float* qg, float* ni,
+                    float* nr, float* nc, float* nwfa, float* nifa, float* ng, float* qb,
+                    const int* land_input, int ims, int ime, int jms, int jme, int kms, int kme,
+                    int its, int ite, int jts, int jte, int kts, int kte, tempo_diags_t* diags) {
+  RunArrays<float> H{t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb, land_input};
+  return run_host(c, cfg, (double)dt, itimestep, H, Bounds{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte}, diags);
+}
+
+int tempo_run_dev_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, double dt, int itimestep, double* t,
+                    double* th, const double* pii, const double* p, const double* w,
+                    const double* dz, double* qv, double* qc, double* qr, double* qi, double* qs,
+                    double* qg, double* ni, double* nr, double* nc, double* nwfa, double* nifa,
+                    double* ng, double* qb, const int* land_input, int ims, int ime, int jms,
+                    int jme, int kms, int kme, int its, int ite, int jts, int jte, int kts, int kte,
+                    tempo_diags_t* diags, void* stream) {
+  RunArrays<double> A{t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb, land_input};
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the default stream
+  return run_dev(c, cfg, dt, itimestep, A, Bounds{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte}, diags, s);
+}
+
+int tempo_run_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, int itimestep, float* t,
+                        float* th, const float* pii, const float* p, const float* w,
+                        const float* dz, float* qv, float* qc, float* qr, float* qi, float* qs,
+                        float* qg, float* ni, float* nr, float* nc, float* nwfa, float* nifa,
+                        float* ng, float* qb, const int* land_input, int ims, int ime, int jms,
+                        int jme, int kms, int kme, int its, int ite, int jts, int jte, int kts,
+                        int kte, tempo_diags_t* diags, void* stream) {
+  RunArrays<float> A{t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb, land_input};
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the default stream
+  return run_dev(c, cfg, (double)dt, itimestep, A, Bounds{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte}, diags, s);
+}
+
+int tempo_aerosol_surface_emissions_dev_c(tempo_ctx_t* c, double dt, double* nwfa,
+                                          const double* nwfa2d, int ims, int ime, int jms, int jme,
+                                          int kms, int kme, int kts, void* stream) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (!nwfa || !nwfa2d) return fail(TEMPO_ERR_ARG, "NULL array");
+  if (ime < ims || jme < jms || kme < kms || kts < kms || kts > kme)
+    return fail(TEMPO_ERR_ARG, "bad bounds");
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  CUDA_TRY(launch_surface_emissions(nwfa, nwfa2d, ime - ims + 1, kme - kms + 1, jme - jms + 1,
+                                    kts - kms, dt, s));
+  return TEMPO_OK;
+}
+
+int tempo_build_tables_c(tempo_ctx_t* c, float* ms) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  int rc = build_tables_gpu(c, ms);
+  if (rc) return rc;
+  return make_f32_tables(c);
+}
+
+int tempo_get_table_c(tempo_ctx_t* c, const char* name, double* host_out, long count, long* needed) {
+  if (!c || !name) return fail(TEMPO_ERR_ARG, "NULL argument");
+  struct E {
+    const char* n;
+    const double* aos;
+    long cnt;
+    int nfam, slot;
+  } tab[] = {
+      {"t_efrw", c->t64.t_efrw, (long)nbr * nbc, 1, 0},
+      {"t_efsw", c->t64.t_efsw, (long)nbs * nbc, 1, 0},
+      {"tpc_wev", c->t64.tpc_wev, (long)nbc * ntb_c * nbc, 1, 0},
+      {"tnc_wev", c->t64.tnc_wev, (long)nbc * ntb_c * nbc, 1, 0},
+      {"tps_iaus", c->t64.tps_iaus, (long)ntb_i * ntb_i1, 1, 0},
+      {"tni_iaus", c->t64.tni_iaus, (long)ntb_i * ntb_i1, 1, 0},
+      {"tpi_ide", c->t64.tpi_ide, (long)ntb_i * ntb_i1, 1, 0},
+      {"tcg_racg", c->t64.qg, QG_COUNT, 5, 0},   {"tmr_racg", c->t64.qg, QG_COUNT, 5, 1},
+      {"tcr_gacr", c->t64.qg, QG_COUNT, 5, 2},   {"tnr_racg", c->t64.qg, QG_COUNT, 5, 3},
+      {"tnr_gacr", c->t64.qg, QG_COUNT, 5, 4},   {"tcs_racs1", c->t64.qs, QS_COUNT, 12, 0},
+      {"tmr_racs1", c->t64.qs, QS_COUNT, 12, 1}, {"tcs_racs2", c->t64.qs, QS_COUNT, 12, 2},
+      {"tmr_racs2", c->t64.qs, QS_COUNT, 12, 3}, {"tcr_sacr1", c->t64.qs, QS_COUNT, 12, 4},
+      {"tms_sacr1", c->t64.qs, QS_COUNT, 12, 5}, {"tcr_sacr2", c->t64.qs, QS_COUNT, 12, 6},
+      {"tms_sacr2", c->t64.qs, QS_COUNT, 12, 7}, {"tnr_racs1", c->t64.qs, QS_COUNT, 12, 8},
+      {"tnr_racs2", c->t64.qs, QS_COUNT, 12, 9}, {"tnr_sacr1", c->t64.qs, QS_COUNT, 12, 10},
+      {"tnr_sacr2", c->t64.qs, QS_COUNT, 12, 11}, {"tpi_qrfz", c->t64.qrfz, QRFZ_COUNT, 4, 0},
+      {"tni_qrfz", c->t64.qrfz, QRFZ_COUNT, 4, 1}, {"tpg_qrfz", c->t64.qrfz, QRFZ_COUNT, 4, 2},
+      {"tnr_qrfz", c->t64.qrfz, QRFZ_COUNT, 4, 3}, {"tpi_qcfz", c->t64.qcfz, QCFZ_COUNT, 2, 0},
+      {"tni_qcfz", c->t64.qcfz, QCFZ_COUNT, 2, 1}};
+  for (auto& t : tab) {
+    if (std::strcmp(t.n, name)) continue;
+    if (needed) *needed = t.cnt;
+    if (!host_out) return TEMPO_OK;
+    if (count < t.cnt) return fail(TEMPO_ERR_ARG, "buffer for %s holds %ld < %ld", name, count, t.cnt);
+    double* tmp = nullptr;
+    if (int rc = dev_alloc(&tmp, (size_t)t.cnt)) return rc;
+    cudaError_t e = aos_gather(tmp, t.aos, t.cnt, t.nfam, t.slot, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host_out, tmp, t.cnt * 8, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail(TEMPO_ERR_CUDA, "get_table: %s", cudaGetErrorString(e));
+    return TEMPO_OK;
+  }
+  return fail(TEMPO_ERR_ARG, "unknown table '%s'", name);
+}
+
+int tempo_write_table_c(tempo_ctx_t* c, const char* name, const char* path) {
+  if (!c || !name || !path) return fail(TEMPO_ERR_ARG, "NULL argument");
+  const char* fz[] = {"tpi_qrfz", "tni_qrfz", "tpg_qrfz", "tnr_qrfz", "tpi_qcfz", "tni_qcfz"};
+  const char* qs[] = {"tcs_racs1", "tmr_racs1", "tcs_racs2", "tmr_racs2", "tcr_sacr1", "tms_sacr1",
+                      "tcr_sacr2", "tms_sacr2", "tnr_racs1", "tnr_racs2", "tnr_sacr1", "tnr_sacr2"};
+  const char* qg[] = {"tcg_racg", "tmr_racg", "tcr_gacr", "tnr_racg", "tnr_gacr"};
+  const char** arrs;
+  int narr;
+  if (!std::strcmp(name, "freezewater")) {
+    arrs = fz;
+    narr = 6;
+  } else if (!std::strcmp(name, "qr_acr_qs")) {
+    arrs = qs;
+    narr = 12;
+  } else if (!std::strcmp(name, "qr_acr_qg")) {
+    arrs = qg;
+    narr = 5;
+  } else {
+    return fail(TEMPO_ERR_ARG, "unknown table family '%s'", name);
+  }
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(TEMPO_ERR_ARG, "cannot create %s", path);
+  std::vector<double> buf;
+  for (int a = 0; a < narr; a++) {
+    long n = 0;
+    tempo_get_table_c(c, arrs[a], nullptr, 0, &n);
+    buf.resize(n);
+    int rc = tempo_get_table_c(c, arrs[a], buf.data(), n, nullptr);
+    if (rc) {
+      std::fclose(f);
+      return rc;
+    }
+    if (host_little()) bswap8(buf.data(), n);
+    if ((long)std::fwrite(buf.data(), 8, n, f) != n) {
+      std::fclose(f);
+      return fail(TEMPO_ERR_ARG, "short write to %s", path);
+    }
+  }
+  std::fclose(f);
+  return TEMPO_OK;
+}
+
+int tempo_last_stats_c(tempo_ctx_t* c, long out[8]) {
+  if (!c || !out) return fail(TEMPO_ERR_ARG, "NULL argument");
+  unsigned long long s[8] = {0};
+  CUDA_TRY(cudaSetDevice(c->device));
+  CUDA_TRY(cudaDeviceSynchronize());  // runs may be enqueued on caller streams
+  CUDA_TRY(cudaMemcpy(s, c->d_stats, sizeof s, cudaMemcpyDeviceToHost));
+  out[0] = c->last_cols;
+  out[1] = (long)s[0];
+  for (int i = 0; i < 5; i++) out[2 + i] = (long)s[1 + i];
+  out[7] = c->launches;
+  return TEMPO_OK;
+}
+
+}  // extern "C"

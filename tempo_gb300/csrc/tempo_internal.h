@@ -1,0 +1,51 @@
+// tempo_internal.h -- interfaces between the translation units of libtempo_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "tempo_consts.h"
+
+namespace tg {
+
+template <class R> struct Tables;
+template <class S> struct StepArgs;
+
+// tempo_step_f64.cu (FP64 drop-in, compiled without FMA contraction)
+cudaError_t launch_step_f64(const StepArgs<double>& a, const Tables<double>& t,
+                            const TempoConsts<double>& c64, cudaStream_t s);
+
+// tempo_step_f32.cu (mixed precision: FP32 bulk, FP64 islands)
+cudaError_t launch_step_mixed_f32(const StepArgs<float>& a, const Tables<float>& t,
+                                  const TempoConsts<float>& c32, const TempoConsts<double>& c64,
+                                  cudaStream_t s);
+cudaError_t launch_step_mixed_f64(const StepArgs<double>& a, const Tables<float>& t,
+                                  const TempoConsts<float>& c32, const TempoConsts<double>& c64,
+                                  cudaStream_t s);
+
+// tempo_tables.cu (FP64 table construction on the GPU)
+struct DevTables64 {
+  double *t_efrw, *t_efsw, *tpc_wev, *tnc_wev, *tps_iaus, *tni_iaus, *tpi_ide;
+  double *qg, *qs, *qrfz, *qcfz;  // AoS layouts described in tempo_level.cuh
+  float* tnccn;
+};
+// small init tables: compute_efrw/efsw, compute_drop_evap, qi_aut_qs
+// (tc: the constant set; the small tables use only its hail-independent members)
+cudaError_t build_small_tables(const DevTables64& t, const TempoBins& bins,
+                               const TempoConsts<double>& tc, cudaStream_t s);
+// the three large tables (tables.F90:493-805) with hail-aware graupel constants
+cudaError_t build_big_tables(const DevTables64& t, const TempoBins& bins,
+                             const TempoConsts<double>& hail_consts, double* work,
+                             size_t work_bytes, cudaStream_t s);
+size_t big_tables_work_bytes();
+// element-wise double -> float copy
+cudaError_t narrow_copy(float* dst, const double* src, long n, cudaStream_t s);
+// AoS <-> Fortran-order SoA conversion for one array of a family
+cudaError_t aos_scatter(double* aos, const double* soa, long n, int nfam, int which, cudaStream_t s);
+cudaError_t aos_gather(double* soa, const double* aos, long n, int nfam, int which, cudaStream_t s);
+// nwfa(i,kts,j) += nwfa2d(i,j)*dt
+cudaError_t launch_surface_emissions(double* nwfa, const double* nwfa2d, long ni, long nk, long nj,
+                                     int kts_off, double dt, cudaStream_t s);
+
+}  // namespace tg

@@ -1,0 +1,514 @@
+// tempo_level.cuh -- per-level microphysics of the TEMPO column step for sm_103a.
+//
+// Every routine of src/module_mp_tempo_main.F90 that is pointwise in k is written here
+// as a device function on one level's scalar state (struct Lev).  The column kernel
+// (tempo_step.cuh) sequences them and does the vertically coupled parts.
+//
+// Template parameter R is the bulk arithmetic type: double for the FP64 drop-in
+// (every operation in the reference's order, compiled without FMA contraction) and
+// float for the mixed form.  The thermodynamic island -- temperature, vapour,
+// density, saturation mixing ratios, (super)saturations and the saturation
+// adjustment -- is always double (type D): differences of nearly equal
+// quantities (qv - qvs) decide condensation and must not lose FP32 digits.
+#pragma once
+
+#include <cstdint>
+
+#include "tempo_consts.h"
+#include "tempo_types.h"
+
+namespace tg {
+
+using D = double;
+
+// ---------------------------------------------------------------------------------
+// math wrappers: accurate library functions for the chosen type (no fast-math)
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ double Pow(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float Pow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double Exp(double x) { return exp(x); }
+__device__ __forceinline__ float Exp(float x) { return expf(x); }
+__device__ __forceinline__ double Log(double x) { return log(x); }
+__device__ __forceinline__ float Log(float x) { return logf(x); }
+__device__ __forceinline__ double Log10(double x) { return log10(x); }
+__device__ __forceinline__ float Log10(float x) { return log10f(x); }
+__device__ __forceinline__ double Sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float Sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double Cos(double x) { return cos(x); }
+__device__ __forceinline__ float Cos(float x) { return cosf(x); }
+__device__ __forceinline__ double Fabs(double x) { return fabs(x); }
+__device__ __forceinline__ float Fabs(float x) { return fabsf(x); }
+__device__ __forceinline__ double Copysign(double a, double b) { return copysign(a, b); }
+__device__ __forceinline__ float Copysign(float a, float b) { return copysignf(a, b); }
+
+// Fortran MAX/MIN on reals (first argument wins ties; no NaN special-casing)
+template <class T> __device__ __forceinline__ T Max(T a, T b) { return a > b ? a : b; }
+template <class T> __device__ __forceinline__ T Min(T a, T b) { return a < b ? a : b; }
+template <class T> __device__ __forceinline__ T Max3(T a, T b, T c) { return Max(Max(a, b), c); }
+template <class T> __device__ __forceinline__ T Min3(T a, T b, T c) { return Min(Min(a, b), c); }
+// NINT: round half away from zero; INT: truncate toward zero
+template <class T> __device__ __forceinline__ int Nint(T x) { return (int)round(x); }
+template <class T> __device__ __forceinline__ int Int(T x) { return (int)x; }
+// real ** integer: binary powering with a reciprocal for negative exponents
+template <class T> __device__ __forceinline__ T Ipow(T x, int m) {
+  unsigned n = m < 0 ? -(unsigned)m : (unsigned)m;
+  T y = (n % 2) ? x : T(1);
+  while (n >>= 1) {
+    x = x * x;
+    if (n % 2) y = y * x;
+  }
+  return m < 0 ? T(1) / y : y;
+}
+
+// ---------------------------------------------------------------------------------
+// constants and tables
+// ---------------------------------------------------------------------------------
+// The constant sets travel with each launch as __grid_constant__ kernel parameters
+// (constant bank, no per-process global state); every level carries pointers to them.
+
+template <class T> __device__ __forceinline__ T ld(const T* p) { return __ldg(p); }
+
+// ---------------------------------------------------------------------------------
+// per-level state
+// ---------------------------------------------------------------------------------
+template <class R>
+struct Lev {
+  const TempoConsts<R>* cs;  // constant set of the bulk type
+  const TempoConsts<D>* cd;  // double constant set (thermodynamic island)
+  // prognostic "1d" values (after the initial checks) and hydrometeor state
+  R qc1d, nc1d, qr1d, nr1d, qi1d, ni1d, qs1d, qg1d, ng1d, qb1d;
+  bool l_qc, l_qr, l_qi, l_qs, l_qg;
+  int idx_bg;
+  R rc, nc, rr, nr, ri, ni, rs, rg, ng, rb, nwfa, nifa;
+  R ilamc, ilami, ilamr, ilamg, mvd_c, mvd_r, mvd_g;
+  R smob, smoc, smo0, smo1, smo2, smoe, smof, smog, smoz;
+  // thermodynamic island
+  D t1d, qv1d, temp, qv, rho, qvs, qvsi, delqvs, ssatw, ssati, tten, qvten;
+  R pres;
+  R rhof, rhof2, diffu, visco, vsc2, tcond, lvap, ocp, lvt2;
+  R qcten, ncten, qiten, niten, qrten, nrten, qsten, qgten, ngten, qbten, nwfaten, nifaten;
+  R vtboost;
+};
+
+// process rates (ty_tend, main:47-64)
+template <class R>
+struct Tend {
+  R prr_wau, pnr_wau, pnc_wau, prr_rcw, pnc_rcw, pnr_rcr;
+  R prs_scw, pnc_scw, png_scw, pbg_scw, prg_gcw, pnc_gcw, pbg_gcw, pri_ihm, pni_ihm, prs_ihm,
+      prg_ihm, prg_scw;
+  R prr_rcs, pnr_rcs, prg_rcs, png_rcs, prs_rcs, pbg_rcs;
+  R prr_rcg, pnr_rcg, prg_rcg, png_rcg, pbg_rcg;
+  R pri_inu, pni_inu, pri_iha, pni_iha;
+  R pri_wfz, pni_wfz;
+  R prg_rfz, png_rfz, pnr_rfz, pri_rfz, pni_rfz, pbg_rfz;
+  R prs_sde, pri_ide, pni_ide, prs_ide, prg_gde, png_gde;
+  R pni_iau, prs_iau;
+  R prr_sml, prr_gml, pbg_sml, pbg_gml, pnr_sml, pnr_gml;
+  R prr_rci, pnr_rci, pri_rci, pni_rci, prg_rci, png_rci, pbg_rci;
+  R pni_sci, prs_sci;
+  R prw_vcd, pnc_wcd, prv_rev, pnr_rev;
+  R pna_rca, pna_sca, pna_gca, pnd_rcd, pnd_scd, pnd_gcd;
+};
+
+__device__ __forceinline__ D rho_gd(int m) {  // rho_g (params:143-144), 1-based
+  return m == 1 ? 50. : m == 2 ? 100. : m == 3 ? 200. : m == 4 ? 300. : m == 5 ? 400.
+         : m == 6 ? 500. : m == 7 ? 600. : m == 8 ? 700. : 800.;
+}
+template <class R> __device__ __forceinline__ R rho_g(int m) { return R(rho_gd(m)); }
+
+// ---------------------------------------------------------------------------------
+// utils.F90
+// ---------------------------------------------------------------------------------
+// calc_rslf / calc_rsif (utils:285-331), always double
+__device__ __forceinline__ D calc_rslf(D p, D t) {
+  D x = Max(-80.0, t - 273.16);
+  D esl = .611583699E03 +
+          x * (.444606896E02 +
+               x * (.143177157e01 +
+                    x * (.264224321e-1 +
+                         x * (.299291081e-3 +
+                              x * (.203154182e-5 +
+                                   x * (.702620698e-8 + x * (.379534310e-11 + x * -.321582393e-13)))))));
+  esl = Min(esl, p * 0.15);
+  return .622 * esl / (p - esl);
+}
+__device__ __forceinline__ D calc_rsif(D p, D t) {
+  D x = Max(-80.0, t - 273.16);
+  D esi = .609868993e03 +
+          x * (.499320233e02 +
+               x * (.184672631e01 +
+                    x * (.402737184e-1 +
+                         x * (.565392987e-3 +
+                              x * (.521693933e-5 +
+                                   x * (.307839583e-7 + x * (.105785160e-9 + x * .161444444e-12)))))));
+  esi = Min(esi, p * 0.15);
+  return .622 * esi / Max(1.e-4, (p - esi));
+}
+
+template <class R> __device__ __forceinline__ int get_nuc(R nc) {  // utils:334-346
+  if ((R(nu_c_scale) / nc) >= R(12.5)) return 15;
+  int v = Nint(R(nu_c_scale) / nc) + 2;
+  return v < 15 ? v : 15;
+}
+
+template <class R>
+__device__ __forceinline__ R poly_a(const R* s, R tc, R X) {  // utils:190-199
+  return s[0] + s[1] * tc + s[2] * X + s[3] * tc * X + s[4] * tc * tc + s[5] * X * X +
+         s[6] * tc * tc * X + s[7] * tc * X * X + s[8] * tc * tc * tc + s[9] * X * X * X;
+}
+
+// snow_moments (utils:148-282).  which: 0 = smob/smoc/smo2, 1 = + ns/smo0/smo1/smoe/
+// smof/smog (initial), 2 = + smoz (final).
+template <class R>
+__device__ void snow_moments(Lev<R>& L, R tc, int which) {
+  const TempoConsts<R>& c = *L.cs;
+  R loga_, a_, b_, smo2_;
+  L.smob = L.rs * c.oams;
+  loga_ = poly_a(c.sa, tc, R(bm_s));
+  a_ = Pow(R(10.0), loga_);
+  b_ = poly_a(c.sb, tc, R(bm_s));
+  smo2_ = Pow(L.smob / a_, R(1.0) / b_);
+  L.smo2 = smo2_;
+  loga_ = poly_a(c.sa, tc, c.cse[0]);
+  a_ = Pow(R(10.0), loga_);
+  b_ = poly_a(c.sb, tc, c.cse[0]);
+  L.smoc = a_ * Pow(smo2_, b_);
+  if (which == 1) {
+    const R* sa = c.sa;
+    const R* sb = c.sb;
+    loga_ = sa[0] + sa[1] * tc + sa[4] * tc * tc + sa[8] * tc * tc * tc;
+    a_ = Pow(R(10.0), loga_);
+    b_ = sb[0] + sb[1] * tc + sb[4] * tc * tc + sb[8] * tc * tc * tc;
+    L.smo0 = a_ * Pow(smo2_, b_);
+    loga_ = sa[0] + sa[1] * tc + sa[2] + sa[3] * tc + sa[4] * tc * tc + sa[5] + sa[6] * tc * tc +
+            sa[7] * tc + sa[8] * tc * tc * tc + sa[9];
+    a_ = Pow(R(10.0), loga_);
+    b_ = sb[0] + sb[1] * tc + sb[2] + sb[3] * tc + sb[4] * tc * tc + sb[5] + sb[6] * tc * tc +
+         sb[7] * tc + sb[8] * tc * tc * tc + sb[9];
+    L.smo1 = a_ * Pow(smo2_, b_);
+    loga_ = poly_a(sa, tc, c.cse[12]);
+    a_ = Pow(R(10.0), loga_);
+    b_ = poly_a(sb, tc, c.cse[12]);
+    L.smoe = a_ * Pow(smo2_, b_);
+    loga_ = poly_a(sa, tc, c.cse[15]);
+    a_ = Pow(R(10.0), loga_);
+    b_ = poly_a(sb, tc, c.cse[15]);
+    L.smof = a_ * Pow(smo2_, b_);
+    loga_ = poly_a(sa, tc, c.cse[16]);
+    a_ = Pow(R(10.0), loga_);
+    b_ = poly_a(sb, tc, c.cse[16]);
+    L.smog = a_ * Pow(smo2_, b_);
+  } else if (which == 2) {
+    loga_ = poly_a(c.sa, tc, c.cse[2]);
+    a_ = Pow(R(10.0), loga_);
+    b_ = poly_a(c.sb, tc, c.cse[2]);
+    L.smoz = a_ * Pow(smo2_, b_);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// check_and_update routines (main:867-1260), one level
+// ---------------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ void aerosol_check(Lev<R>& L, uint32_t f, R dt) {  // main:867-888
+  R rho = R(L.rho);
+  if (f & F_NWFA) L.nwfa = (L.nwfa + L.nwfaten * dt) * rho;  // nwfa holds nwfa1d on entry
+  if (f & F_NIFA) L.nifa = (L.nifa + L.nifaten * dt) * rho;
+  L.nwfa = Max(R(nwfa_default) * rho, Min(R(aero_max) * rho, L.nwfa));
+  L.nifa = Max(R(nifa_default) * rho, Min(R(aero_max) * rho, L.nifa));
+}
+
+// cloud_check_and_update (main:891-973) on (q, n) = (qc1d, nc1d) or temporaries
+template <class R>
+__device__ void cloud_check(Lev<R>& L, R& q, R& n, bool has_nc, R ncsave, R dt, R odt) {
+  const TempoConsts<R>& c = *L.cs;
+  R rho = R(L.rho);
+  bool hit_limit = false;
+  int nu_c;
+  R lamc, xdc;
+  if (q + L.qcten * dt > R(r1)) {
+    L.l_qc = true;
+    L.rc = (q + L.qcten * dt) * rho;
+    q = q + L.qcten * dt;
+    if (has_nc) {
+      L.nc = Max(R(nt_c_min), (n + L.ncten * dt) * rho);
+      if (L.nc <= R(nt_c_min)) {
+        hit_limit = true;
+        L.nc = R(nt_c_min);
+      }
+      if (L.nc > R(nt_c_max)) {
+        hit_limit = true;
+        L.nc = R(nt_c_max);
+      }
+      nu_c = get_nuc(L.nc);
+      lamc = Pow(L.nc * c.am_r * c.ccg[nu_c - 1][1] * c.ocg1[nu_c - 1] / L.rc, c.obmr);
+      xdc = (R(bm_r) + R(nu_c) + R(1.0)) / lamc;
+      if (xdc < R(d0c)) {
+        lamc = c.cce[nu_c - 1][1] / R(d0c);
+        hit_limit = true;
+      } else if (xdc > R(d0r) * R(2.0)) {
+        lamc = c.cce[nu_c - 1][1] / (R(d0r) * R(2.0));
+        hit_limit = true;
+      }
+      L.nc = c.ccg[nu_c - 1][0] * c.ocg2[nu_c - 1] * L.rc / c.am_r * Pow(lamc, R(bm_r));
+      if (hit_limit) L.ncten = (L.nc / rho - n) * odt;
+      n = Max(R(nt_c_min) / rho,
+              Min(c.ccg[nu_c - 1][0] * c.ocg2[nu_c - 1] * q / c.am_r * Pow(lamc, R(bm_r)),
+                  R(nt_c_max) / rho));
+    } else {
+      L.nc = ncsave;
+    }
+    nu_c = get_nuc(L.nc);
+    lamc = Pow(L.nc * c.am_r * c.ccg[nu_c - 1][1] * c.ocg1[nu_c - 1] / L.rc, c.obmr);
+    L.ilamc = R(1.0) / lamc;
+    L.mvd_c = Max(Min((R(3.0) + R(nu_c) + R(0.672)) * L.ilamc, R(d0r)), R(d0c));
+  } else {
+    L.l_qc = false;
+    L.rc = R(r1);
+    L.nc = R(nt_c_min);
+    L.mvd_c = R(d0c);
+    L.ilamc = R(0.0);
+    L.qcten = -q * odt;
+    q = R(0.0);
+    if (has_nc) {
+      L.ncten = -n * odt;
+      n = R(0.0);
+    }
+  }
+}
+
+// rain_check_and_update (main:976-1042)
+template <class R>
+__device__ void rain_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
+  const TempoConsts<R>& c = *L.cs;
+  R rho = R(L.rho);
+  bool hit_limit = false;
+  R lamr;
+  if (q + L.qrten * dt > R(r1)) {
+    L.l_qr = true;
+    L.rr = (q + L.qrten * dt) * rho;
+    q = q + L.qrten * dt;
+    L.nr = Max(R(r2), (n + L.nrten * dt) * rho);
+    if (L.nr <= R(r2)) {
+      hit_limit = true;
+      L.mvd_r = R(1.0e-3);
+      lamr = (R(3.0) + R(mu_r) + R(0.672)) / L.mvd_r;
+      L.nr = c.crg[1] * c.org3 * L.rr * Pow(lamr, R(bm_r)) / c.am_r;
+    }
+    lamr = Pow(c.am_r * c.crg[2] * c.org2 * L.nr / L.rr, c.obmr);
+    L.mvd_r = (R(3.0) + R(mu_r) + R(0.672)) / lamr;
+    if (L.mvd_r > R(d0r_max)) {
+      hit_limit = true;
+      L.mvd_r = R(d0r_max);
+      lamr = (R(3.0) + R(mu_r) + R(0.672)) / L.mvd_r;
+      L.nr = c.crg[1] * c.org3 * L.rr * Pow(lamr, R(bm_r)) / c.am_r;
+    } else if (L.mvd_r < R(d0r) * R(0.75)) {
+      hit_limit = true;
+      L.mvd_r = R(d0r) * R(0.75);
+      lamr = (R(3.0) + R(mu_r) + R(0.672)) / L.mvd_r;
+      L.nr = c.crg[1] * c.org3 * L.rr * Pow(lamr, R(bm_r)) / c.am_r;
+    }
+    if (hit_limit) L.nrten = (L.nr / rho - n) * odt;
+    n = c.crg[1] * c.org3 * q * Pow(lamr, R(bm_r)) / c.am_r;
+    L.ilamr = R(1.0) / lamr;
+  } else {
+    L.l_qr = false;
+    L.rr = R(r1);
+    L.nr = R(r2);
+    L.mvd_r = R(d0r);
+    L.ilamr = R(0.0);
+    L.qrten = -q * odt;
+    L.nrten = -n * odt;
+    q = R(0.0);
+    n = R(0.0);
+  }
+}
+
+// ice_check_and_update (main:1045-1107)
+template <class R>
+__device__ void ice_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
+  const TempoConsts<R>& c = *L.cs;
+  R rho = R(L.rho);
+  bool hit_limit = false;
+  R lami, xdi;
+  if (q + L.qiten * dt > R(r1)) {
+    L.l_qi = true;
+    L.ri = (q + L.qiten * dt) * rho;
+    q = q + L.qiten * dt;
+    L.ni = Max(R(r2), (n + L.niten * dt) * rho);
+    if (L.ni <= R(r2)) {
+      hit_limit = true;
+      lami = c.cie[1] / R(5.e-6);
+      L.ni = Min(R(max_ni), c.cig[0] * c.oig2 * L.ri / c.am_i * Pow(lami, R(bm_i)));
+    }
+    lami = Pow(c.am_i * c.cig[1] * c.oig1 * L.ni / L.ri, c.obmi);
+    xdi = (R(bm_i) + R(mu_i) + R(1.0)) / lami;
+    if (xdi < R(5.e-6)) {
+      hit_limit = true;
+      lami = c.cie[1] / R(5.e-6);
+      L.ni = Min(R(max_ni), c.cig[0] * c.oig2 * L.ri / c.am_i * Pow(lami, R(bm_i)));
+    } else if (xdi > R(d0s)) {
+      hit_limit = true;
+      lami = c.cie[1] / R(d0s);
+      L.ni = c.cig[0] * c.oig2 * L.ri / c.am_i * Pow(lami, R(bm_i));
+    }
+    if (hit_limit) L.niten = (L.ni / rho - n) * odt;
+    n = Max(R(r2) / rho, Min(c.cig[0] * c.oig2 * q / c.am_i * Pow(lami, R(bm_i)), R(max_ni) / rho));
+    L.ilami = R(1.0) / lami;
+  } else {
+    L.l_qi = false;
+    L.ri = R(r1);
+    L.ni = R(r2);
+    L.ilami = R(0.0);
+    L.qiten = -q * odt;
+    L.niten = -n * odt;
+    q = R(0.0);
+    n = R(0.0);
+  }
+}
+
+// snow_check_and_update (main:1110-1134)
+template <class R>
+__device__ __forceinline__ void snow_check(Lev<R>& L, R& q, R dt, R odt) {
+  R rho = R(L.rho);
+  if (q + L.qsten * dt > R(r1)) {
+    L.l_qs = true;
+    L.rs = (q + L.qsten * dt) * rho;
+    q = q + L.qsten * dt;
+  } else {
+    L.l_qs = false;
+    L.rs = R(r1);
+    L.qsten = -q * odt;
+    q = R(0.0);
+  }
+}
+
+// graupel_check_and_update (main:1137-1231)
+template <class R>
+__device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R odt) {
+  const TempoConsts<R>& c = *L.cs;
+  R rho = R(L.rho);
+  bool hit_limit = false;
+  R lamg;
+  if (q + L.qgten * dt > R(r1)) {
+    L.l_qg = true;
+    L.rg = (q + L.qgten * dt) * rho;
+    q = q + L.qgten * dt;
+    if (hail) {
+      L.ng = Max(R(r2), (n + L.ngten * dt) * rho);
+      L.rb = Min(Max(L.rg * R(meters3_to_liters) / rho_g<R>(nrhg), (b + L.qbten * dt) * rho),
+                 L.rg * R(meters3_to_liters) / rho_g<R>(1));
+      L.idx_bg = max(1, min(Nint(R(10.0) * L.rg / L.rb) + 1, nrhg));
+      const int ig = L.idx_bg;
+      if (L.ng <= R(r2)) {
+        hit_limit = true;
+        L.mvd_g = R(1.5e-3);
+        lamg = (R(3.0) + R(mu_g) + R(0.672)) / L.mvd_g;
+        L.ng = c.cgg[0][1] * c.ogg3 * L.rg * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
+      }
+      lamg = Pow(c.am_g[ig - 1] * c.cgg[0][2] * c.ogg2 * L.ng / L.rg, c.obmg);
+      L.mvd_g = (R(3.0) + R(mu_g) + R(0.672)) / lamg;
+      if (L.mvd_g > R(25.4e-3)) {
+        hit_limit = true;
+        L.mvd_g = R(25.4e-3);
+        lamg = (R(3.0) + R(mu_g) + R(0.672)) / L.mvd_g;
+        L.ng = c.cgg[0][1] * c.ogg3 * L.rg * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
+      } else if (L.mvd_g < R(d0r)) {
+        hit_limit = true;
+        L.mvd_g = R(d0r);
+        lamg = (R(3.0) + R(mu_g) + R(0.672)) / L.mvd_g;
+        L.ng = c.cgg[0][1] * c.ogg3 * L.rg * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
+      }
+      if (hit_limit) L.ngten = (L.ng / rho - n) * odt;
+      n = c.cgg[0][1] * c.ogg3 * q * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
+      b = Min(Max(q * R(meters3_to_liters) / rho_g<R>(nrhg), b + L.qbten * dt),
+              R(meters3_to_liters) * q / rho_g<R>(1));
+      L.idx_bg = max(1, min(Nint(R(10.0) * q / b) + 1, nrhg));
+    } else {
+      L.idx_bg = idx_bg1;
+      R ygra1 = Log10(Max(R(1.e-9), L.rg));
+      R zans1 = R(3.4) + R(2.0 / 7.0) * (ygra1 + R(8.0));
+      R n0_exp = Max(R(gonv_min), Min(Pow(R(10.0), zans1), R(gonv_max)));
+      R lam_exp = Pow(n0_exp * c.am_g[idx_bg1 - 1] * c.cgg[0][0] / L.rg, c.oge1);
+      lamg = lam_exp * Pow(c.cgg[0][2] * c.ogg2 * c.ogg1, c.obmg);
+      L.ng = c.cgg[0][1] * c.ogg3 * L.rg * Pow(lamg, R(bm_g)) / c.am_g[idx_bg1 - 1];
+      L.rb = R(meters3_to_liters) * L.rg / rho_g<R>(idx_bg1);
+    }
+    L.ilamg = R(1.0) / lamg;
+    L.mvd_g = (R(3.0) + R(mu_g) + R(0.672)) * L.ilamg;
+  } else {
+    L.l_qg = false;
+    L.rg = R(r1);
+    L.ng = R(r2);
+    L.mvd_g = R(d0g);
+    L.ilamg = R(0.0);
+    L.idx_bg = idx_bg1;
+    L.rb = R(meters3_to_liters) * R(r1) / rho_g<R>(idx_bg1);
+    L.qgten = -q * odt;
+    q = R(0.0);
+    if (hail) {
+      L.ngten = -n * odt;
+      L.qbten = -b * odt;
+      n = R(0.0);
+      b = R(0.0);
+    }
+  }
+}
+
+// graupel_init (main:1234-1260) for one level
+template <class R>
+__device__ __forceinline__ void graupel_init(Lev<R>& L) {
+  const TempoConsts<R>& c = *L.cs;
+  if (L.qg1d > R(r1)) {
+    R rho = R(L.rho);
+    R rg = L.qg1d * rho;
+    R rb = rg * R(meters3_to_liters) / rho_g<R>(idx_bg1);
+    int idx = max(1, min(Nint(R(10.0) * rg / rb) + 1, nrhg));
+    R mvd_g = R(5.e-3);
+    R lamg = (R(3.0) + R(mu_g) + R(0.672)) / mvd_g;
+    R ng = c.cgg[0][1] * c.ogg3 * rg * Pow(lamg, R(bm_g)) / c.am_g[idx - 1];
+    L.ng1d = ng / rho;
+    L.qb1d = rb / rho;
+  }
+}
+
+// thermo_vars (main:1263-1310) for one level; returns ssati > 0
+template <class R>
+__device__ bool thermo(Lev<R>& L) {
+  D otemp = 1.0 / L.temp;
+  D tempc = L.temp - t0;
+  L.rhof = R(Sqrt(L.cd->rho_not / L.rho));
+  L.rhof2 = Sqrt(L.rhof);
+  L.qvs = calc_rslf(D(L.pres), L.temp);
+  L.delqvs = Max(0.0, calc_rslf(D(L.pres), t0) - L.qv);
+  if (tempc <= 0.0)
+    L.qvsi = calc_rsif(D(L.pres), L.temp);
+  else
+    L.qvsi = L.qvs;
+  D satw = L.qv / L.qvs;
+  D sati = L.qv / L.qvsi;
+  L.ssatw = satw - 1.0;
+  L.ssati = sati - 1.0;
+  if (Fabs(L.ssatw) < eps) L.ssatw = 0.0;
+  if (Fabs(L.ssati) < eps) L.ssati = 0.0;
+  R rtc = R(tempc);
+  L.diffu = R(2.11e-5) * Pow(R(L.temp / t0), R(1.94)) * (R(101325.0) / L.pres);
+  if (tempc >= 0.0)
+    L.visco = (R(1.718) + R(0.0049) * rtc) * R(1.0e-5);
+  else
+    L.visco = (R(1.718) + R(0.0049) * rtc - R(1.2e-5) * rtc * rtc) * R(1.0e-5);
+  D ocp = 1.0 / (cp * (1.0 + 0.887 * L.qv));
+  L.ocp = R(ocp);
+  L.vsc2 = Sqrt(R(L.rho) / L.visco);
+  D lvap = lvap0 + (2106.0 - 4218.0) * tempc;
+  L.lvap = R(lvap);
+  L.tcond = (R(5.69) + R(0.0168) * rtc) * R(1.0e-5) * R(418.936);
+  L.lvt2 = R(lvap * lvap * ocp * L.cd->orv * otemp * otemp);
+  return L.ssati > 0.0;
+}
+
+__device__ __forceinline__ D rho_of(const TempoConsts<D>& cd, D pres, D temp, D qv) {  // main:325
+  return cd.roverrv * pres / (rdry * temp * (qv + cd.roverrv));
+}
+
+}  // namespace tg

@@ -246,3 +246,95 @@ def column_water(fields: dict) -> np.ndarray:
     rho = roverrv * p / (RD * t * (qv + roverrv))
     q = qv + fields["qc"] + fields["qr"] + fields["qi"] + fields["qs"] + fields["qg"]
     return np.sum(q * rho * dz, axis=1)
+
+
+def config1_torch(seed: int = 0, ni: int = 1024, nj: int = 1024, nz: int = 65,
+                  device: str = "cuda", dtype=None, hail: bool = False, deep: bool = False,
+                  clear_frac: float = 0.4):
+    """The config1 generator evaluated with torch on the GPU (for the 10^6-column
+    benchmark, where the NumPy version would spend minutes on the host).  Same recipe
+    and distributions as :func:`_profiles` via :func:`_config1_cols`, drawn from a
+    torch generator seeded with 2000 + seed, so the values differ from the NumPy
+    stream.  Returns a dict of (nj, nz, ni) tensors."""
+    import torch
+
+    dtype = dtype or torch.float32
+    g = torch.Generator(device=device)
+    g.manual_seed(2000 + seed)
+    ncol = ni * nj
+    f64 = torch.float64
+    dz = torch.as_tensor(stretched_dz(nz), dtype=f64, device=device)
+
+    def U(lo, hi, shape):
+        return lo + (hi - lo) * torch.rand(shape, generator=g, device=device, dtype=f64)
+
+    def N(shape):
+        return torch.randn(shape, generator=g, device=device, dtype=f64)
+
+    def LN(median, sigma, shape):
+        return median * torch.exp(sigma * N(shape))
+
+    zc = torch.cumsum(dz, 0) - 0.5 * dz
+    z = zc.expand(ncol, nz)
+    t = torch.where(z <= 12000.0, 300.0 - 6.5e-3 * z, torch.full_like(z, 300.0 - 6.5e-3 * 12000.0))
+    p = torch.empty((ncol, nz), dtype=f64, device=device)
+    p[:, 0] = 100000.0 * torch.exp(-G * zc[0] / (RD * t[:, 0]))
+    for k in range(1, nz):
+        tbar = 0.5 * (t[:, k] + t[:, k - 1])
+        p[:, k] = p[:, k - 1] * torch.exp(-G * (zc[k] - zc[k - 1]) / (RD * tbar))
+    rh = torch.where(z < 10000.0, U(0.7, 1.05, (ncol, nz)), torch.full_like(z, 0.3))
+    rho = p / (RD * t)
+    clear = U(0, 1, (ncol,)) < (0.0 if deep else clear_frac)
+    base = U(300.0, 3000.0, (ncol,))
+    depth = U(8e3, 14e3, (ncol,)) if deep else U(0.5e3, 12e3, (ncol,))
+    w = 3.0 * N((ncol, nz))
+    conv = U(0, 1, (ncol,)) < 0.05
+    w = torch.where(conv[:, None], U(5.0, 20.0, (ncol, 1)).expand(ncol, nz), w)
+    zb, zt = base[:, None], (base + depth)[:, None]
+    zr = torch.clamp(zb + 0.5 * (zt - zb), max=4150.0)
+    in_cloud = (z >= zb) & (z <= zt)
+    warm = t > T0
+    liq = in_cloud & (t > T0 - 20.0)
+    zero = torch.zeros((ncol, nz), dtype=f64, device=device)
+    qc = torch.where(liq, LN(0.3e-3, 0.5, (ncol, nz)), zero)
+    if deep:
+        sc = in_cloud & (t <= T0) & (t > T0 - 20.0)
+        qc = torch.where(sc, torch.clamp(LN(0.8e-3, 0.6, (ncol, nz)), max=2.0e-3), qc)
+    nc = torch.where(qc > 0, torch.full_like(qc, 1.0e8), zero)
+    qr = torch.where(z < zr, LN(0.5e-3, 0.5, (ncol, nz)), zero)
+    lam = (math.pi * 1000.0 * 8.0e6 / (rho * torch.clamp(qr, min=1e-30))) ** 0.25
+    nr = torch.where(qr > 0, 8.0e6 / (lam * rho), zero)
+    ice = (~warm) & (z <= zt) & (z >= zb)
+    qi = torch.where(ice, LN(0.02e-3, 0.5, (ncol, nz)), zero)
+    ni_ = torch.where(qi > 0, torch.full_like(qi, 1.0e5), zero)
+    qs = torch.where(ice, LN(0.3e-3, 0.5, (ncol, nz)), zero)
+    if hail:
+        qg = torch.where(ice | (in_cloud & warm), torch.clamp(LN(2.0e-3, 0.6, (ncol, nz)), max=8.0e-3), zero)
+        ng = torch.where(qg > 0, 10.0 ** U(2.0, 5.0, (ncol, nz)), zero)
+        qb = torch.where(qg > 0, 1000.0 * qg / U(300.0, 900.0, (ncol, nz)), zero)
+    else:
+        qg = torch.where(ice, LN(0.1e-3, 0.5, (ncol, nz)), zero)
+        ng = qb = None
+    m = clear[:, None]
+    hydro = [qc, nc, qr, nr, qi, ni_, qs, qg] + ([ng, qb] if hail else [])
+    hydro = [torch.where(m, zero, a) for a in hydro]
+    cloudy = in_cloud & ~m
+    rh = torch.where(cloudy, torch.maximum(rh, U(0.98, 1.02, (ncol, nz))), rh)
+    x = torch.clamp(t - 273.16, min=-80.0)
+    c = [.611583699E03, .444606896E02, .143177157e01, .264224321e-1, .299291081e-3,
+         .203154182e-5, .702620698e-8, .379534310e-11, -.321582393e-13]
+    esl = torch.full_like(x, c[8])
+    for ci in c[7::-1]:
+        esl = ci + x * esl
+    esl = torch.minimum(esl, p * 0.15)
+    qv = rh * 0.622 * esl / (p - esl)
+    names = ["qc", "nc", "qr", "nr", "qi", "ni", "qs", "qg"] + (["ng", "qb"] if hail else [])
+    cols = dict(zip(names, hydro))
+    cols.update(t=t, p=p, w=w, dz=dz.expand(ncol, nz), qv=qv,
+                nwfa=torch.full((ncol, nz), 1.0e9, dtype=f64, device=device),
+                nifa=torch.full((ncol, nz), 1.0e6, dtype=f64, device=device))
+    out = {}
+    for k, v in cols.items():
+        out[k] = v.reshape(nj, ni, nz).permute(0, 2, 1).contiguous().to(dtype)
+        del v
+    return out

@@ -1,0 +1,42 @@
+"""Shared fixtures.  `gpu`-marked tests need a GB300 and the built CUDA library;
+everything else runs on the CPU (the oracle is test infrastructure)."""
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+REPO = Path(__file__).resolve().parents[1]
+if str(REPO) not in sys.path:
+    sys.path.insert(0, str(REPO))
+
+TABLES = REPO / "tables"
+REF = Path("/root/reference")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a GB300 GPU and the CUDA library")
+
+
+@pytest.fixture(scope="session")
+def oracle_mod():
+    import oracle
+    oracle.build()
+    return oracle
+
+
+@pytest.fixture(scope="session")
+def oracle_tables(oracle_mod, tmp_path_factory):
+    """Oracle initialised hail-aware with its own table build, and the three tables
+    written in the reference's big-endian file format (plus the CCN file)."""
+    o = oracle_mod
+    o.init(True, TABLES / "ccn_activate.bin")
+    o.build_big_tables()
+    d = tmp_path_factory.mktemp("tables")
+    lib = o.load()
+    assert lib.oracle_write_freezewater(str(d / "freeze_water_data_tempo_v3").encode()) == 0
+    assert lib.oracle_write_qr_acr_qs(str(d / "qr_acr_qs_data_tempo_v3").encode()) == 0
+    assert lib.oracle_write_qr_acr_qg(str(d / "qr_acr_qg_data_tempo_v3").encode()) == 0
+    (d / "ccn_activate.bin").write_bytes((TABLES / "ccn_activate.bin").read_bytes())
+    return d

@@ -1,0 +1,75 @@
+"""Helpers shared by the parity tests: run one workload through the oracle and the
+CUDA library on identical inputs, and compare field by field."""
+from __future__ import annotations
+
+import numpy as np
+
+OUT3 = ("t", "qv", "qc", "qr", "qi", "qs", "qg", "ni", "nr", "nc", "nwfa", "nifa", "ng", "qb")
+# absolute floors below which differences are judged against the floor instead of the
+# value (the reference's existence thresholds r1 = 1e-12 kg/m3, r2 = 1e-6 /m3 scaled
+# to per-kg mixing ratios)
+FLOOR = {"t": 1.0, "qv": 1e-12, "qc": 1e-12, "qr": 1e-12, "qi": 1e-12, "qs": 1e-12, "qg": 1e-12,
+         "ni": 1e-6, "nr": 1e-6, "nc": 1e-6, "nwfa": 1.0, "nifa": 1.0, "ng": 1e-6, "qb": 1e-12,
+         "rain_precip": 1e-12, "ice_liquid_equiv_precip": 1e-12,
+         "snow_liquid_equiv_precip": 1e-12, "graupel_liquid_equiv_precip": 1e-12,
+         "frozen_fraction": 1e-12, "frz_rain_precip": 1e-12, "max_hail_diameter_sfc": 1e-6,
+         "max_hail_diameter_column": 1e-6, "refl10cm": 1.0, "re_cloud": 1e-9, "re_ice": 1e-9,
+         "re_snow": 1e-9, "rain_med_vol_diam": 1e-9, "graupel_med_vol_diam": 1e-9,
+         "cloud_number_mixing_ratio": 1e-6}
+DIAG2 = ("rain_precip", "ice_liquid_equiv_precip", "snow_liquid_equiv_precip",
+         "graupel_liquid_equiv_precip", "frozen_fraction", "frz_rain_precip",
+         "max_hail_diameter_sfc", "max_hail_diameter_column")
+DIAG3 = ("refl10cm", "re_cloud", "re_ice", "re_snow", "rain_med_vol_diam",
+         "graupel_med_vol_diam", "cloud_number_mixing_ratio")
+
+
+def make_diags(shape, diag3=DIAG3, dtype=np.float64):
+    nj, nk, ni = shape
+    d = {n: np.full((nj, ni), np.nan, dtype=dtype) for n in DIAG2}
+    d.update({n: np.full((nj, nk, ni), np.nan, dtype=dtype) for n in diag3})
+    return d
+
+
+def run_oracle(oracle, cfg_over: dict, wl, fields=None, itimestep=1, diag3=DIAG3, nthreads=0):
+    f = {k: v.copy() for k, v in (fields or wl.fields).items()}
+    d = make_diags(f["p"].shape, diag3)
+    cfg = oracle.default_cfgs(**cfg_over)
+    rc = oracle.run(cfg, wl.dt, itimestep, f, d, nthreads=nthreads)
+    assert rc == 0, f"oracle_run returned {rc}"
+    return f, d
+
+
+def run_gpu(ctx, cfg_over: dict, wl, fields=None, itimestep=1, diag3=DIAG3, dtype=np.float64):
+    import tempo_gb300 as tg
+    f = {k: np.ascontiguousarray(v.astype(dtype)) for k, v in (fields or wl.fields).items()}
+    d = make_diags(f["p"].shape, diag3, dtype)
+    cfg = tg.default_cfgs(**cfg_over)
+    ctx.run(f, wl.dt, itimestep, diags=d, cfgs=cfg)
+    return f, d
+
+
+def rel_err(a, b, floor):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b) / np.maximum(np.abs(b), floor)
+
+
+def compare(fa, da, fb, db, names3=OUT3):
+    """Per-field (max, rms) relative error of a against b (b = oracle)."""
+    out = {}
+    for n in names3:
+        if n in fa and n in fb:
+            e = rel_err(fa[n], fb[n], FLOOR[n])
+            out[n] = (float(e.max()), float(np.sqrt(np.mean(e * e))))
+    for n in tuple(DIAG2) + tuple(DIAG3):
+        if n in da and n in db:
+            assert not np.isnan(db[n]).any(), f"oracle left {n} unset"
+            assert not np.isnan(da[n]).any(), f"{n} not written"
+            e = rel_err(da[n], db[n], FLOOR[n])
+            out[n] = (float(e.max()), float(np.sqrt(np.mean(e * e))))
+    return out
+
+
+def worst(errs):
+    k = max(errs, key=lambda n: errs[n][0])
+    return k, errs[k][0]
