@@ -12,7 +12,6 @@ if str(REPO) not in sys.path:
     sys.path.insert(0, str(REPO))
 
 TABLES = REPO / "tables"
-REF = Path("/root/reference")
 
 
 def pytest_configure(config):
@@ -40,3 +39,24 @@ def oracle_tables(oracle_mod, tmp_path_factory):
     assert lib.oracle_write_qr_acr_qg(str(d / "qr_acr_qg_data_tempo_v3").encode()) == 0
     (d / "ccn_activate.bin").write_bytes((TABLES / "ccn_activate.bin").read_bytes())
     return d
+
+
+@pytest.fixture(scope="session")
+def tg():
+    """The CUDA library's Python binding (built in-tree if stale)."""
+    import tempo_gb300
+    tempo_gb300.build.build()
+    return tempo_gb300
+
+
+@pytest.fixture(scope="session")
+def ctx_hail(tg, oracle_tables):
+    """Hail-aware context on the oracle's tables (read from the reference file format)."""
+    return tg.TempoContext(table_dir=oracle_tables, build_tables=False,
+                           cfgs=tg.default_cfgs(hailaware_flag=1))
+
+
+@pytest.fixture(scope="session")
+def ctx_nohail(tg, oracle_tables):
+    return tg.TempoContext(table_dir=oracle_tables, build_tables=False,
+                           cfgs=tg.default_cfgs(hailaware_flag=0))

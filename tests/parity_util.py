@@ -73,3 +73,34 @@ def compare(fa, da, fb, db, names3=OUT3):
 def worst(errs):
     k = max(errs, key=lambda n: errs[n][0])
     return k, errs[k][0]
+
+
+def graupel_density_ties(qg, qb, rtol=1e-12):
+    """Levels at the rounding tie of the graupel density class.
+
+    The class is idx_bg = nint(10 * rg / rb) + 1 (module_mp_tempo_main.F90:1172, 1198).
+    Where the volume rb sits at its low-density clamp rg * 1000 / rho_g(1) (main:1169-1170),
+    10 * rg / rb is 0.5 up to one rounding, so a one-ulp difference in rg -- e.g. from
+    the device's and the host's pow/exp -- moves the class between 1 and 2.  Those
+    classes differ in am_g by rho_g(2) / rho_g(1) = 2, so the median volume diameter
+    (proportional to am_g**(-1/3)) moves by exactly 2**(1/3), while mass and number
+    (independent of am_g, main:1175-1196) do not.  Returns the boolean mask of such
+    levels, judged on the final qg, qb."""
+    qg = np.asarray(qg, dtype=np.float64)
+    qb = np.asarray(qb, dtype=np.float64)
+    ok = (qg > 1e-12) & (qb > 0)
+    r = np.where(ok, 10.0 * qg / np.where(qb > 0, qb, 1.0), 0.0)
+    return ok & (np.abs(r - 0.5) <= rtol * 0.5)
+
+
+def mvd_g_tie_flips(mvd_got, mvd_want, ties, rtol=1e-12):
+    """Splits graupel MVD differences at density-class ties into class flips (ratio
+    exactly 2**(+-1/3)) and returns (number of flips, max relative error of the rest)."""
+    a = np.asarray(mvd_got, dtype=np.float64)
+    b = np.asarray(mvd_want, dtype=np.float64)
+    e = np.abs(a - b) / np.maximum(np.abs(b), FLOOR["graupel_med_vol_diam"])
+    ratio = np.where(b > 0, a / np.where(b > 0, b, 1.0), 1.0)
+    c = 2.0 ** (1.0 / 3.0)
+    flip = ties & ((np.abs(ratio - c) <= 1e-10 * c) | (np.abs(ratio - 1.0 / c) <= 1e-10 / c))
+    rest = np.where(flip, 0.0, e)
+    return int(flip.sum()), float(rest.max())

@@ -6,29 +6,11 @@ format).  Table construction on the GPU: within 1e-12 relative of the oracle's."
 import numpy as np
 import pytest
 
-from parity_util import compare, run_gpu, run_oracle, worst
+from parity_util import (compare, graupel_density_ties, mvd_g_tie_flips, run_gpu,
+                         run_oracle, worst)
 
 pytestmark = pytest.mark.gpu
 TOL64 = 1e-12
-
-
-@pytest.fixture(scope="module")
-def tg():
-    import tempo_gb300
-    tempo_gb300.build.build()
-    return tempo_gb300
-
-
-@pytest.fixture(scope="module")
-def ctx_hail(tg, oracle_tables):
-    return tg.TempoContext(table_dir=oracle_tables, build_tables=False,
-                           cfgs=tg.default_cfgs(hailaware_flag=1))
-
-
-@pytest.fixture(scope="module")
-def ctx_nohail(tg, oracle_tables):
-    return tg.TempoContext(table_dir=oracle_tables, build_tables=False,
-                           cfgs=tg.default_cfgs(hailaware_flag=0))
 
 
 def test_small_tables_match_oracle(ctx_hail, oracle_mod):
@@ -96,6 +78,14 @@ def test_config2_hail_fp64_matches_oracle(ctx_hail, oracle_mod):
                 cloud_number_mixing_ratio_flag=1)
     fo, do = run_oracle(oracle_mod, over, wl)
     fg, dg = run_gpu(ctx_hail, over, wl)
+    # the graupel MVD may flip by 2**(1/3) at exact density-class ties (see
+    # parity_util.graupel_density_ties); everything else, the MVD elsewhere included,
+    # holds the FP64 tolerance
+    ties = graupel_density_ties(fo["qg"], fo["qb"])
+    flips, e_mvd = mvd_g_tie_flips(dg["graupel_med_vol_diam"], do["graupel_med_vol_diam"], ties)
+    assert e_mvd < TOL64, e_mvd
+    assert flips <= ties.sum() <= 0.01 * (fo["qg"] > 1e-12).sum(), (flips, ties.sum())
+    dg = {k: v for k, v in dg.items() if k != "graupel_med_vol_diam"}
     errs = compare(fg, dg, fo, do)
     name, e = worst(errs)
     assert e < TOL64, (name, e, errs)
