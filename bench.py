@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ref-columns", type=int, default=131072,
+                    help="columns per step of the reference arm's bounded sample")
     return ap.parse_args()
 
 
@@ -150,20 +152,78 @@ def cpu_baseline(seconds: float, nz: int, dt: float, sample_cols: int = 16384):
                       f"FP64 CPU restatement, {cores} OpenMP threads, {el:.1f} s"}
 
 
+# per-field floors below which differences are judged against the floor (the
+# reference's existence thresholds r1 = 1e-12, r2 = 1e-6, in per-kg units)
+FLOORS = {"t": 1.0, "qv": 1e-12, "qc": 1e-12, "qr": 1e-12, "qi": 1e-12, "qs": 1e-12,
+          "qg": 1e-12, "ni": 1e-6, "nr": 1e-6, "nc": 1e-6, "nwfa": 1.0, "nifa": 1.0,
+          "rain_precip": 1e-12, "snow_liquid_equiv_precip": 1e-12,
+          "graupel_liquid_equiv_precip": 1e-12, "ice_liquid_equiv_precip": 1e-12,
+          "re_cloud": 1e-9, "re_ice": 1e-9, "re_snow": 1e-9}
+
+
+def mixed_vs_fp64(f32, d32, f64, d64):
+    """Per-field max and RMS relative error of one mixed step against one FP64 step
+    from the same state; reflectivity as max and RMS absolute dBZ difference."""
+    import torch
+    out = {}
+    for src32, src64 in ((f32, f64), (d32, d64)):
+        for k, fl in FLOORS.items():
+            if k in src32 and k in src64:
+                a = src32[k].double()
+                b = src64[k]
+                e = (a - b).abs() / b.abs().clamp_min(fl)
+                out[k] = {"max": float(e.max()), "rms": float(torch.sqrt((e * e).mean()))}
+    if "refl10cm" in d32:
+        e = (d32["refl10cm"].double() - d64["refl10cm"]).abs()
+        out["refl10cm_dbz"] = {"max_abs": float(e.max()),
+                               "rms_abs": float(torch.sqrt((e * e).mean()))}
+    return out
+
+
 def run_reference(args, rank, world):
+    """The reference arm: the FP64 CPU restatement on all host cores (the Fortran
+    reference has no compiler on either machine), W untimed and K timed steps, each
+    step one bounded sample of the workload's columns.  Rank 0 only."""
     if rank != 0:
         return
-    cb = cpu_baseline(max(5.0, args.cpu_seconds), args.nz, args.dt)
-    line = {"metric": METRIC, "impl": "reference", "value": cb["value"], "unit": "column-steps/s",
+    import oracle
+    from tempo_gb300 import workloads as W
+    oracle.build()
+    oracle.init(False, REPO / "tables" / "ccn_activate.bin")
+    oracle.build_big_tables()
+    ncol = args.ref_columns
+    wl = W.config1(seed=11, ni=ncol, nj=1, nz=args.nz, steps=1, dt=args.dt)
+    cfg = oracle.default_cfgs(hailaware_flag=0)
+    f = {k: v.copy() for k, v in wl.fields.items()}
+    nj, nk, ni = f["p"].shape
+    d = {"rain_precip": np.zeros((nj, ni)), "refl10cm": np.zeros((nj, nk, ni)),
+         "re_cloud": np.zeros((nj, nk, ni)), "re_ice": np.zeros((nj, nk, ni)),
+         "re_snow": np.zeros((nj, nk, ni))}
+    it = 1
+    for _ in range(args.warmup):
+        oracle.run(cfg, args.dt, it, f, d)
+        it += 1
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.run(cfg, args.dt, it, f, d)
+        it += 1
+    el = time.perf_counter() - t0
+    value = ncol * args.steps / el
+    cores = os.cpu_count()
+    sample = (f"each step {ncol} of the {args.ni * args.nj} columns x {args.nz} levels of the "
+              f"same generator, FP64 CPU restatement, {cores} OpenMP threads, "
+              f"{args.steps} steps in {el:.1f} s")
+    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "column-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * args.ni * args.nj / cb["value"],
+            "ms_per_step": 1e3 * args.ni * args.nj / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded config1 generator)",
             "config": {"workload": f"config1: {args.ni * args.nj} columns x {args.nz} levels, "
                                    f"dt={args.dt}s (timed on a bounded column sample)",
                        "parallelism": "cpu-openmp"},
-            "cpu_baseline": cb,
-            "e2e": {"value": cb["value"], "unit": "column-steps/s", "h2d_bytes_per_step": 0,
+            "cpu_baseline": {"value": value, "unit": "column-steps/s", "cores": cores,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "column-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -203,15 +263,24 @@ def main():
     if world > 1:
         dist.barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # per-kernel durations: CUDA events recorded by the library around its four
+    # kernels on the launching stream, read after each step
+    ctx.set_kernel_timing(True)
+    kms = {k: 0.0 for k in ctx.KERNELS}
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(args.steps):
             ctx.run_device(f32, args.dt, it, diags=diag)
             it += 1
+            for k, v in ctx.kernel_times().items():
+                kms[k] += v
         e1.record(stream)
         torch.cuda.synchronize()
+    ctx.set_kernel_timing(False)
     ms = e0.elapsed_time(e1)
+    kms = {k: v / args.steps for k, v in kms.items()}
+    step_kernel_ms = sum(kms.values())
     stats = ctx.stats()
     if world > 1:
         t = torch.tensor([ms], device=f"cuda:{local}")
@@ -220,12 +289,17 @@ def main():
     ms_step = ms / args.steps
     value = world * ncol * args.steps / (ms / 1e3)
 
-    # FP64 drop-in on the same columns (a few steps; FP64 is 1/64 rate on GB300)
+    # FP64 drop-in on the same columns (a few steps; FP64 is 1/64 rate on GB300).  Its
+    # first step, from the same state as one mixed step, gives the mixed form's error.
     ctx.set_precision(tg.PREC_FP64)
     f64 = {k: v.double() for k, v in f32.items()}
     d64 = {k: v.double() for k, v in diag.items()}
-    ctx.run_device(f64, args.dt, 1, diags=d64)
+    ctx.run_device(f64, args.dt, it, diags=d64)
+    ctx.set_precision(tg.PREC_MIXED)
+    ctx.run_device(f32, args.dt, it, diags=diag)
     torch.cuda.synchronize()
+    mixed_error = mixed_vs_fp64(f32, diag, f64, d64)
+    ctx.set_precision(tg.PREC_FP64)
     e0.record(stream)
     for s in range(args.fp64_steps):
         ctx.run_device(f64, args.dt, 2 + s, diags=d64)
@@ -254,7 +328,7 @@ def main():
     peak_src = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
     alg_bytes = ncol * (4 * nz * (N_IN3 + N_OUT3) + 4 * N_OUT2)
-    achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    achieved = alg_bytes / (step_kernel_ms / 1e3) / 1e9
     clocks = clk.summary()
     out = {
         "metric": METRIC, "value": value, "unit": "column-steps/s", "n_gpus": world,
@@ -268,12 +342,15 @@ def main():
                    "l2": "inputs (8.5 GB) larger than L2", "parallelism": f"replicas x{world}"},
         "fp64_value": world * ncol / (ms64 / 1e3), "fp64_ms_per_step": ms64,
         "fp32_over_fp64": ms64 / ms_step,
+        "mixed_error_vs_fp64": mixed_error,
         "e2e": {"value": e2e_value, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "path": "tempo_run_f32_c (host arrays)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic_from_profiles(),
-                     "kernel": "tempo_column_kernel<float,float>",
-                     "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src},
+                     "kernel": "column step = tempo_{prep,points,sedim,final}_kernel<float,float>",
+                     "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src,
+                     "kernel_ms": kms,
+                     "kernel_share": {k: v / step_kernel_ms for k, v in kms.items()}},
         "gpu_launches": args.steps * stats.get("launches", 1),
         "clocks": clocks,
         "step_stats": stats,

@@ -186,6 +186,13 @@ int tempo_build_tables_c(tempo_ctx_t *ctx, float *elapsed_ms);
  * kernel launches. */
 int tempo_last_stats_c(tempo_ctx_t *ctx, long out[8]);
 
+/* No reference counterpart.  With on != 0, each later run records CUDA events on its
+ * stream around its four kernels (prep, points, sedim, final);
+ * tempo_kernel_times_c waits for the last run's events and returns the four kernel
+ * durations in milliseconds. */
+int tempo_set_kernel_timing(tempo_ctx_t *ctx, int on);
+int tempo_kernel_times_c(tempo_ctx_t *ctx, float ms[4]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -88,6 +88,7 @@ def load() -> ctypes.CDLL:
         lib.oracle_table_ptr.restype = _DP
         lib.oracle_ccn_ptr.argtypes = [ctypes.POINTER(ctypes.c_long)]
         lib.oracle_ccn_ptr.restype = ctypes.POINTER(ctypes.c_float)
+        lib.oracle_set_tie_sink.argtypes = [_IP]
         lib.oracle_param.argtypes = [ctypes.c_char_p, ctypes.c_int]
         lib.oracle_param.restype = ctypes.c_double
         lib.oracle_calc_gamma_p.argtypes = [ctypes.c_double, ctypes.c_double]
@@ -167,13 +168,16 @@ def _dp(a):
 
 
 def run(cfg: OCfg, dt: float, itimestep: int, fields: dict, diags: dict | None = None,
-        bounds=None, nthreads: int = 0) -> int:
+        bounds=None, nthreads: int = 0, ties: np.ndarray | None = None) -> int:
     """tempo_run over 3-D fields shaped (nj, nk, ni) (Fortran (i,k,j), i fastest).
 
     ``fields`` maps argument names (t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni,
     nr, nc, nwfa, nifa, ng, qb, land_input) to arrays; missing = not present.  Arrays
     with intent(inout) are updated in place.  ``diags`` maps diagnostic names to
-    preallocated float64 arrays (2-D (nj, ni), 3-D (nj, nk, ni)).
+    preallocated float64 arrays (2-D (nj, ni), 3-D (nj, nk, ni)).  ``ties``: optional
+    int32 array of the 2-D tile shape that receives, per column, 1 if the step passed
+    an index computation within one rounding of its discontinuity (see
+    ``oracle_set_tie_sink``).
     """
     lib = load()
     ref = fields.get("p")
@@ -194,8 +198,15 @@ def run(cfg: OCfg, dt: float, itimestep: int, fields: dict, diags: dict | None =
     args = [fields.get(n) for n in ("t", "th", "pii", "p", "w", "dz", "qv", "qc", "qr", "qi",
                                     "qs", "qg", "ni", "nr", "nc", "nwfa", "nifa", "ng", "qb",
                                     "qc_bl", "qcfrac_bl")]
-    rc = lib.oracle_run(ctypes.byref(cfg), float(dt), int(itimestep), *[_dp(a) for a in args],
-                        land_p, b, ctypes.byref(d), int(nthreads))
+    if ties is not None:
+        assert ties.dtype == np.int32 and ties.flags.c_contiguous
+        lib.oracle_set_tie_sink(ties.ctypes.data_as(_IP))
+    try:
+        rc = lib.oracle_run(ctypes.byref(cfg), float(dt), int(itimestep),
+                            *[_dp(a) for a in args], land_p, b, ctypes.byref(d), int(nthreads))
+    finally:
+        if ties is not None:
+            lib.oracle_set_tie_sink(None)
     return rc
 
 

@@ -16,6 +16,27 @@
 #include "oracle_common.h"
 #include "tempo_oracle.h"
 
+/* Rounding-tie detection (checker-only instrumentation, no effect on results).
+ * nint(x) and int(y) are discontinuous at half-integers and integers; where the
+ * reference's arithmetic puts an argument there up to one rounding (e.g. the graupel
+ * density class 10*rg/rb = 0.5 when rb sits at its clamp rg*1000/rho_g(1)), any
+ * last-bit difference of a libm result moves the index.  The column is flagged so
+ * that a comparison can tell such branch flips from real mismatches. */
+static _Thread_local int t_tie;      /* flags of the current column */
+static _Thread_local int t_tie_bit;  /* 1 before sedimentation, 2 in the final checks */
+static int *g_tie_sink;
+void oracle_set_tie_sink(int *flags) { g_tie_sink = flags; }
+static inline int nint_tie(double x) {
+  double f = x - floor(x);
+  if (fabs(f - 0.5) <= 1e-12 * fmax2(1.0, fabs(x))) t_tie |= t_tie_bit;
+  return nint(x);
+}
+static inline int int_tie(double y, int current_max) {
+  if ((int)y + 1 >= current_max && fabs(y - nearbyint(y)) <= 1e-12 * fmax2(1.0, fabs(y)))
+    t_tie |= 1;
+  return (int)y;
+}
+
 /* ty_tend (main:47-64): 74 FP64 process-rate columns, in the tend_work order :167-266 */
 enum {
   PRR_WAU, PNR_WAU, PNC_WAU, PRR_RCW, PNC_RCW, PNR_RCR,
@@ -350,7 +371,7 @@ static void graupel_check_and_update(int nz, const double *rho, int *l_qg, doubl
         ng[k] = fmax2(r2, (ng1d[k] + ngten[k] * dt) * rho[k]);
         rb[k] = fmin2(fmax2(rg[k] * meters3_to_liters / RHO_G(nrhg), (qb1d[k] + qbten[k] * dt) * rho[k]),
                       rg[k] * meters3_to_liters / RHO_G(1));
-        idx[k] = imax(1, imin(nint(10.0 * rg[k] / rb[k]) + 1, nrhg));
+        idx[k] = imax(1, imin(nint_tie(10.0 * rg[k] / rb[k]) + 1, nrhg));
         if (ng[k] <= r2) {
           hit_limit = 1;
           mvd_g[k] = 1.5e-3;
@@ -374,7 +395,7 @@ static void graupel_check_and_update(int nz, const double *rho, int *l_qg, doubl
         ng1d[k] = CGG(2, 1) * ogg3 * qg1d[k] * pow(lamg, bm_g) / AM_G(idx[k]);
         qb1d[k] = fmin2(fmax2(qg1d[k] * meters3_to_liters / RHO_G(nrhg), qb1d[k] + qbten[k] * dt),
                         meters3_to_liters * qg1d[k] / RHO_G(1));
-        idx[k] = imax(1, imin(nint(10.0 * qg1d[k] / qb1d[k]) + 1, nrhg));
+        idx[k] = imax(1, imin(nint_tie(10.0 * qg1d[k] / qb1d[k]) + 1, nrhg));
       } else {
         idx[k] = idx_bg1;
         double ygra1 = log10(fmax2(1.e-9, rg[k]));
@@ -413,7 +434,7 @@ static void graupel_init(int nz, const double *rho, const double *qg1d, double *
     if (qg1d[k] > r1) {
       double rg = qg1d[k] * rho[k];
       double rb = rg * meters3_to_liters / RHO_G(idx_bg1);
-      int idx = imax(1, imin(nint(10.0 * rg / rb) + 1, nrhg));
+      int idx = imax(1, imin(nint_tie(10.0 * rg / rb) + 1, nrhg));
       double mvd_g = 5.e-3;
       double lamg = (3.0 + mu_g + 0.672) / mvd_g;
       double ng = CGG(2, 1) * ogg3 * rg * pow(lamg, bm_g) / AM_G(idx);
@@ -637,7 +658,7 @@ static void rain_fallspeed(int nz, const double *rhof, const double *rr, const d
     if (fmax2(vt[k], vtn[k]) > 1.e-3) {
       *ktop = imax(*ktop, k + 1);
       double dz_by_vt = dz1d[k] / fmax2(vt[k], vtn[k]);
-      *substeps = imax(*substeps, (int)(dt / dz_by_vt + 1.0));
+      *substeps = imax(*substeps, int_tie(dt / dz_by_vt + 1.0, *substeps));
     }
   }
   if (*ktop == nz) *ktop = nz - 1;
@@ -671,7 +692,7 @@ static void graupel_fallspeed(int nz, const double *rhof, const double *rho, con
     if (vt[k] > 1.e-3) {
       *ktop = imax(*ktop, k + 1);
       double dz_by_vt = dz1d[k] / vt[k];
-      *substeps = imax(*substeps, (int)(dt / dz_by_vt + 1.0));
+      *substeps = imax(*substeps, int_tie(dt / dz_by_vt + 1.0, *substeps));
     }
   }
   if (*ktop == nz) *ktop = nz - 1;
@@ -709,7 +730,7 @@ static void snow_fallspeed(int nz, const double *rhof, const double *rs, const d
     if (vt[k] > 1.e-3) {
       *ktop = imax(*ktop, k + 1);
       double dz_by_vt = dz1d[k] / vt[k];
-      *substeps = imax(*substeps, (int)(dt / dz_by_vt + 1.0));
+      *substeps = imax(*substeps, int_tie(dt / dz_by_vt + 1.0, *substeps));
     }
   }
   if (*ktop == nz) *ktop = nz - 1;
@@ -732,7 +753,7 @@ static void ice_fallspeed(int nz, const double *rhof, const double *ri, const do
     if (vt[k] > 1.e-3) {
       *ktop = imax(*ktop, k + 1);
       double dz_by_vt = dz1d[k] / vt[k];
-      *substeps = imax(*substeps, (int)(dt / dz_by_vt + 1.0));
+      *substeps = imax(*substeps, int_tie(dt / dz_by_vt + 1.0, *substeps));
     }
   }
   if (*ktop == nz) *ktop = nz - 1;
@@ -1876,6 +1897,7 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
     w->smoe[k] = w->smof[k] = w->smog[k] = w->smoz[k] = w->ns[k] = 0.0;
     if (w->l_qs[k]) snow_moments_all(w, k, 2);
   }
+  t_tie_bit = 2; /* a tie in the final check moves only this level's graupel diagnostics */
   graupel_check_and_update(nz, w->rho, w->l_qg, qg1d, ng1d, qb1d, w->rg, w->ng, w->rb, w->idx_bg,
                            w->qgten, w->ngten, w->qbten, w->ilamg, w->mvd_g, dt, odt);
 
@@ -2001,6 +2023,8 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
       co.mhd = cfg->max_hail_diameter_flag ? o_mhd : NULL;
       co.ncmr = cfg->cloud_number_mixing_ratio_flag ? o_ncm : NULL;
       mdiag_t md;
+      t_tie = 0;
+      t_tie_bit = 1;
       tempo_main_col(cfg, is_first_step, qv1d, qc1d, qi1d, qr1d, qs1d, qg1d, qb ? qb1d : NULL,
                      ni1d, nr1d, nc ? nc1d : NULL, ng ? ng1d : NULL, nwfa ? nwfa1d : NULL,
                      nifa ? nifa1d : NULL, t1d, p1d, w1d, dz1d, land_input ? &land1d : NULL, dt, w,
@@ -2009,6 +2033,7 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
       for (int s = 0; s < 5; s++)
         if (md.substeps[s] > lmax[s]) lmax[s] = md.substeps[s];
       long c2 = T2(i, j);
+      if (g_tie_sink) g_tie_sink[c2] = t_tie;
       if (dg->rain_precip) dg->rain_precip[c2] = md.rain_precip;
       if (dg->ice_liquid_equiv_precip) dg->ice_liquid_equiv_precip[c2] = md.ice_liquid_equiv_precip;
       if (dg->snow_liquid_equiv_precip) dg->snow_liquid_equiv_precip[c2] = md.snow_liquid_equiv_precip;

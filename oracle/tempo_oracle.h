@@ -138,6 +138,14 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep,
  * [2..6] max substeps rain/graupel/snow/ice/cloud(=1). */
 void oracle_last_stats(long out[8]);
 
+/* Checker instrumentation: when flags != NULL, oracle_run writes per tile column
+ * (2-D diagnostic layout) the bits of the index computations that the column's step
+ * passed within one rounding of their discontinuity (nint at a half-integer, int at
+ * an integer): 1 = before or in sedimentation (graupel density class, substep
+ * count: can move every later field of the column), 2 = graupel density class in
+ * the final check (moves only that level's graupel diagnostics).  NULL turns it off. */
+void oracle_set_tie_sink(int *flags);
+
 #ifdef __cplusplus
 }
 #endif

@@ -111,6 +111,8 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
                                       ctypes.POINTER(ctypes.c_long)]
     lib.tempo_build_tables_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_float)]
     lib.tempo_last_stats_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_long)]
+    lib.tempo_set_kernel_timing.argtypes = [_VP, i]
+    lib.tempo_kernel_times_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_float)]
     _lib = lib
     return lib
 
@@ -262,6 +264,18 @@ class TempoContext:
         ms = ctypes.c_float()
         _check(load_library().tempo_build_tables_c(self._h, ctypes.byref(ms)))
         return ms.value
+
+    KERNELS = ("prep", "points", "sedim", "final")
+
+    def set_kernel_timing(self, on: bool = True):
+        """Record CUDA events around the four kernels of each later run."""
+        _check(load_library().tempo_set_kernel_timing(self._h, int(bool(on))))
+
+    def kernel_times(self) -> dict:
+        """Durations (ms) of the four kernels of the last run; waits for it."""
+        ms = (ctypes.c_float * 4)()
+        _check(load_library().tempo_kernel_times_c(self._h, ms))
+        return dict(zip(self.KERNELS, (float(x) for x in ms)))
 
     def stats(self) -> dict:
         out = (ctypes.c_long * 8)()

@@ -71,6 +71,8 @@ struct tempo_ctx {
   int precision = TEMPO_PREC_FP64;
   TempoConsts<double> c64{};
   TempoConsts<float> c32{};
+  IslandConsts<double> i64{};
+  IslandConsts<df> idf{};
   TempoBins bins{};
   DevTables64 t64{};
   // FP32 copies for the mixed kernels
@@ -84,6 +86,8 @@ struct tempo_ctx {
   long launches = 0;
   std::vector<Mirror> mirrors;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool kernel_timing = false;
+  cudaEvent_t kev[kStepLaunches + 1] = {};
 };
 
 namespace {
@@ -432,22 +436,48 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   a.dt = dt;
   a.nc_single = resolve_nc_value(cfg);
   a.flags = f;
+  // decay rates of the aerosol initial profiles (init_*_friendly_aerosols,
+  // aerosols:14-73; h_01 = 0.8 km), host libm as in the reference
+  a.niccn3 = -1.0 * std::log(naccn1 / naccn0) / 0.8;
+  a.niin3 = -1.0 * std::log(nain1 / nain0) / 0.8;
   const bool mixed = c->precision == TEMPO_PREC_MIXED;
+  // scratch: island-type point fields (double or double-float, 8 bytes either way),
+  // bulk-type fall speeds, per-slot sums, slot map, masks and the slot counter
   const size_t rsz = mixed ? sizeof(float) : sizeof(double);
-  const size_t sd_bytes = (size_t)SD_N * a.nz * a.ncol_pad * sizeof(double);
-  const size_t sr_bytes = (size_t)SR_N * a.nz * a.ncol_pad * rsz;
-  if (int rc = ensure_scratch(c, sd_bytes + sr_bytes + 256)) return rc;
-  a.sd = (double*)c->scratch;
-  a.sr = (void*)((char*)c->scratch + (sd_bytes + 255) / 256 * 256);
+  const size_t npad = (size_t)a.ncol_pad, nzs = (size_t)a.nz;
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t sd_bytes = al((size_t)SD_N * nzs * npad * 8);
+  const size_t sr_bytes = al((size_t)SR_N * nzs * npad * rsz);
+  const size_t sc_bytes = al((size_t)SC_N * npad * 8);
+  const size_t act_bytes = al(npad * sizeof(int));
+  const size_t pm_bytes = al(nzs * npad);
+  const size_t cm_bytes = al(npad);
+  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + 256;
+  if (int rc = ensure_scratch(c, total)) return rc;
+  char* sp = (char*)c->scratch;
+  a.sd = sp;
+  sp += sd_bytes;
+  a.sr = sp;
+  sp += sr_bytes;
+  a.sc = sp;
+  sp += sc_bytes;
+  a.act = (int*)sp;
+  sp += act_bytes;
+  a.pmask = (uint8_t*)sp;
+  sp += pm_bytes;
+  a.cmask = (uint8_t*)sp;
+  sp += cm_bytes;
+  a.nact = (unsigned int*)sp;
   a.stats = c->d_stats;
   CUDA_TRY(cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s));
+  CUDA_TRY(cudaMemsetAsync(a.nact, 0, sizeof(unsigned int), s));
   c->last_cols = a.ncol;
-  c->launches = 1;
+  c->launches = kStepLaunches;
   if (!mixed) {
     if constexpr (sizeof(S) == sizeof(double)) {
       Tables<double> T{c->t64.t_efrw, c->t64.t_efsw, c->t64.tnc_wev, c->t64.tps_iaus, c->t64.tni_iaus,
                        c->t64.tpi_ide, c->t64.tnccn, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
-      CUDA_TRY(launch_step_f64(a, T, c->c64, s));
+      CUDA_TRY(launch_step_f64(a, T, c->c64, c->i64, s, c->kernel_timing ? c->kev : nullptr));
       return TEMPO_OK;
     } else {
       return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
@@ -456,9 +486,9 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
                   c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
   if constexpr (sizeof(S) == sizeof(double))
-    CUDA_TRY(launch_step_mixed_f64(a, T, c->c32, c->c64, s));
+    CUDA_TRY(launch_step_mixed_f64(a, T, c->c32, c->idf, s, c->kernel_timing ? c->kev : nullptr));
   else
-    CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->c64, s));
+    CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->idf, s, c->kernel_timing ? c->kev : nullptr));
   return TEMPO_OK;
 }
 
@@ -601,6 +631,8 @@ int tempo_init_c(const int* aerosolaware_flag, const int* hailaware_flag, const 
     return bail(fail(TEMPO_ERR_CUDA, "stream/event creation: %s", cudaGetErrorString(e)));
   make_consts(&c->c64, c->hail);
   narrow_consts(c->c64, &c->c32);
+  make_island_consts(c->c64, &c->i64);
+  make_island_consts(c->c64, &c->idf);
   make_bins(&c->bins);
   int rc;
   if ((rc = alloc_tables(c))) return bail(rc);
@@ -631,6 +663,8 @@ int tempo_ctx_destroy(tempo_ctx_t* c) {
   for (auto& m : c->mirrors) cudaFree(m.d);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (cudaEvent_t& e : c->kev)
+    if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return TEMPO_OK;
@@ -641,6 +675,24 @@ int tempo_set_precision(tempo_ctx_t* c, int precision) {
   if (precision != TEMPO_PREC_FP64 && precision != TEMPO_PREC_MIXED)
     return fail(TEMPO_ERR_ARG, "unknown precision %d", precision);
   c->precision = precision;
+  return TEMPO_OK;
+}
+
+int tempo_set_kernel_timing(tempo_ctx_t* c, int on) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  CUDA_TRY(cudaSetDevice(c->device));
+  if (on && !c->kev[0])
+    for (cudaEvent_t& e : c->kev) CUDA_TRY(cudaEventCreate(&e));
+  c->kernel_timing = on != 0;
+  return TEMPO_OK;
+}
+
+int tempo_kernel_times_c(tempo_ctx_t* c, float ms[4]) {
+  if (!c || !ms) return fail(TEMPO_ERR_ARG, "NULL argument");
+  if (!c->kernel_timing) return fail(TEMPO_ERR_STATE, "kernel timing is off (tempo_set_kernel_timing)");
+  CUDA_TRY(cudaSetDevice(c->device));
+  CUDA_TRY(cudaEventSynchronize(c->kev[kStepLaunches]));
+  for (int i = 0; i < kStepLaunches; i++) CUDA_TRY(cudaEventElapsedTime(&ms[i], c->kev[i], c->kev[i + 1]));
   return TEMPO_OK;
 }
 

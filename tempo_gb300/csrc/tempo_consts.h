@@ -81,6 +81,20 @@ void make_consts(TempoConsts<double>* c, bool hailaware);
 // Narrows every member to float for the mixed-precision kernels.
 void narrow_consts(const TempoConsts<double>& d, TempoConsts<float>* f);
 
+// Constants of the thermodynamic island, in the island type (double, or the
+// double-float pair of the mixed form split once on the host).
+template <class I>
+struct IslandConsts {
+  I rho_not, orv, roverrv, lfus;
+};
+template <class I>
+inline void make_island_consts(const TempoConsts<double>& d, IslandConsts<I>* o) {
+  o->rho_not = I(d.rho_not);
+  o->orv = I(d.orv);
+  o->roverrv = I(d.roverrv);
+  o->lfus = I(d.lfus);
+}
+
 // Bin arrays needed by the table builders (host copies; params:613-722).
 struct TempoBins {
   double dc[nbc], dtc[nbc], di[nbi], dti[nbi], dr[nbr], dtr[nbr], ds[nbs], dts[nbs];

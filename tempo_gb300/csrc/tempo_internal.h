@@ -6,6 +6,7 @@
 #include <cstdint>
 
 #include "tempo_consts.h"
+#include "tempo_dfloat.cuh"
 
 namespace tg {
 
@@ -14,15 +15,18 @@ template <class S> struct StepArgs;
 
 // tempo_step_f64.cu (FP64 drop-in, compiled without FMA contraction)
 cudaError_t launch_step_f64(const StepArgs<double>& a, const Tables<double>& t,
-                            const TempoConsts<double>& c64, cudaStream_t s);
+                            const TempoConsts<double>& c64, const IslandConsts<double>& i64,
+                            cudaStream_t s, const cudaEvent_t* ev);
 
-// tempo_step_f32.cu (mixed precision: FP32 bulk, FP64 islands)
+// tempo_step_f32.cu (mixed precision: FP32 bulk, double-float islands)
 cudaError_t launch_step_mixed_f32(const StepArgs<float>& a, const Tables<float>& t,
-                                  const TempoConsts<float>& c32, const TempoConsts<double>& c64,
-                                  cudaStream_t s);
+                                  const TempoConsts<float>& c32, const IslandConsts<df>& idf,
+                                  cudaStream_t s, const cudaEvent_t* ev);
 cudaError_t launch_step_mixed_f64(const StepArgs<double>& a, const Tables<float>& t,
-                                  const TempoConsts<float>& c32, const TempoConsts<double>& c64,
-                                  cudaStream_t s);
+                                  const TempoConsts<float>& c32, const IslandConsts<df>& idf,
+                                  cudaStream_t s, const cudaEvent_t* ev);
+// kernels launched per step (prep, points, sedim, final)
+constexpr int kStepLaunches = 4;
 
 // tempo_tables.cu (FP64 table construction on the GPU)
 struct DevTables64 {

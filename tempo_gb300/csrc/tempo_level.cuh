@@ -8,18 +8,25 @@
 // (every operation in the reference's order, compiled without FMA contraction) and
 // float for the mixed form.  The thermodynamic island -- temperature, vapour,
 // density, saturation mixing ratios, (super)saturations and the saturation
-// adjustment -- is always double (type D): differences of nearly equal
-// quantities (qv - qvs) decide condensation and must not lose FP32 digits.
+// adjustment -- has the island type Isl<R>: double in the FP64 drop-in, double-float
+// (tempo_dfloat.cuh, ~48 bits on the FP32 pipes) in the mixed form.  Differences of
+// nearly equal quantities (qv - qvs) decide condensation and must not lose digits.
 #pragma once
 
 #include <cstdint>
 
 #include "tempo_consts.h"
+#include "tempo_dfloat.cuh"
 #include "tempo_types.h"
 
 namespace tg {
 
 using D = double;
+
+// island type of a bulk type
+template <class R> struct IslandOf { using type = double; };
+template <> struct IslandOf<float> { using type = df; };
+template <class R> using Isl = typename IslandOf<R>::type;
 
 // ---------------------------------------------------------------------------------
 // math wrappers: accurate library functions for the chosen type (no fast-math)
@@ -73,8 +80,9 @@ template <class T> __device__ __forceinline__ T ld(const T* p) { return __ldg(p)
 // ---------------------------------------------------------------------------------
 template <class R>
 struct Lev {
-  const TempoConsts<R>* cs;  // constant set of the bulk type
-  const TempoConsts<D>* cd;  // double constant set (thermodynamic island)
+  using I = Isl<R>;
+  const TempoConsts<R>* cs;   // constant set of the bulk type
+  const IslandConsts<I>* ci;  // constants of the thermodynamic island
   // prognostic "1d" values (after the initial checks) and hydrometeor state
   R qc1d, nc1d, qr1d, nr1d, qi1d, ni1d, qs1d, qg1d, ng1d, qb1d;
   bool l_qc, l_qr, l_qi, l_qs, l_qg;
@@ -83,7 +91,7 @@ struct Lev {
   R ilamc, ilami, ilamr, ilamg, mvd_c, mvd_r, mvd_g;
   R smob, smoc, smo0, smo1, smo2, smoe, smof, smog, smoz;
   // thermodynamic island
-  D t1d, qv1d, temp, qv, rho, qvs, qvsi, delqvs, ssatw, ssati, tten, qvten;
+  I t1d, qv1d, temp, qv, rho, qvs, qvsi, delqvs, ssatw, ssati, tten, qvten;
   R pres;
   R rhof, rhof2, diffu, visco, vsc2, tcond, lvap, ocp, lvt2;
   R qcten, ncten, qiten, niten, qrten, nrten, qsten, qgten, ngten, qbten, nwfaten, nifaten;
@@ -119,10 +127,10 @@ template <class R> __device__ __forceinline__ R rho_g(int m) { return R(rho_gd(m
 // ---------------------------------------------------------------------------------
 // utils.F90
 // ---------------------------------------------------------------------------------
-// calc_rslf / calc_rsif (utils:285-331), always double
-__device__ __forceinline__ D calc_rslf(D p, D t) {
-  D x = Max(-80.0, t - 273.16);
-  D esl = .611583699E03 +
+// calc_rslf / calc_rsif (utils:285-331) in the island type
+template <class I> __device__ __forceinline__ I calc_rslf(I p, I t) {
+  I x = Max(I(-80.0), t - 273.16);
+  I esl = .611583699E03 +
           x * (.444606896E02 +
                x * (.143177157e01 +
                     x * (.264224321e-1 +
@@ -132,9 +140,9 @@ __device__ __forceinline__ D calc_rslf(D p, D t) {
   esl = Min(esl, p * 0.15);
   return .622 * esl / (p - esl);
 }
-__device__ __forceinline__ D calc_rsif(D p, D t) {
-  D x = Max(-80.0, t - 273.16);
-  D esi = .609868993e03 +
+template <class I> __device__ __forceinline__ I calc_rsif(I p, I t) {
+  I x = Max(I(-80.0), t - 273.16);
+  I esi = .609868993e03 +
           x * (.499320233e02 +
                x * (.184672631e01 +
                     x * (.402737184e-1 +
@@ -142,7 +150,7 @@ __device__ __forceinline__ D calc_rsif(D p, D t) {
                               x * (.521693933e-5 +
                                    x * (.307839583e-7 + x * (.105785160e-9 + x * .161444444e-12)))))));
   esi = Min(esi, p * 0.15);
-  return .622 * esi / Max(1.e-4, (p - esi));
+  return .622 * esi / Max(I(1.e-4), (p - esi));
 }
 
 template <class R> __device__ __forceinline__ int get_nuc(R nc) {  // utils:334-346
@@ -475,40 +483,43 @@ __device__ __forceinline__ void graupel_init(Lev<R>& L) {
 // thermo_vars (main:1263-1310) for one level; returns ssati > 0
 template <class R>
 __device__ bool thermo(Lev<R>& L) {
-  D otemp = 1.0 / L.temp;
-  D tempc = L.temp - t0;
-  L.rhof = R(Sqrt(L.cd->rho_not / L.rho));
+  using I = Isl<R>;
+  I otemp = 1.0 / L.temp;
+  I tempc = L.temp - t0;
+  L.rhof = R(Sqrt(L.ci->rho_not / L.rho));
   L.rhof2 = Sqrt(L.rhof);
-  L.qvs = calc_rslf(D(L.pres), L.temp);
-  L.delqvs = Max(0.0, calc_rslf(D(L.pres), t0) - L.qv);
+  L.qvs = calc_rslf(I(L.pres), L.temp);
+  L.delqvs = Max(I(0.0), calc_rslf(I(L.pres), I(t0)) - L.qv);
   if (tempc <= 0.0)
-    L.qvsi = calc_rsif(D(L.pres), L.temp);
+    L.qvsi = calc_rsif(I(L.pres), L.temp);
   else
     L.qvsi = L.qvs;
-  D satw = L.qv / L.qvs;
-  D sati = L.qv / L.qvsi;
+  I satw = L.qv / L.qvs;
+  I sati = L.qv / L.qvsi;
   L.ssatw = satw - 1.0;
   L.ssati = sati - 1.0;
-  if (Fabs(L.ssatw) < eps) L.ssatw = 0.0;
-  if (Fabs(L.ssati) < eps) L.ssati = 0.0;
+  if (Fabs(L.ssatw) < eps) L.ssatw = I(0.0);
+  if (Fabs(L.ssati) < eps) L.ssati = I(0.0);
   R rtc = R(tempc);
   L.diffu = R(2.11e-5) * Pow(R(L.temp / t0), R(1.94)) * (R(101325.0) / L.pres);
   if (tempc >= 0.0)
     L.visco = (R(1.718) + R(0.0049) * rtc) * R(1.0e-5);
   else
     L.visco = (R(1.718) + R(0.0049) * rtc - R(1.2e-5) * rtc * rtc) * R(1.0e-5);
-  D ocp = 1.0 / (cp * (1.0 + 0.887 * L.qv));
-  L.ocp = R(ocp);
+  // multiplicative factors: the bulk type suffices (they scale, never cancel)
+  R ocp = R(1.0) / (R(cp) * (R(1.0) + R(0.887) * R(L.qv)));
+  L.ocp = ocp;
   L.vsc2 = Sqrt(R(L.rho) / L.visco);
-  D lvap = lvap0 + (2106.0 - 4218.0) * tempc;
-  L.lvap = R(lvap);
+  R lvap = R(lvap0) + (R(2106.0) - R(4218.0)) * rtc;
+  L.lvap = lvap;
   L.tcond = (R(5.69) + R(0.0168) * rtc) * R(1.0e-5) * R(418.936);
-  L.lvt2 = R(lvap * lvap * ocp * L.cd->orv * otemp * otemp);
+  L.lvt2 = lvap * lvap * ocp * R(L.ci->orv) * R(otemp) * R(otemp);
   return L.ssati > 0.0;
 }
 
-__device__ __forceinline__ D rho_of(const TempoConsts<D>& cd, D pres, D temp, D qv) {  // main:325
-  return cd.roverrv * pres / (rdry * temp * (qv + cd.roverrv));
+template <class I>
+__device__ __forceinline__ I rho_of(const IslandConsts<I>& ci, I pres, I temp, I qv) {  // main:325
+  return ci.roverrv * pres / (rdry * temp * (qv + ci.roverrv));
 }
 
 }  // namespace tg

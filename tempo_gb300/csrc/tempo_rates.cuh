@@ -24,8 +24,8 @@ __device__ __forceinline__ int decade_index(R x, int n2, int nmax) {
   int idx = Int(x / Ipow(R(10.0), n)) + 10 * (n - n2) - (n - n2);
   return max(1, min(idx, nmax));
 }
-template <class R> __device__ __forceinline__ int temperature_index(D tempk) {  // main:2511-2523
-  D tempc = tempk - t0;
+template <class R> __device__ __forceinline__ int temperature_index(Isl<R> tempk) {  // main:2511-2523
+  Isl<R> tempc = tempk - t0;
   int it = Int((R(tempc) - R(2.5)) / R(5.0)) - 1;
   it = max(1, -it);
   return min(it, ntb_t);
@@ -667,11 +667,11 @@ __device__ void check_over_depletion(const Lev<R>& L, Tend<R>& t, R odt) {
 // sum_tendencies (main:1441-1513)
 template <class R>
 __device__ void sum_tendencies(Lev<R>& L, const Tend<R>& t) {
-  const TempoConsts<D>& cd = *L.cd;
+  using I = Isl<R>;
   R orho = R(1. / L.rho);
-  D orho_d = 1. / L.rho;
-  D lfus2 = lsub - D(L.lvap);
-  L.qvten = L.qvten + D(-t.pri_inu - t.pri_iha - t.pri_ide - t.prs_ide - t.prs_sde - t.prg_gde) * orho_d;
+  I orho_d = 1. / L.rho;
+  I lfus2 = lsub - I(L.lvap);
+  L.qvten = L.qvten + I(-t.pri_inu - t.pri_iha - t.pri_ide - t.prs_ide - t.prs_sde - t.prg_gde) * orho_d;
   L.qcten = L.qcten + (-t.prr_wau - t.pri_wfz - t.prr_rcw - t.prs_scw - t.prg_scw - t.prg_gcw) * orho;
   L.ncten = L.ncten + (-t.pnc_wau - t.pnc_rcw - t.pni_wfz - t.pnc_scw - t.pnc_gcw) * orho;
   L.qiten = L.qiten + (t.pri_inu + t.pri_iha + t.pri_ihm + t.pri_wfz + t.pri_rfz + t.pri_ide -
@@ -691,14 +691,14 @@ __device__ void sum_tendencies(Lev<R>& L, const Tend<R>& t) {
   L.qbten = L.qbten + (t.pbg_scw + t.pbg_rfz + t.pbg_gcw + t.pbg_rci + t.pbg_rcs + t.pbg_rcg +
                        t.pbg_sml - t.pbg_gml +
                        R(meters3_to_liters) * (t.prg_gde - t.prg_ihm) / rho_g<R>(L.idx_bg)) * orho;
-  D ocp = D(L.ocp);
+  I ocp = I(L.ocp);
   if (L.temp < t0) {
-    L.tten = L.tten + (lsub * ocp * D(t.pri_inu + t.pri_ide + t.prs_ide + t.prs_sde + t.prg_gde + t.pri_iha) +
-                       lfus2 * ocp * D(t.pri_wfz + t.pri_rfz + t.prg_rfz + t.prs_scw + t.prg_scw +
+    L.tten = L.tten + (lsub * ocp * I(t.pri_inu + t.pri_ide + t.prs_ide + t.prs_sde + t.prg_gde + t.pri_iha) +
+                       lfus2 * ocp * I(t.pri_wfz + t.pri_rfz + t.prg_rfz + t.prs_scw + t.prg_scw +
                                        t.prg_gcw + t.prg_rcs + t.prs_rcs + t.prr_rci + t.prg_rcg)) * orho_d;
   } else {
-    L.tten = L.tten + (cd.lfus * ocp * D(-t.prr_sml - t.prr_gml - t.prr_rcg - t.prr_rcs) +
-                       lsub * ocp * D(t.prs_sde + t.prg_gde)) * orho_d;
+    L.tten = L.tten + (L.ci->lfus * ocp * I(-t.prr_sml - t.prr_gml - t.prr_rcg - t.prr_rcs) +
+                       lsub * ocp * I(t.prs_sde + t.prg_gde)) * orho_d;
   }
 }
 
@@ -747,17 +747,19 @@ __device__ void cloud_condensation(const Lev<R>& L, Tend<R>& t, const Tables<R>&
                                    uint32_t f, R ncsave, R dt, R odt) {
   const TempoConsts<R>& c = *L.cs;
   if (Fabs(L.ssatw) < eps) return;
+  using I = Isl<R>;
   R orho = R(1.0 / L.rho);
-  D lvt2 = D(L.lvt2);
-  D clap = (L.qv - L.qvs) / (1.0 + lvt2 * L.qvs);
-  for (int n = 1; n <= 3; n++) {
-    D fcd = L.qvs * Exp(lvt2 * clap) - L.qv + clap;
-    D dfcd = L.qvs * lvt2 * Exp(lvt2 * clap) + 1.0;
+  I lvt2 = I(L.lvt2);
+  I clap = (L.qv - L.qvs) / (1.0 + lvt2 * L.qvs);
+  for (int n = 1; n <= 3; n++) {  // Newton on qvs exp(lvt2 c) - qv + c = 0 (main:2002-2007)
+    const I ex = Exp(lvt2 * clap);
+    I fcd = L.qvs * ex - L.qv + clap;
+    I dfcd = L.qvs * lvt2 * ex + 1.0;
     clap = clap - fcd / dfcd;
   }
-  D xrc = D(L.rc) + clap * L.rho;
+  I xrc = I(L.rc) + clap * L.rho;
   if (xrc > r1) {
-    t.prw_vcd = R(clap * D(odt));
+    t.prw_vcd = R(clap * I(odt));
     if (clap > eps) {
       R xnc;
       if (f & F_NWFA)
@@ -823,7 +825,7 @@ __device__ void rain_evaporation(const Lev<R>& L, Tend<R>& t, R odt) {
     t.prv_rev = t1_evap * L.diffu * R(-L.ssatw) * n0_r * rvs *
                 (c.t1_qr_ev * Pow(L.ilamr, c.cre[9]) +
                  c.t2_qr_ev * L.vsc2 * L.rhof2 * Pow(lamr + R(0.5) * R(fv_r), -c.cre[10]));
-    R rate_max = Min((L.rr * orho * odt), R((L.qvs - L.qv) * D(odt)));
+    R rate_max = Min((L.rr * orho * odt), R((L.qvs - L.qv) * Isl<R>(odt)));
     t.prv_rev = Min(rate_max, t.prv_rev * orho);
     if (t.prr_gml > R(0.0)) {
       R eva_factor = Min(R(1.0), R(0.01) + R(0.99 - 0.01) * (tempc / R(20.0)));

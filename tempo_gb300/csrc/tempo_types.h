@@ -41,18 +41,31 @@ enum : uint32_t {
   F_DT_RIME = 1u << 16  // dt > timestep_conversion_rime_to_rain
 };
 
-// scratch fields stored in double (thermo island and sedimentation island)
+// per-point scratch fields in the island type (thermodynamic and sedimentation islands);
+// SD_HGT (height of the level for the aerosol profiles) is written only when nwfa or
+// nifa is absent
 enum SDField : int {
   SD_TTEN, SD_QV, SD_RHO,
   SD_XRR, SD_XNR, SD_XRG, SD_XNG, SD_XRB, SD_XRS, SD_XRI, SD_XNI, SD_XRC, SD_XNC,
   SD_TQR, SD_TNR, SD_TQG, SD_TNG, SD_TQB, SD_TQS, SD_TQI, SD_TNI, SD_TQC, SD_TNC,
-  SD_N
+  SD_HGT, SD_N
 };
-// scratch fields stored in the bulk type R (fall-speed candidates; < 0 = absent)
+// per-point scratch fields in the bulk type R (fall-speed candidates; < 0 = absent)
 enum SRField : int {
   SR_VTR, SR_VTNR, SR_VTG, SR_VTNG, SR_VTSA, SR_VTSB, SR_VTI, SR_VTNI, SR_VTC, SR_VTNC, SR_N
 };
+// per-column scratch in the island type: precipitation sums of the sedimentation
+enum SCField : int { SC_PR, SC_PG, SC_PS, SC_PI, SC_PC, SC_N };
+// per-point existence bits after phase A (any(l_q*) drives the sedimentation)
+enum PMaskBit : uint8_t { PM_QR = 1, PM_QG = 2, PM_QS = 4, PM_QI = 8, PM_QC = 16 };
+// per-column bits
+enum CMaskBit : uint8_t { CM_GINIT = 1 };
 
+// One step's arguments.  The step runs as four kernels over the tile's columns:
+// prep (per column: early-exit test, compaction of active columns into slots),
+// points (per active level: phase A), sedim (per active column: sedimentation),
+// final (per active level: phase C).  Scratch is indexed by active-column slot s,
+// [field][level][slot] with slot fastest.
 template <class S>
 struct StepArgs {
   S *t, *th;
@@ -69,9 +82,15 @@ struct StepArgs {
   long ncol, ncol_pad;
   double dt;
   double nc_single;   // single-moment cloud number (m^-3) when nc is absent and no land
+  double niccn3, niin3;  // decay rates of the aerosol initial profiles (aerosols:14-73)
   uint32_t flags;
-  double* sd;         // [SD_N][nz][ncol_pad]
+  void* sd;           // Isl<R>[SD_N][nz][ncol_pad]
   void* sr;           // R[SR_N][nz][ncol_pad]
+  void* sc;           // Isl<R>[SC_N][ncol_pad]
+  int* act;           // [ncol_pad] column of each active slot
+  unsigned int* nact; // active-slot counter (zero before prep)
+  uint8_t* pmask;     // [nz][ncol_pad]
+  uint8_t* cmask;     // [ncol_pad]
   unsigned long long* stats;  // [0] early exits, [1..5] max substeps
 };
 

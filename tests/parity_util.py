@@ -30,11 +30,12 @@ def make_diags(shape, diag3=DIAG3, dtype=np.float64):
     return d
 
 
-def run_oracle(oracle, cfg_over: dict, wl, fields=None, itimestep=1, diag3=DIAG3, nthreads=0):
+def run_oracle(oracle, cfg_over: dict, wl, fields=None, itimestep=1, diag3=DIAG3, nthreads=0,
+               ties=None):
     f = {k: v.copy() for k, v in (fields or wl.fields).items()}
     d = make_diags(f["p"].shape, diag3)
     cfg = oracle.default_cfgs(**cfg_over)
-    rc = oracle.run(cfg, wl.dt, itimestep, f, d, nthreads=nthreads)
+    rc = oracle.run(cfg, wl.dt, itimestep, f, d, nthreads=nthreads, ties=ties)
     assert rc == 0, f"oracle_run returned {rc}"
     return f, d
 
@@ -75,32 +76,48 @@ def worst(errs):
     return k, errs[k][0]
 
 
-def graupel_density_ties(qg, qb, rtol=1e-12):
-    """Levels at the rounding tie of the graupel density class.
-
-    The class is idx_bg = nint(10 * rg / rb) + 1 (module_mp_tempo_main.F90:1172, 1198).
-    Where the volume rb sits at its low-density clamp rg * 1000 / rho_g(1) (main:1169-1170),
-    10 * rg / rb is 0.5 up to one rounding, so a one-ulp difference in rg -- e.g. from
-    the device's and the host's pow/exp -- moves the class between 1 and 2.  Those
-    classes differ in am_g by rho_g(2) / rho_g(1) = 2, so the median volume diameter
-    (proportional to am_g**(-1/3)) moves by exactly 2**(1/3), while mass and number
-    (independent of am_g, main:1175-1196) do not.  Returns the boolean mask of such
-    levels, judged on the final qg, qb."""
-    qg = np.asarray(qg, dtype=np.float64)
-    qb = np.asarray(qb, dtype=np.float64)
-    ok = (qg > 1e-12) & (qb > 0)
-    r = np.where(ok, 10.0 * qg / np.where(qb > 0, qb, 1.0), 0.0)
-    return ok & (np.abs(r - 0.5) <= rtol * 0.5)
+def _col_err(a, b, floor):
+    """Per-column max relative error of a 2-D (nj, ni) or 3-D (nj, nk, ni) field."""
+    e = rel_err(a, b, floor)
+    return e.max(axis=1) if e.ndim == 3 else e
 
 
-def mvd_g_tie_flips(mvd_got, mvd_want, ties, rtol=1e-12):
-    """Splits graupel MVD differences at density-class ties into class flips (ratio
-    exactly 2**(+-1/3)) and returns (number of flips, max relative error of the rest)."""
-    a = np.asarray(mvd_got, dtype=np.float64)
-    b = np.asarray(mvd_want, dtype=np.float64)
-    e = np.abs(a - b) / np.maximum(np.abs(b), FLOOR["graupel_med_vol_diam"])
-    ratio = np.where(b > 0, a / np.where(b > 0, b, 1.0), 1.0)
-    c = 2.0 ** (1.0 / 3.0)
-    flip = ties & ((np.abs(ratio - c) <= 1e-10 * c) | (np.abs(ratio - 1.0 / c) <= 1e-10 / c))
-    rest = np.where(flip, 0.0, e)
-    return int(flip.sum()), float(rest.max())
+GRAUPEL_DIAGS = ("graupel_med_vol_diam", "refl10cm", "max_hail_diameter_sfc",
+                 "max_hail_diameter_column")
+
+
+def compare_with_ties(fa, da, fb, db, ties, tol, names3=OUT3):
+    """Column-wise comparison of a against the oracle b that tells rounding-tie branch
+    flips from real mismatches.
+
+    ``ties`` (int, (nj, ni)) comes from the oracle's tie sink: bit 1 = the column's
+    step passed an index computation within one rounding of its discontinuity before
+    or during sedimentation (the graupel density class nint(10 rg / rb) at the
+    low-density clamp rb = rg * 1000 / rho_g(1), module_mp_tempo_main.F90:1169-1171,
+    where 10 rg / rb = 0.5 up to one rounding; or a substep count int(dt vt / dz + 1));
+    bit 2 = the same class tie in the final check (moves only that level's graupel
+    diagnostics).  A last-bit difference of a libm result (the device's vs glibc's)
+    can move such an index, and with it the column.
+
+    Returns (worst error over unflagged columns, worst error of the non-graupel-
+    diagnostic outputs over bit-2-only columns, number of bit-1 columns that deviate
+    beyond tol, names of the fields of the worst unflagged error)."""
+    ties = np.asarray(ties)
+    b1 = (ties & 1).astype(bool)
+    b2only = ((ties & 2).astype(bool)) & ~b1
+    clean = ~(b1 | b2only)
+    worst_clean, worst_b2, which = 0.0, 0.0, None
+    dev1 = np.zeros_like(b1)
+    items = [(n, fa, fb) for n in names3 if n in fa and n in fb]
+    items += [(n, da, db) for n in tuple(DIAG2) + tuple(DIAG3) if n in da and n in db]
+    for n, A, B in items:
+        assert not np.isnan(B[n]).any(), f"oracle left {n} unset"
+        assert not np.isnan(A[n]).any(), f"{n} not written"
+        e = _col_err(A[n], B[n], FLOOR[n])
+        m = float(e[clean].max()) if clean.any() else 0.0
+        if m > worst_clean:
+            worst_clean, which = m, n
+        if n not in GRAUPEL_DIAGS and b2only.any():
+            worst_b2 = max(worst_b2, float(e[b2only].max()))
+        dev1 |= b1 & (e > tol)
+    return worst_clean, worst_b2, int(dev1.sum()), which

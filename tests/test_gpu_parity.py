@@ -6,8 +6,7 @@ format).  Table construction on the GPU: within 1e-12 relative of the oracle's."
 import numpy as np
 import pytest
 
-from parity_util import (compare, graupel_density_ties, mvd_g_tie_flips, run_gpu,
-                         run_oracle, worst)
+from parity_util import compare, compare_with_ties, run_gpu, run_oracle, worst
 
 pytestmark = pytest.mark.gpu
 TOL64 = 1e-12
@@ -76,19 +75,16 @@ def test_config2_hail_fp64_matches_oracle(ctx_hail, oracle_mod):
     wl = W.config2(ni=32, nj=16)
     over = dict(hailaware_flag=1, rain_med_vol_diam_flag=1, graupel_med_vol_diam_flag=1,
                 cloud_number_mixing_ratio_flag=1)
-    fo, do = run_oracle(oracle_mod, over, wl)
+    ties = np.zeros(wl.fields["p"].shape[::2], np.int32)
+    fo, do = run_oracle(oracle_mod, over, wl, ties=ties)
     fg, dg = run_gpu(ctx_hail, over, wl)
-    # the graupel MVD may flip by 2**(1/3) at exact density-class ties (see
-    # parity_util.graupel_density_ties); everything else, the MVD elsewhere included,
-    # holds the FP64 tolerance
-    ties = graupel_density_ties(fo["qg"], fo["qb"])
-    flips, e_mvd = mvd_g_tie_flips(dg["graupel_med_vol_diam"], do["graupel_med_vol_diam"], ties)
-    assert e_mvd < TOL64, e_mvd
-    assert flips <= ties.sum() <= 0.01 * (fo["qg"] > 1e-12).sum(), (flips, ties.sum())
-    dg = {k: v for k, v in dg.items() if k != "graupel_med_vol_diam"}
-    errs = compare(fg, dg, fo, do)
-    name, e = worst(errs)
-    assert e < TOL64, (name, e, errs)
+    # hail-aware graupel has exact rounding ties in its density class (see
+    # parity_util.compare_with_ties): unflagged columns hold the FP64 tolerance, and
+    # at most 1 % of the columns may move by a class flip
+    clean, b2, moved, which = compare_with_ties(fg, dg, fo, do, ties, TOL64)
+    assert clean < TOL64, (which, clean)
+    assert b2 < TOL64, b2
+    assert moved <= max(1, ties.size // 100), (moved, int((ties & 1).astype(bool).sum()))
 
 
 def test_config1_multistep_fp64_matches_oracle(ctx_nohail, oracle_mod):
