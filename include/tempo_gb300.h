@@ -193,6 +193,26 @@ int tempo_last_stats_c(tempo_ctx_t *ctx, long out[8]);
 int tempo_set_kernel_timing(tempo_ctx_t *ctx, int on);
 int tempo_kernel_times_c(tempo_ctx_t *ctx, float ms[4]);
 
+/* No reference counterpart.  Autotuner of the mixed form on FP32 device storage: runs
+ * the step `reps` times with every variant of its per-level kernel (thread-to-work
+ * mapping and register budget) on private copies of the given state -- the caller's
+ * arrays are not modified -- times the per-level kernel with CUDA events on `stream`,
+ * and keeps the fastest variant for later TEMPO_PREC_MIXED runs on FP32 storage.
+ * Arguments as tempo_run_dev_f32_c; times_ms (optional, `count` entries) receives each
+ * variant's best time, *chosen (optional) the variant kept.  Needs device memory for a
+ * copy of every array the step writes. */
+int tempo_autotune_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float dt,
+                             int itimestep, float *t, float *th, const float *pii,
+                             const float *p, const float *w, const float *dz, float *qv,
+                             float *qc, float *qr, float *qi, float *qs, float *qg, float *ni,
+                             float *nr, float *nc, float *nwfa, float *nifa, float *ng,
+                             float *qb, const int *land_input, int ims, int ime, int jms,
+                             int jme, int kms, int kme, int its, int ite, int jts, int jte,
+                             int kts, int kte, tempo_diags_t *tempo_diags, void *stream,
+                             int reps, float *times_ms, int count, int *chosen);
+/* No reference counterpart.  Selects the per-level kernel variant directly (0..7). */
+int tempo_set_points_variant(tempo_ctx_t *ctx, int variant);
+
 #ifdef __cplusplus
 }
 #endif

@@ -112,6 +112,12 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
     lib.tempo_build_tables_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_float)]
     lib.tempo_last_stats_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_long)]
     lib.tempo_set_kernel_timing.argtypes = [_VP, i]
+    lib.tempo_autotune_dev_f32_c.argtypes = ([_VP, ctypes.POINTER(TempoCfgs), ctypes.c_float, i]
+                                             + [_VP] * 19 + [_VP] + [i] * 12
+                                             + [ctypes.POINTER(TempoDiags), _VP, i,
+                                                ctypes.POINTER(ctypes.c_float), i,
+                                                ctypes.POINTER(ctypes.c_int)])
+    lib.tempo_set_points_variant.argtypes = [_VP, i]
     lib.tempo_kernel_times_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_float)]
     _lib = lib
     return lib
@@ -237,6 +243,39 @@ class TempoContext:
         _check(fn(self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs,
                   land.data_ptr() if land is not None else None,
                   ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte, ctypes.byref(d), sptr))
+
+    def autotune_device(self, fields: dict, dt: float, itimestep: int, diags: Optional[dict] = None,
+                        bounds=None, stream=None, cfgs: Optional[TempoCfgs] = None,
+                        reps: int = 2):
+        """Picks the fastest per-level kernel variant of the mixed form for this
+        workload (tempo_autotune_dev_f32_c) on private copies of the float32 CUDA
+        tensors; returns (chosen variant, per-variant time in ms)."""
+        import torch
+        lib = load_library()
+        cfg = cfgs if cfgs is not None else self.cfgs
+        p = fields["p"]
+        if p.dtype != torch.float32:
+            raise TempoError(-1, "autotune works on float32 device arrays")
+        nj, nk, ni = p.shape
+        b = list(bounds) if bounds is not None else [1, ni, 1, nj, 1, nk] * 3
+        ptrs = [(fields[n].data_ptr() if fields.get(n) is not None else None) for n in FIELDS]
+        land = fields.get("land_input")
+        d = TempoDiags()
+        for n in DIAG2 + DIAG3:
+            a = (diags or {}).get(n)
+            if a is not None:
+                setattr(d, n, a.data_ptr())
+        s = stream if stream is not None else torch.cuda.current_stream(p.device)
+        times = (ctypes.c_float * 8)()
+        chosen = ctypes.c_int(-1)
+        _check(lib.tempo_autotune_dev_f32_c(
+            self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs,
+            land.data_ptr() if land is not None else None, *b[6:], ctypes.byref(d),
+            ctypes.c_void_p(s.cuda_stream), int(reps), times, 8, ctypes.byref(chosen)))
+        return chosen.value, [float(x) for x in times]
+
+    def set_points_variant(self, v: int):
+        _check(load_library().tempo_set_points_variant(self._h, int(v)))
 
     def aerosol_surface_emissions(self, dt: float, nwfa, nwfa2d, kts: int = 1, stream=None):
         """tempo_aerosol_surface_emissions (driver:516-529) on CUDA tensors."""

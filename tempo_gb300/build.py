@@ -23,10 +23,13 @@ INCLUDE = REPO / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(INCLUDE),
                "-I", str(CSRC), *ARCH]
+# (source, extra flags, object name)
 UNITS = [
-    ("tempo_step_f64.cu", ["-fmad=false"]),
-    ("tempo_step_f32.cu", []),
-    ("tempo_tables.cu", ["-fmad=false"]),
+    ("tempo_step_f64.cu", ["-fmad=false"], "tempo_step_f64"),
+    ("tempo_step_f32.cu", [], "tempo_step_f32"),
+    ("tempo_points_f32.cu", ["-DTEMPO_VARIANT_SET=0"], "tempo_points_f32_lo"),
+    ("tempo_points_f32.cu", ["-DTEMPO_VARIANT_SET=1"], "tempo_points_f32_hi"),
+    ("tempo_tables.cu", ["-fmad=false"], "tempo_tables"),
 ]
 HOST_UNITS = ["tempo_capi.cpp", "tempo_host_init.cpp"]
 
@@ -60,8 +63,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     nvcc = _nvcc()
     jobs = []
-    for src, extra in UNITS:
-        obj = BUILD / (Path(src).stem + ".o")
+    for src, extra, name in UNITS:
+        obj = BUILD / (name + ".o")
         jobs.append([nvcc, *NVCC_COMMON, *extra, "-c", str(CSRC / src), "-o", str(obj)])
     for src in HOST_UNITS:
         obj = BUILD / (Path(src).stem + ".o")
@@ -78,7 +81,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(run, jobs))
-    objs = [str(BUILD / (Path(s).stem + ".o")) for s, _ in UNITS] + \
+    objs = [str(BUILD / (name + ".o")) for _, _, name in UNITS] + \
            [str(BUILD / (Path(s).stem + ".o")) for s in HOST_UNITS]
     tmp = LIB.with_suffix(f".so.tmp{os.getpid()}")
     run([nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart_static"])

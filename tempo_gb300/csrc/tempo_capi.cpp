@@ -88,6 +88,7 @@ struct tempo_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool kernel_timing = false;
   cudaEvent_t kev[kStepLaunches + 1] = {};
+  int points_variant = 0;  // mixed form on FP32 storage (tempo_autotune_dev_f32_c)
 };
 
 namespace {
@@ -488,7 +489,8 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   if constexpr (sizeof(S) == sizeof(double))
     CUDA_TRY(launch_step_mixed_f64(a, T, c->c32, c->idf, s, c->kernel_timing ? c->kev : nullptr));
   else
-    CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->idf, s, c->kernel_timing ? c->kev : nullptr));
+    CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->idf, s, c->kernel_timing ? c->kev : nullptr,
+                                   c->points_variant));
   return TEMPO_OK;
 }
 
@@ -748,6 +750,92 @@ int tempo_run_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, int i
   RunArrays<float> A{t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb, land_input};
   cudaStream_t s = (cudaStream_t)stream;  // NULL: the default stream
   return run_dev(c, cfg, (double)dt, itimestep, A, Bounds{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte}, diags, s);
+}
+
+int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, int itimestep,
+                             float* t, float* th, const float* pii, const float* p, const float* w,
+                             const float* dz, float* qv, float* qc, float* qr, float* qi,
+                             float* qs, float* qg, float* ni, float* nr, float* nc, float* nwfa,
+                             float* nifa, float* ng, float* qb, const int* land_input, int ims,
+                             int ime, int jms, int jme, int kms, int kme, int its, int ite, int jts,
+                             int jte, int kts, int kte, tempo_diags_t* diags, void* stream,
+                             int reps, float* times_ms, int count, int* chosen) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (c->precision != TEMPO_PREC_MIXED)
+    return fail(TEMPO_ERR_STATE, "autotune needs TEMPO_PREC_MIXED (tempo_set_precision)");
+  const Bounds b{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte};
+  if (int rc = check_bounds(b)) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  CUDA_TRY(cudaSetDevice(c->device));
+  if (reps < 1) reps = 1;
+  // private copies of every array the step writes: the caller's state is untouched
+  const size_t ext = (size_t)(ime - ims + 1) * (kme - kms + 1) * (jme - jms + 1);
+  const size_t n2 = (size_t)(ite - its + 1) * (jte - jts + 1), n3 = n2 * (kte - kts + 1);
+  float* io[] = {t, th, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb};
+  constexpr int NIO = sizeof(io) / sizeof(io[0]);
+  float* cp[NIO] = {};
+  void** dsrc = diags ? (void**)diags : nullptr;
+  constexpr int ND = sizeof(tempo_diags_t) / sizeof(void*);
+  tempo_diags_t dcopy{};
+  void** dd = (void**)&dcopy;
+  auto release = [&]() {
+    for (float* q : cp) cudaFree(q);
+    for (int i = 0; i < ND; i++) cudaFree(dd[i]);
+  };
+  for (int i = 0; i < NIO; i++)
+    if (io[i] && cudaMalloc(&cp[i], ext * sizeof(float)) != cudaSuccess) {
+      release();
+      return fail(TEMPO_ERR_NOMEM, "autotune: copy of the state (%zu floats)", ext);
+    }
+  for (int i = 0; i < ND; i++)
+    if (dsrc && dsrc[i] && cudaMalloc(&dd[i], (i < 8 ? n2 : n3) * sizeof(float)) != cudaSuccess) {
+      release();
+      return fail(TEMPO_ERR_NOMEM, "autotune: diagnostic buffers");
+    }
+  const bool timing = c->kernel_timing;
+  const int saved_variant = c->points_variant;
+  int rc = tempo_set_kernel_timing(c, 1);
+  float best = 0.0f;
+  int best_v = saved_variant;
+  for (int v = 0; v < kPointsVariants && rc == TEMPO_OK; v++) {
+    c->points_variant = v;
+    float vbest = 0.0f;
+    for (int r = 0; r < reps && rc == TEMPO_OK; r++) {
+      for (int i = 0; i < NIO; i++)
+        if (io[i] && cudaMemcpyAsync(cp[i], io[i], ext * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+          rc = fail(TEMPO_ERR_CUDA, "autotune: state copy");
+      if (rc) break;
+      RunArrays<float> A{cp[0], cp[1], pii, p, w, dz, cp[2], cp[3], cp[4], cp[5], cp[6],
+                         cp[7], cp[8], cp[9], cp[10], cp[11], cp[12], cp[13], cp[14], land_input};
+      rc = run_dev(c, cfg, (double)dt, itimestep, A, b, diags ? &dcopy : nullptr, s);
+      float ms[kStepLaunches];
+      if (rc == TEMPO_OK) rc = tempo_kernel_times_c(c, ms);
+      if (rc == TEMPO_OK && (r == 0 || ms[1] < vbest)) vbest = ms[1];
+    }
+    if (rc) break;
+    if (times_ms && v < count) times_ms[v] = vbest;
+    if (v == 0 || vbest < best) {
+      best = vbest;
+      best_v = v;
+    }
+  }
+  if (!timing) tempo_set_kernel_timing(c, 0);
+  cudaStreamSynchronize(s);
+  release();
+  if (rc) {
+    c->points_variant = saved_variant;
+    return rc;
+  }
+  c->points_variant = best_v;
+  if (chosen) *chosen = best_v;
+  return TEMPO_OK;
+}
+
+int tempo_set_points_variant(tempo_ctx_t* c, int variant) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (variant < 0 || variant >= kPointsVariants) return fail(TEMPO_ERR_ARG, "variant %d outside [0, %d)", variant, kPointsVariants);
+  c->points_variant = variant;
+  return TEMPO_OK;
 }
 
 int tempo_aerosol_surface_emissions_dev_c(tempo_ctx_t* c, double dt, double* nwfa,

@@ -12,6 +12,7 @@ namespace tg {
 
 template <class R> struct Tables;
 template <class S> struct StepArgs;
+template <class I> struct IslandConsts;
 
 // tempo_step_f64.cu (FP64 drop-in, compiled without FMA contraction)
 cudaError_t launch_step_f64(const StepArgs<double>& a, const Tables<double>& t,
@@ -21,10 +22,23 @@ cudaError_t launch_step_f64(const StepArgs<double>& a, const Tables<double>& t,
 // tempo_step_f32.cu (mixed precision: FP32 bulk, double-float islands)
 cudaError_t launch_step_mixed_f32(const StepArgs<float>& a, const Tables<float>& t,
                                   const TempoConsts<float>& c32, const IslandConsts<df>& idf,
-                                  cudaStream_t s, const cudaEvent_t* ev);
+                                  cudaStream_t s, const cudaEvent_t* ev, int points_variant);
 cudaError_t launch_step_mixed_f64(const StepArgs<double>& a, const Tables<float>& t,
                                   const TempoConsts<float>& c32, const IslandConsts<df>& idf,
                                   cudaStream_t s, const cudaEvent_t* ev);
+// tempo_points_f32.cu: points kernel of the mixed form on FP32 storage, variant v in
+// [0, kPointsVariants) (tempo_step.cuh describes the variants)
+cudaError_t launch_points_mixed_f32(int v, const StepArgs<float>& a, const Tables<float>& t,
+                                    const TempoConsts<float>& c, const IslandConsts<df>& ci,
+                                    cudaStream_t s);
+cudaError_t launch_points_mixed_f32_lo(int v, const StepArgs<float>& a, const Tables<float>& t,
+                                       const TempoConsts<float>& c, const IslandConsts<df>& ci,
+                                       cudaStream_t s);
+cudaError_t launch_points_mixed_f32_hi(int v, const StepArgs<float>& a, const Tables<float>& t,
+                                       const TempoConsts<float>& c, const IslandConsts<df>& ci,
+                                       cudaStream_t s);
+// number of points-kernel variants of the mixed form on FP32 storage
+constexpr int kPointsVariants = 8;
 // kernels launched per step (prep, points, sedim, final)
 constexpr int kStepLaunches = 4;
 

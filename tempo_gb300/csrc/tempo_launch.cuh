@@ -6,27 +6,41 @@
 
 namespace tg {
 
+constexpr int kBlock = 128;
+
+inline unsigned points_grid(long ncol, int nz) {
+  const unsigned long long npts = (unsigned long long)ncol * (unsigned long long)nz;
+  return (unsigned)((npts + kBlock - 1) / kBlock);
+}
+
+// points kernel, variant V; its grid covers every column's levels and threads past the
+// active count (read on the device after prep) return at once
+template <class R, class S, int V>
+cudaError_t launch_points(const StepArgs<S>& a, const Tables<R>& T, const TempoConsts<R>& c,
+                          const IslandConsts<Isl<R>>& ci, cudaStream_t s) {
+  tempo_points_kernel<R, S, V><<<points_grid(a.ncol, a.nz), kBlock, 0, s>>>(a, T, c, ci);
+  return cudaGetLastError();
+}
+
 // ev (optional, kStepLaunches + 1 events): recorded before each kernel and after the
-// last, for per-kernel durations measured on the launching stream
-template <class R, class S>
-cudaError_t launch_step(const StepArgs<S>& a, const Tables<R>& T, const TempoConsts<R>& c,
-                        const IslandConsts<Isl<R>>& ci, cudaStream_t s, const cudaEvent_t* ev) {
-  constexpr int B = 128;
+// last, for per-kernel durations measured on the launching stream.  points() launches
+// the points kernel (the variant is the caller's choice).
+template <class R, class S, class Points>
+cudaError_t launch_step(const StepArgs<S>& a, const TempoConsts<R>& c, const IslandConsts<Isl<R>>& ci,
+                        cudaStream_t s, const cudaEvent_t* ev, Points&& points) {
   const unsigned long long ncol = (unsigned long long)a.ncol;
-  const unsigned long long npts = ncol * (unsigned long long)a.nz;
   if (ncol == 0) return cudaSuccess;
-  const unsigned gcol = (unsigned)((ncol + B - 1) / B);
-  const unsigned gpts = (unsigned)((npts + B - 1) / B);
-  // points/final size their grids for every column; threads past the active count
-  // (read on the device after prep) return at once
+  const unsigned gcol = (unsigned)((ncol + kBlock - 1) / kBlock);
+  const unsigned gpts = points_grid(a.ncol, a.nz);
   if (ev) cudaEventRecord(ev[0], s);
-  tempo_prep_kernel<R, S><<<gcol, B, 0, s>>>(a, c, ci);
+  tempo_prep_kernel<R, S><<<gcol, kBlock, 0, s>>>(a, c, ci);
   if (ev) cudaEventRecord(ev[1], s);
-  tempo_points_kernel<R, S><<<gpts, B, 0, s>>>(a, T, c, ci);
+  cudaError_t e = points();
+  if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[2], s);
-  tempo_sedim_kernel<R, S><<<gcol, B, 0, s>>>(a);
+  tempo_sedim_kernel<R, S><<<gcol, kBlock, 0, s>>>(a);
   if (ev) cudaEventRecord(ev[3], s);
-  tempo_final_kernel<R, S><<<gpts, B, 0, s>>>(a, c, ci);
+  tempo_final_kernel<R, S><<<gpts, kBlock, 0, s>>>(a, c, ci);
   if (ev) cudaEventRecord(ev[4], s);
   return cudaGetLastError();
 }

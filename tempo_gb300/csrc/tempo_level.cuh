@@ -92,6 +92,7 @@ struct Lev {
   R smob, smoc, smo0, smo1, smo2, smoe, smof, smog, smoz;
   // thermodynamic island
   I t1d, qv1d, temp, qv, rho, qvs, qvsi, delqvs, ssatw, ssati, tten, qvten;
+  I qvs_t0;  // calc_rslf(p, t0): pressure is fixed through the step, so once per level
   R pres;
   R rhof, rhof2, diffu, visco, vsc2, tcond, lvap, ocp, lvt2;
   R qcten, ncten, qiten, niten, qrten, nrten, qsten, qgten, ngten, qbten, nwfaten, nifaten;
@@ -391,6 +392,19 @@ __device__ __forceinline__ void snow_check(Lev<R>& L, R& q, R dt, R odt) {
   }
 }
 
+// Graupel density class nint(10 rg / rb) + 1 in [1, nrhg] (main:1171, 1200).  Where rb
+// sits at its low-density clamp rg * 1000 / rho_g(1) the ratio is rho_g(1) / 100 = 0.5
+// exactly, a rounding tie of nint.  The FP64 drop-in evaluates the ratio as the
+// reference does (the tie then resolves by the last bit of rg); the mixed form, whose
+// FP32 rg carries no such bit, takes the exact ratio's class, nint(0.5) + 1 = 2.
+template <class R>
+__device__ __forceinline__ int density_class(R ratio, R rb, R rb_lowdens_clamp) {
+  if constexpr (sizeof(R) == sizeof(float)) {
+    if (!(rb < rb_lowdens_clamp)) return 2;
+  }
+  return max(1, min(Nint(ratio) + 1, nrhg));
+}
+
 // graupel_check_and_update (main:1137-1231)
 template <class R>
 __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R odt) {
@@ -404,9 +418,9 @@ __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R od
     q = q + L.qgten * dt;
     if (hail) {
       L.ng = Max(R(r2), (n + L.ngten * dt) * rho);
-      L.rb = Min(Max(L.rg * R(meters3_to_liters) / rho_g<R>(nrhg), (b + L.qbten * dt) * rho),
-                 L.rg * R(meters3_to_liters) / rho_g<R>(1));
-      L.idx_bg = max(1, min(Nint(R(10.0) * L.rg / L.rb) + 1, nrhg));
+      const R rb_hi = L.rg * R(meters3_to_liters) / rho_g<R>(1);
+      L.rb = Min(Max(L.rg * R(meters3_to_liters) / rho_g<R>(nrhg), (b + L.qbten * dt) * rho), rb_hi);
+      L.idx_bg = density_class(R(10.0) * L.rg / L.rb, L.rb, rb_hi);
       const int ig = L.idx_bg;
       if (L.ng <= R(r2)) {
         hit_limit = true;
@@ -429,9 +443,9 @@ __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R od
       }
       if (hit_limit) L.ngten = (L.ng / rho - n) * odt;
       n = c.cgg[0][1] * c.ogg3 * q * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
-      b = Min(Max(q * R(meters3_to_liters) / rho_g<R>(nrhg), b + L.qbten * dt),
-              R(meters3_to_liters) * q / rho_g<R>(1));
-      L.idx_bg = max(1, min(Nint(R(10.0) * q / b) + 1, nrhg));
+      const R b_hi = R(meters3_to_liters) * q / rho_g<R>(1);
+      b = Min(Max(q * R(meters3_to_liters) / rho_g<R>(nrhg), b + L.qbten * dt), b_hi);
+      L.idx_bg = density_class(R(10.0) * q / b, b, b_hi);
     } else {
       L.idx_bg = idx_bg1;
       R ygra1 = Log10(Max(R(1.e-9), L.rg));
@@ -489,7 +503,7 @@ __device__ bool thermo(Lev<R>& L) {
   L.rhof = R(Sqrt(L.ci->rho_not / L.rho));
   L.rhof2 = Sqrt(L.rhof);
   L.qvs = calc_rslf(I(L.pres), L.temp);
-  L.delqvs = Max(I(0.0), calc_rslf(I(L.pres), I(t0)) - L.qv);
+  L.delqvs = Max(I(0.0), L.qvs_t0 - L.qv);
   if (tempc <= 0.0)
     L.qvsi = calc_rsif(I(L.pres), L.temp);
   else

@@ -24,6 +24,8 @@
 // (double: FP64 drop-in; float: mixed form with double-float islands), S the storage.
 #pragma once
 
+#include <type_traits>
+
 #include "tempo_rates.cuh"
 
 namespace tg {
@@ -79,6 +81,7 @@ __device__ __forceinline__ void load_level(const StepArgs<S>& a, long e, Lev<R>&
   L.temp = L.t1d;
   L.qv = Max(I(min_qv), L.qv1d);
   L.rho = rho_of(*L.ci, I(L.pres), L.temp, L.qv);
+  L.qvs_t0 = calc_rslf(I(L.pres), I(t0));
   L.tten = L.qvten = I(0.0);
   L.qcten = L.ncten = L.qiten = L.niten = L.qrten = L.nrten = L.qsten = L.qgten = L.ngten =
       L.qbten = L.nwfaten = L.nifaten = R(0);
@@ -221,11 +224,102 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
   atomicAdd(a.stats, 1ull);
 }
 
+// One stage of phase A, each followed by thermo_vars in the caller: 0 = process
+// rates, limiter, tendency sums, provisional update and checks on temporaries
+// (main:420-522); 1 = saturation adjustment (main:530-560); 2 = rain evaporation
+// (main:563-588).
+template <class R>
+__device__ __forceinline__ void points_stage(int stage, Lev<R>& L, Tend<R>& td, const Tables<R>& T,
+                                             const IslandConsts<Isl<R>>& ci, uint32_t f, R w, R dt,
+                                             R odt, Isl<R> dti, R ncsave, R ncsave_cond, R nwfa_in,
+                                             R nifa_in) {
+  using I = Isl<R>;
+  const bool has_nc = f & F_NC, has_nwfa = f & F_NWFA, has_nifa = f & F_NIFA, hail = f & F_HAIL;
+  if (stage == 0) {
+    if (!(f & F_NOMICRO)) {
+      warm_rain(L, td, T, odt);
+      rain_snow_rain_graupel(L, td, T, odt);
+      ice_nucleation(L, td, T, w, f, dt, odt);
+      const R t1s = t1_subl_of(L);
+      ice_processes(L, td, T, w, t1s, odt);
+      riming(L, td, T, odt);
+      melting(L, td, t1s, f, dt, odt);
+      if (has_nwfa || has_nifa) aerosol_scavenging(L, td, odt);
+    }
+    check_over_depletion(L, td, odt);
+    sum_tendencies(L, td);
+
+    // provisional update (main:460-468)
+    L.temp = L.t1d + L.tten * dti;
+    L.qv = Max(I(min_qv), L.qv1d + L.qvten * dti);
+    L.rho = rho_of(ci, I(L.pres), L.temp, L.qv);
+    {
+      R rho = R(L.rho);
+      L.nwfaten = L.nwfaten - (td.pna_rca + td.pna_sca + td.pna_gca + td.pni_iha) / rho;
+      L.nifaten = L.nifaten - (td.pnd_rcd + td.pnd_scd + td.pnd_gcd) / rho;
+    }
+    if (has_nwfa) L.nwfa = nwfa_in;
+    if (has_nifa) L.nifa = nifa_in;
+    aerosol_check(L, f, dt);
+
+    // checks on temporaries (main:475-522)
+    R xq = L.qc1d, xn = L.nc1d, xb;
+    cloud_check(L, xq, xn, has_nc, ncsave, dt, odt);
+    xq = L.qr1d;
+    xn = L.nr1d;
+    rain_check(L, xq, xn, dt, odt);
+    xq = L.qi1d;
+    xn = L.ni1d;
+    ice_check(L, xq, xn, dt, odt);
+    xq = L.qs1d;
+    snow_check(L, xq, dt, odt);
+    L.smo0 = L.smo1 = L.smo2 = L.smob = L.smoc = L.smoe = L.smof = L.smog = R(0);
+    if (L.l_qs) snow_moments(L, R(Min(I(-0.1), L.temp - t0)), 0);
+    xq = L.qg1d;
+    xn = L.ng1d;
+    xb = L.qb1d;
+    graupel_check(L, xq, xn, xb, hail, dt, odt);
+  } else if (stage == 1) {
+    cloud_condensation(L, td, T, w, f, ncsave_cond, dt, odt);
+    L.qvten = L.qvten - I(td.prw_vcd);
+    L.qcten = L.qcten + td.prw_vcd;
+    L.ncten = L.ncten + td.pnc_wcd;
+    L.nwfaten = L.nwfaten - td.pnc_wcd;
+    L.tten = L.tten + I(L.lvap) * L.ocp * td.prw_vcd;
+    R xq = L.qc1d, xn = L.nc1d;
+    cloud_check(L, xq, xn, has_nc, ncsave, dt, odt);
+    L.qv = Max(I(min_qv), L.qv1d + L.qvten * dti);
+    L.temp = L.t1d + L.tten * dti;
+    L.rho = rho_of(ci, I(L.pres), L.temp, L.qv);
+  } else {
+    rain_evaporation(L, td, odt);
+    L.qrten = L.qrten - td.prv_rev;
+    L.qvten = L.qvten + I(td.prv_rev);
+    L.nrten = L.nrten - td.pnr_rev;
+    L.nwfaten = L.nwfaten + td.pnr_rev;
+    L.tten = L.tten - I(L.lvap) * L.ocp * td.prv_rev;
+    R xq = L.qr1d, xn = L.nr1d;
+    rain_check(L, xq, xn, dt, odt);
+    L.qv = Max(I(min_qv), L.qv1d + L.qvten * dti);
+    L.temp = L.t1d + L.tten * dti;
+    L.rho = rho_of(ci, I(L.pres), L.temp, L.qv);
+  }
+}
+
+// Variants of the points kernel (picked per context by tempo_autotune_c): bit 0 drives
+// the stages from one loop with a single copy of thermo_vars (smaller code, more live
+// registers) instead of inlining each stage; bits 1-2 select the minimum resident
+// blocks per SM asked of the register allocator (1, 3, 4 or 5 blocks of 128 threads:
+// no cap, 170, 128 or 102 registers per thread).
+__host__ __device__ constexpr int points_min_blocks(int v) {
+  return ((v >> 1) & 3) == 0 ? 1 : ((v >> 1) & 3) + 2;
+}
+
 // ---------------------------------------------------------------------------------
 // points: phase A at one (level, active slot)
 // ---------------------------------------------------------------------------------
-template <class R, class S>
-__global__ void __launch_bounds__(128) tempo_points_kernel(const __grid_constant__ StepArgs<S> a,
+template <class R, class S, int V>
+__global__ void __launch_bounds__(128, points_min_blocks(V)) tempo_points_kernel(const __grid_constant__ StepArgs<S> a,
                                                             const __grid_constant__ Tables<R> T,
                                                             const __grid_constant__ TempoConsts<R> cst,
                                                             const __grid_constant__ IslandConsts<Isl<R>> ci) {
@@ -270,83 +364,33 @@ __global__ void __launch_bounds__(128) tempo_points_kernel(const __grid_constant
   initial_checks(L, f, ncsave, do_ginit, dt, odt);
   L.qcten = L.qiten = L.qrten = L.qsten = L.qgten = L.ngten = L.qbten = L.niten = L.nrten =
       L.ncten = R(0);
-  thermo(L);
 
+  // thermo_vars runs after the initial checks and after each of the three stages
+  // that follow (main:412, 524, 557, 585)
   Tend<R> td = {};
-  if (!(f & F_NOMICRO)) {
-    warm_rain(L, td, T, odt);
-    rain_snow_rain_graupel(L, td, T, odt);
-    ice_nucleation(L, td, T, w, f, dt, odt);
-    const R t1s = t1_subl_of(L);
-    ice_processes(L, td, T, w, t1s, odt);
-    riming(L, td, T, odt);
-    melting(L, td, t1s, f, dt, odt);
-    if (has_nwfa || has_nifa) aerosol_scavenging(L, td, odt);
-  }
-  check_over_depletion(L, td, odt);
-  sum_tendencies(L, td);
-
-  // provisional update (main:460-468)
-  L.temp = L.t1d + L.tten * dti;
-  L.qv = Max(I(min_qv), L.qv1d + L.qvten * dti);
-  L.rho = rho_of(ci, I(L.pres), L.temp, L.qv);
-  {
-    R rho = R(L.rho);
-    L.nwfaten = L.nwfaten - (td.pna_rca + td.pna_sca + td.pna_gca + td.pni_iha) / rho;
-    L.nifaten = L.nifaten - (td.pnd_rcd + td.pnd_scd + td.pnd_gcd) / rho;
-  }
-  if (has_nwfa) L.nwfa = nwfa_in;
-  if (has_nifa) L.nifa = nifa_in;
-  aerosol_check(L, f, dt);
-
-  // checks on temporaries (main:475-522)
-  R xq = L.qc1d, xn = L.nc1d, xb;
-  cloud_check(L, xq, xn, has_nc, ncsave, dt, odt);
-  xq = L.qr1d;
-  xn = L.nr1d;
-  rain_check(L, xq, xn, dt, odt);
-  xq = L.qi1d;
-  xn = L.ni1d;
-  ice_check(L, xq, xn, dt, odt);
-  xq = L.qs1d;
-  snow_check(L, xq, dt, odt);
-  L.smo0 = L.smo1 = L.smo2 = L.smob = L.smoc = L.smoe = L.smof = L.smog = R(0);
-  if (L.l_qs) snow_moments(L, R(Min(I(-0.1), L.temp - t0)), 0);
-  xq = L.qg1d;
-  xn = L.ng1d;
-  xb = L.qb1d;
-  graupel_check(L, xq, xn, xb, hail, dt, odt);
-  thermo(L);
-
-  if (!(f & F_NOMICRO) && (f & F_COND)) {  // main:530-560
-    cloud_condensation(L, td, T, w, f, ncsave_cond, dt, odt);
-    L.qvten = L.qvten - I(td.prw_vcd);
-    L.qcten = L.qcten + td.prw_vcd;
-    L.ncten = L.ncten + td.pnc_wcd;
-    L.nwfaten = L.nwfaten - td.pnc_wcd;
-    L.tten = L.tten + I(L.lvap) * L.ocp * td.prw_vcd;
-    xq = L.qc1d;
-    xn = L.nc1d;
-    cloud_check(L, xq, xn, has_nc, ncsave, dt, odt);
-    L.qv = Max(I(min_qv), L.qv1d + L.qvten * dti);
-    L.temp = L.t1d + L.tten * dti;
-    L.rho = rho_of(ci, I(L.pres), L.temp, L.qv);
+  const bool do_cond = !(f & F_NOMICRO) && (f & F_COND);
+  const bool do_evap = !(f & F_NOMICRO);
+  if constexpr (V & 1) {
+    int stage = 0;
+#pragma unroll 1
+    for (;;) {
+      thermo(L);
+      if (stage > 2) break;
+      points_stage(stage, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
+      stage = stage == 0 ? (do_cond ? 1 : do_evap ? 2 : 3) : stage == 1 ? (do_evap ? 2 : 3) : 3;
+    }
+  } else {
     thermo(L);
-  }
-  if (!(f & F_NOMICRO)) {  // main:563-588
-    rain_evaporation(L, td, odt);
-    L.qrten = L.qrten - td.prv_rev;
-    L.qvten = L.qvten + I(td.prv_rev);
-    L.nrten = L.nrten - td.pnr_rev;
-    L.nwfaten = L.nwfaten + td.pnr_rev;
-    L.tten = L.tten - I(L.lvap) * L.ocp * td.prv_rev;
-    xq = L.qr1d;
-    xn = L.nr1d;
-    rain_check(L, xq, xn, dt, odt);
-    L.qv = Max(I(min_qv), L.qv1d + L.qvten * dti);
-    L.temp = L.t1d + L.tten * dti;
-    L.rho = rho_of(ci, I(L.pres), L.temp, L.qv);
+    points_stage(0, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
     thermo(L);
+    if (do_cond) {
+      points_stage(1, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
+      thermo(L);
+    }
+    if (do_evap) {
+      points_stage(2, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
+      thermo(L);
+    }
   }
 
   // fall-speed candidates (main:1770-1977), unfilled; < 0 marks "absent"
@@ -434,6 +478,12 @@ __global__ void __launch_bounds__(128) tempo_points_kernel(const __grid_constant
   sd[SD_TNI * fsd + o] = I(L.niten);
   sd[SD_TQC * fsd + o] = I(L.qcten);
   sd[SD_TNC * fsd + o] = I(L.ncten);
+  if constexpr (!std::is_same<I, double>::value) {
+    // the mixed form's sedimentation multiplies by these instead of dividing per sweep
+    const I odz = 1.0 / ldi<I>(a.dz + e);
+    sd[SD_ODZ * fsd + o] = odz;
+    sd[SD_OZR * fsd + o] = odz / L.rho;
+  }
   sr[SR_VTR * fsd + o] = vtr;
   sr[SR_VTNR * fsd + o] = vtnr;
   sr[SR_VTG * fsd + o] = vtg;
@@ -528,6 +578,29 @@ __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant_
     const R* vt = sr + fv * fsd;
     const I osteps = 1.0 / I(steps);
     const I lim = I(limit);
+    if constexpr (!std::is_same<I, double>::value) {
+      // mixed form: the same fluxes and order, with the per-level factors 1/dz and
+      // 1/(dz rho) precomputed in the points kernel
+      const I* odz = sd + SD_ODZ * fsd;
+      const I* ozr = sd + SD_OZR * fsd;
+      const I cx = dti * osteps;
+      int k = nz - 1;
+      I s_top = I(vt[k * cs]) * x[k * cs];
+      ten[k * cs] = ten[k * cs] - s_top * ozr[k * cs] * osteps;
+      x[k * cs] = Max(lim, x[k * cs] - s_top * odz[k * cs] * cx);
+      I s_up = (ktop == nz - 1) ? s_top : I(vt[ktop * cs]) * x[ktop * cs];
+      I s0 = (nz == 1) ? s_top : I(vt[0]) * x[0];
+      for (k = ktop - 1; k >= 0; k--) {
+        const I s_k = I(vt[k * cs]) * x[k * cs];
+        const I dflux = s_up - s_k;
+        ten[k * cs] = ten[k * cs] + dflux * ozr[k * cs] * osteps;
+        x[k * cs] = Max(lim, x[k * cs] + dflux * odz[k * cs] * cx);
+        if (k == 0) s0 = s_k;
+        s_up = s_k;
+      }
+      if (precip && x[0] > low_limit_mass_for_precip) *precip = *precip + s0 * dti * osteps;
+      return;
+    }
     int k = nz - 1;
     I s_top = I(vt[k * cs]) * x[k * cs];
     I odz = 1.0 / ldi<I>(dzp + k * NI), orho = 1.0 / rho[k * cs];

@@ -8,7 +8,9 @@ namespace tg {
 cudaError_t launch_step_f64(const StepArgs<double>& a, const Tables<double>& t,
                             const TempoConsts<double>& c64, const IslandConsts<double>& i64,
                             cudaStream_t s, const cudaEvent_t* ev) {
-  return launch_step<double, double>(a, t, c64, i64, s, ev);
+  return launch_step<double, double>(a, c64, i64, s, ev, [&] {
+    return launch_points<double, double, 0>(a, t, c64, i64, s);
+  });
 }
 
 }  // namespace tg

@@ -48,7 +48,9 @@ enum SDField : int {
   SD_TTEN, SD_QV, SD_RHO,
   SD_XRR, SD_XNR, SD_XRG, SD_XNG, SD_XRB, SD_XRS, SD_XRI, SD_XNI, SD_XRC, SD_XNC,
   SD_TQR, SD_TNR, SD_TQG, SD_TNG, SD_TQB, SD_TQS, SD_TQI, SD_TNI, SD_TQC, SD_TNC,
-  SD_HGT, SD_N
+  SD_HGT,
+  SD_ODZ, SD_OZR,  // 1 / dz and 1 / (dz rho) of the level (mixed form: sedimentation factors)
+  SD_N
 };
 // per-point scratch fields in the bulk type R (fall-speed candidates; < 0 = absent)
 enum SRField : int {

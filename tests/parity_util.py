@@ -49,18 +49,26 @@ def run_gpu(ctx, cfg_over: dict, wl, fields=None, itimestep=1, diag3=DIAG3, dtyp
     return f, d
 
 
-def rel_err(a, b, floor):
+def rel_err(a, b, floor, scale=None):
+    """|a - b| relative to max(|b|, floor) -- and, for a prognostic field, to the
+    magnitude it had before the step (``scale``): the step computes new = old +
+    tendency * dt, so where that sum cancels (a species nearly used up) the rounding
+    of old and of the tendency, not of the small result, sets the attainable error."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
-    return np.abs(a - b) / np.maximum(np.abs(b), floor)
+    den = np.maximum(np.abs(b), floor)
+    if scale is not None:
+        den = np.maximum(den, np.abs(np.asarray(scale, dtype=np.float64)))
+    return np.abs(a - b) / den
 
 
-def compare(fa, da, fb, db, names3=OUT3):
-    """Per-field (max, rms) relative error of a against b (b = oracle)."""
+def compare(fa, da, fb, db, names3=OUT3, inputs=None):
+    """Per-field (max, rms) relative error of a against b (b = oracle); ``inputs``: the
+    fields before the step, the scale of the prognostic fields (see rel_err)."""
     out = {}
     for n in names3:
         if n in fa and n in fb:
-            e = rel_err(fa[n], fb[n], FLOOR[n])
+            e = rel_err(fa[n], fb[n], FLOOR[n], None if inputs is None else inputs.get(n))
             out[n] = (float(e.max()), float(np.sqrt(np.mean(e * e))))
     for n in tuple(DIAG2) + tuple(DIAG3):
         if n in da and n in db:
@@ -76,9 +84,9 @@ def worst(errs):
     return k, errs[k][0]
 
 
-def _col_err(a, b, floor):
+def _col_err(a, b, floor, scale=None):
     """Per-column max relative error of a 2-D (nj, ni) or 3-D (nj, nk, ni) field."""
-    e = rel_err(a, b, floor)
+    e = rel_err(a, b, floor, scale)
     return e.max(axis=1) if e.ndim == 3 else e
 
 
@@ -86,7 +94,7 @@ GRAUPEL_DIAGS = ("graupel_med_vol_diam", "refl10cm", "max_hail_diameter_sfc",
                  "max_hail_diameter_column")
 
 
-def compare_with_ties(fa, da, fb, db, ties, tol, names3=OUT3):
+def compare_with_ties(fa, da, fb, db, ties, tol, names3=OUT3, inputs=None):
     """Column-wise comparison of a against the oracle b that tells rounding-tie branch
     flips from real mismatches.
 
@@ -101,23 +109,30 @@ def compare_with_ties(fa, da, fb, db, ties, tol, names3=OUT3):
 
     Returns (worst error over unflagged columns, worst error of the non-graupel-
     diagnostic outputs over bit-2-only columns, number of bit-1 columns that deviate
-    beyond tol, names of the fields of the worst unflagged error)."""
+    beyond tol, name of the field of the worst unflagged error, fraction of the
+    unflagged (point, field) values beyond tol)."""
     ties = np.asarray(ties)
     b1 = (ties & 1).astype(bool)
     b2only = ((ties & 2).astype(bool)) & ~b1
     clean = ~(b1 | b2only)
     worst_clean, worst_b2, which = 0.0, 0.0, None
+    n_all = n_over = 0
     dev1 = np.zeros_like(b1)
     items = [(n, fa, fb) for n in names3 if n in fa and n in fb]
     items += [(n, da, db) for n in tuple(DIAG2) + tuple(DIAG3) if n in da and n in db]
     for n, A, B in items:
         assert not np.isnan(B[n]).any(), f"oracle left {n} unset"
         assert not np.isnan(A[n]).any(), f"{n} not written"
-        e = _col_err(A[n], B[n], FLOOR[n])
+        sc = None if (inputs is None or A is da) else inputs.get(n)
+        e = _col_err(A[n], B[n], FLOOR[n], sc)
+        ep = rel_err(A[n], B[n], FLOOR[n], sc)
+        ep = ep.transpose(0, 2, 1)[clean] if ep.ndim == 3 else ep[clean]
+        n_all += ep.size
+        n_over += int((ep > tol).sum())
         m = float(e[clean].max()) if clean.any() else 0.0
         if m > worst_clean:
             worst_clean, which = m, n
         if n not in GRAUPEL_DIAGS and b2only.any():
             worst_b2 = max(worst_b2, float(e[b2only].max()))
         dev1 |= b1 & (e > tol)
-    return worst_clean, worst_b2, int(dev1.sum()), which
+    return worst_clean, worst_b2, int(dev1.sum()), which, n_over / max(1, n_all)

@@ -1,0 +1,124 @@
+"""The mixed-precision form (FP32 bulk, double-float islands) against the FP64 oracle.
+
+Per-field max and RMS relative error (relative to the larger of the oracle's value,
+the field's value before the step and the reference's existence threshold),
+column water budget and 10-cm reflectivity in dBZ, on the stretched-grid workload
+(config-1 generator) and the hail-aware deep-convection workload (config-2
+generator).  Bounds are stated per field below.  FP32 process rates move values by
+about 1e-7 relative; larger differences come from threshold branches (existence
+limits, table bin edges) that an FP32 value crosses where the FP64 one does not, so
+RMS is held tighter than the maximum.
+"""
+import numpy as np
+import pytest
+
+from parity_util import DIAG2, FLOOR, compare, make_diags, rel_err, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+# (max, rms) relative-error bounds per field
+BOUNDS = {
+    "t": (1e-6, 1e-7), "qv": (1e-5, 1e-6),
+    "qc": (5e-2, 1e-4), "qr": (5e-2, 1e-4), "qi": (1e-3, 1e-5), "qs": (1e-3, 1e-5),
+    "qg": (5e-2, 3e-4), "ni": (1e-2, 1e-5), "nr": (5e-2, 1e-4), "nc": (5e-1, 2e-3),
+    "nwfa": (5e-2, 2e-4), "nifa": (1e-3, 1e-5), "ng": (5e-2, 1e-4), "qb": (5e-2, 1e-4),
+}
+DIAG_BOUNDS = (1e-1, 1e-3)   # diagnostics other than reflectivity
+REFL_DBZ = (0.5, 1e-2)       # (max, rms) absolute dBZ
+
+
+def _run_mixed_f32(ctx, over, wl, itimestep=1):
+    import tempo_gb300 as tg
+    f = {k: np.ascontiguousarray(v.astype(np.float32)) for k, v in wl.fields.items()}
+    d = make_diags(f["p"].shape, dtype=np.float32)
+    ctx.set_precision(tg.PREC_MIXED)
+    try:
+        ctx.run(f, wl.dt, itimestep, diags=d, cfgs=tg.default_cfgs(**over))
+    finally:
+        ctx.set_precision(tg.PREC_FP64)
+    return f, d
+
+
+def _column_water(f, rho, dz):
+    q = sum(f[n] for n in ("qv", "qc", "qr", "qi", "qs", "qg"))
+    return (q.astype(np.float64) * rho * dz).sum(axis=1)   # kg m-2 per column
+
+
+def _check(fm, dm, fo, do, wl):
+    # the FP32 inputs are the FP64 inputs rounded: compare on the oracle run from
+    # those same rounded inputs
+    errs = compare(fm, {k: v for k, v in dm.items() if k != "refl10cm"}, fo,
+                   {k: v for k, v in do.items() if k != "refl10cm"}, inputs=wl.fields)
+    bad = []
+    for n, (mx, rms) in errs.items():
+        bmx, brms = BOUNDS.get(n, DIAG_BOUNDS)
+        if mx > bmx or rms > brms:
+            bad.append((n, mx, rms))
+    e = np.abs(dm["refl10cm"].astype(np.float64) - do["refl10cm"])
+    if e.max() > REFL_DBZ[0] or np.sqrt((e * e).mean()) > REFL_DBZ[1]:
+        bad.append(("refl10cm_dbz", float(e.max()), float(np.sqrt((e * e).mean()))))
+    # water budget: sum of water over the column plus surface precipitation (mm =
+    # kg m-2), with the input density and layer depths for both runs
+    from tempo_gb300.workloads import RD
+    t, p, dz = wl.fields["t"], wl.fields["p"], wl.fields["dz"]
+    roverrv = RD / 461.5
+    rho = roverrv * p / (RD * t * (np.maximum(1e-10, wl.fields["qv"]) + roverrv))
+    precip = lambda d: sum(d[n].astype(np.float64) for n in DIAG2[:4])  # noqa: E731
+    w0 = _column_water(wl.fields, rho, dz)
+    res_o = _column_water(fo, rho, dz) + precip(do) - w0
+    res_m = _column_water(fm, rho, dz) + precip(dm) - w0
+    budget = float(np.max(np.abs(res_m - res_o) / np.maximum(w0, 1e-12)))
+    if budget > 1e-6:
+        bad.append(("water_budget", budget, None))
+    return bad, errs
+
+
+def _rounded(wl):
+    from copy import copy
+    w2 = copy(wl)
+    w2.fields = {k: v.astype(np.float32).astype(np.float64) for k, v in wl.fields.items()}
+    return w2
+
+
+def test_mixed_config1_within_bounds(ctx_nohail, oracle_mod):
+    from tempo_gb300 import workloads as W
+    oracle_mod.init(False)
+    wl = _rounded(W.config1(ni=64, nj=16, steps=1))
+    over = dict(hailaware_flag=0)
+    fo, do = run_oracle(oracle_mod, over, wl)
+    fm, dm = _run_mixed_f32(ctx_nohail, over, wl)
+    bad, errs = _check(fm, dm, fo, do, wl)
+    oracle_mod.init(True)
+    assert not bad, bad
+
+
+def _columns(d, jj, ii):
+    """The columns (jj, ii) of every (nj, nk, ni) / (nj, ni) array, as (1, nk, n) / (1, n)."""
+    out = {}
+    for k, v in d.items():
+        out[k] = v[jj, :, ii].T[None] if v.ndim == 3 else v[jj, ii][None]
+    return out
+
+
+def test_mixed_config2_hail_within_bounds(ctx_hail, oracle_mod):
+    """Hail-aware graupel: the density class nint(10 rg / rb) sits on a rounding tie
+    wherever rb is at its low-density clamp (10 rg / rb = 0.5).  The FP64 reference
+    resolves it by the last bits of rg (class 2 in most cases, class 1 in about one
+    case in twelve); the mixed form takes the exact class 2.  Columns whose oracle
+    step passed such a tie before sedimentation move with it (fall speeds differ by
+    the class) and are excluded; all other columns hold the bounds."""
+    from tempo_gb300 import workloads as W
+    oracle_mod.init(True)
+    wl = _rounded(W.config2(ni=32, nj=16))
+    over = dict(hailaware_flag=1, rain_med_vol_diam_flag=1, graupel_med_vol_diam_flag=1)
+    ties = np.zeros(wl.fields["p"].shape[::2], np.int32)
+    fo, do = run_oracle(oracle_mod, over, wl, ties=ties)
+    fm, dm = _run_mixed_f32(ctx_hail, over, wl)
+    jj, ii = np.nonzero((ties & 1) == 0)
+    assert len(jj) >= ties.size // 2
+    sub = lambda d: _columns(d, jj, ii)  # noqa: E731
+    from copy import copy
+    wsub = copy(wl)
+    wsub.fields = sub(wl.fields)
+    bad, errs = _check(sub(fm), sub(dm), sub(fo), sub(do), wsub)
+    assert not bad, bad
