@@ -213,6 +213,13 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, f
 /* No reference counterpart.  Selects the per-level kernel variant directly (0..7). */
 int tempo_set_points_variant(tempo_ctx_t *ctx, int variant);
 
+/* No reference counterpart.  With on != 0, a run captures its work (counter resets and
+ * the four kernels) into a CUDA graph the first time it sees a given argument set
+ * (pointers, bounds, dt, flags, precision, variant) and replays the graph on later
+ * runs with the same set; up to 8 graphs are kept per context.  With kernel timing on,
+ * the graph carries the timing events. */
+int tempo_set_graphs(tempo_ctx_t *ctx, int on);
+
 #ifdef __cplusplus
 }
 #endif

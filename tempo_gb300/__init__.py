@@ -118,6 +118,7 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
                                                 ctypes.POINTER(ctypes.c_float), i,
                                                 ctypes.POINTER(ctypes.c_int)])
     lib.tempo_set_points_variant.argtypes = [_VP, i]
+    lib.tempo_set_graphs.argtypes = [_VP, i]
     lib.tempo_kernel_times_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_float)]
     _lib = lib
     return lib
@@ -273,6 +274,10 @@ class TempoContext:
             land.data_ptr() if land is not None else None, *b[6:], ctypes.byref(d),
             ctypes.c_void_p(s.cuda_stream), int(reps), times, 8, ctypes.byref(chosen)))
         return chosen.value, [float(x) for x in times]
+
+    def set_graphs(self, on: bool = True):
+        """Capture each distinct step into a CUDA graph and replay it (tempo_set_graphs)."""
+        _check(load_library().tempo_set_graphs(self._h, int(bool(on))))
 
     def set_points_variant(self, v: int):
         _check(load_library().tempo_set_points_variant(self._h, int(v)))

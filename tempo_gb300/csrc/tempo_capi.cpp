@@ -63,6 +63,14 @@ struct Mirror {
 
 }  // namespace
 
+namespace {
+constexpr size_t kGraphCache = 8;
+struct GraphEntry {
+  std::string key;  // bytes of the step arguments + precision, variant, storage size
+  cudaGraphExec_t exec;
+};
+}  // namespace
+
 struct tempo_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -89,6 +97,8 @@ struct tempo_ctx {
   bool kernel_timing = false;
   cudaEvent_t kev[kStepLaunches + 1] = {};
   int points_variant = 0;  // mixed form on FP32 storage (tempo_autotune_dev_f32_c)
+  bool use_graphs = false;
+  std::vector<GraphEntry> graphs;  // captured steps, oldest first
 };
 
 namespace {
@@ -435,6 +445,10 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   a.ncol = (long)a.ti * a.tj;
   a.ncol_pad = (a.ncol + 31) / 32 * 32;
   a.dt = dt;
+  a.odt = 1.0 / dt;
+  a.dt_hi = (float)dt;
+  a.dt_lo = (float)(dt - (double)a.dt_hi);
+  a.odt_f = (float)a.odt;
   a.nc_single = resolve_nc_value(cfg);
   a.flags = f;
   // decay rates of the aerosol initial profiles (init_*_friendly_aerosols,
@@ -470,27 +484,64 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   sp += cm_bytes;
   a.nact = (unsigned int*)sp;
   a.stats = c->d_stats;
-  CUDA_TRY(cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s));
-  CUDA_TRY(cudaMemsetAsync(a.nact, 0, sizeof(unsigned int), s));
   c->last_cols = a.ncol;
   c->launches = kStepLaunches;
-  if (!mixed) {
-    if constexpr (sizeof(S) == sizeof(double)) {
-      Tables<double> T{c->t64.t_efrw, c->t64.t_efsw, c->t64.tnc_wev, c->t64.tps_iaus, c->t64.tni_iaus,
-                       c->t64.tpi_ide, c->t64.tnccn, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
-      CUDA_TRY(launch_step_f64(a, T, c->c64, c->i64, s, c->kernel_timing ? c->kev : nullptr));
-      return TEMPO_OK;
-    } else {
-      return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
+  if (!mixed && sizeof(S) != sizeof(double))
+    return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
+  const bool timed = c->kernel_timing;
+  // the step's work on stream st: counters reset, then the four kernels
+  auto enqueue = [&](cudaStream_t st) -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.nact, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+    const cudaEvent_t* ev = timed ? c->kev : nullptr;
+    if (!mixed) {
+      if constexpr (sizeof(S) == sizeof(double)) {
+        Tables<double> T{c->t64.t_efrw, c->t64.t_efsw, c->t64.tnc_wev, c->t64.tps_iaus, c->t64.tni_iaus,
+                         c->t64.tpi_ide, c->t64.tnccn, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
+        return launch_step_f64(a, T, c->c64, c->i64, st, ev);
+      }
+      return cudaErrorInvalidValue;
     }
+    Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
+                    c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
+    if constexpr (sizeof(S) == sizeof(double))
+      return launch_step_mixed_f64(a, T, c->c32, c->idf, st, ev);
+    else
+      return launch_step_mixed_f32(a, T, c->c32, c->idf, st, ev, c->points_variant);
+  };
+  if (!c->use_graphs) {
+    CUDA_TRY(enqueue(s));
+    return TEMPO_OK;
   }
-  Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
-                  c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
-  if constexpr (sizeof(S) == sizeof(double))
-    CUDA_TRY(launch_step_mixed_f64(a, T, c->c32, c->idf, s, c->kernel_timing ? c->kev : nullptr));
-  else
-    CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->idf, s, c->kernel_timing ? c->kev : nullptr,
-                                   c->points_variant));
+  // CUDA graph: captured once per distinct argument set, replayed on the caller's stream
+  std::string key((const char*)&a, sizeof a);
+  key.push_back((char)c->precision);
+  key.push_back((char)c->points_variant);
+  key.push_back((char)sizeof(S));
+  key.push_back((char)timed);  // event-record nodes around the kernels
+  cudaGraphExec_t exec = nullptr;
+  for (auto& g : c->graphs)
+    if (g.key == key) exec = g.exec;
+  if (!exec) {
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue(c->stream);
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &graph);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return fail(TEMPO_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(TEMPO_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    if (c->graphs.size() >= kGraphCache) {
+      cudaGraphExecDestroy(c->graphs.front().exec);
+      c->graphs.erase(c->graphs.begin());
+    }
+    c->graphs.push_back(GraphEntry{key, exec});
+  }
+  CUDA_TRY(cudaGraphLaunch(exec, s));
   return TEMPO_OK;
 }
 
@@ -667,6 +718,7 @@ int tempo_ctx_destroy(tempo_ctx_t* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   for (cudaEvent_t& e : c->kev)
     if (e) cudaEventDestroy(e);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return TEMPO_OK;
@@ -828,6 +880,12 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, 
   }
   c->points_variant = best_v;
   if (chosen) *chosen = best_v;
+  return TEMPO_OK;
+}
+
+int tempo_set_graphs(tempo_ctx_t* c, int on) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  c->use_graphs = on != 0;
   return TEMPO_OK;
 }
 

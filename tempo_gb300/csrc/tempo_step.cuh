@@ -32,6 +32,18 @@ namespace tg {
 
 template <class I, class S> __device__ __forceinline__ I ldi(const S* p) { return I(*p); }
 
+// the time step in the bulk type, its reciprocal, and the time step in the island type
+// (host-computed, so that no kernel of the mixed form converts or divides in FP64)
+template <class R, class S> __device__ __forceinline__ R step_dt(const StepArgs<S>& a) {
+  if constexpr (sizeof(R) == sizeof(double)) return a.dt; else return a.dt_hi;
+}
+template <class R, class S> __device__ __forceinline__ R step_odt(const StepArgs<S>& a) {
+  if constexpr (sizeof(R) == sizeof(double)) return a.odt; else return a.odt_f;
+}
+template <class R, class S> __device__ __forceinline__ Isl<R> step_dti(const StepArgs<S>& a) {
+  if constexpr (sizeof(R) == sizeof(double)) return a.dt; else return df(a.dt_hi, a.dt_lo);
+}
+
 // geometry of column c of the tile
 struct ColGeom {
   long base;   // memory offset of (its+ii, kts, jts+jj)
@@ -133,7 +145,7 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
   const uint32_t f = a.flags;
   const int nz = a.nz;
   const bool hail = f & F_HAIL;
-  const R dt = R(a.dt), odt = R(1.0 / a.dt);
+  const R dt = step_dt<R>(a), odt = step_odt<R>(a);
   ColGeom g = {};
   bool early = true, do_ginit = false;
   if (valid) {
@@ -335,8 +347,8 @@ __global__ void __launch_bounds__(128, points_min_blocks(V)) tempo_points_kernel
   const long e = g.base + (long)k * a.NI;
   const uint32_t f = a.flags;
   const bool has_nc = f & F_NC, has_nwfa = f & F_NWFA, has_nifa = f & F_NIFA, hail = f & F_HAIL;
-  const R dt = R(a.dt), odt = R(1.0 / a.dt);
-  const I dti = I(a.dt);
+  const R dt = step_dt<R>(a), odt = step_odt<R>(a);
+  const I dti = step_dti<R>(a);
   const R ncsave = ncsave_of<R>(a, g);
   const R ncsave_cond = has_nc ? R(nt_c_l) : ncsave;
   const bool do_ginit = a.cmask[s] & CM_GINIT;
@@ -516,8 +528,8 @@ __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant_
   const long cs = a.ncol_pad, fsd = (long)nz * cs;
   I* sd = reinterpret_cast<I*>(a.sd) + s;
   R* sr = reinterpret_cast<R*>(a.sr) + s;
-  const R dt = R(a.dt);
-  const I dti = I(a.dt);
+  const R dt = step_dt<R>(a);
+  const I dti = step_dti<R>(a);
   const S* dzp = a.dz + g.base;
 
   uint8_t any = 0;
@@ -702,8 +714,8 @@ __global__ void __launch_bounds__(128) tempo_final_kernel(const __grid_constant_
   const long e = g.base + (long)k * a.NI;
   const uint32_t f = a.flags;
   const bool has_nc = f & F_NC, hail = f & F_HAIL;
-  const R dt = R(a.dt), odt = R(1.0 / a.dt);
-  const I dti = I(a.dt);
+  const R dt = step_dt<R>(a), odt = step_odt<R>(a);
+  const I dti = step_dti<R>(a);
   const R ncsave = ncsave_of<R>(a, g);
   const long cs = a.ncol_pad, fsd = (long)nz * cs, o = (long)k * cs + s;
   const I* sd = reinterpret_cast<const I*>(a.sd);

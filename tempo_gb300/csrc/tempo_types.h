@@ -83,6 +83,8 @@ struct StepArgs {
   int ti, tj, nz;     // tile extents
   long ncol, ncol_pad;
   double dt;
+  double odt;         // 1 / dt
+  float dt_hi, dt_lo, odt_f;  // dt as a double-float pair and 1/dt in float (mixed form)
   double nc_single;   // single-moment cloud number (m^-3) when nc is absent and no land
   double niccn3, niin3;  // decay rates of the aerosol initial profiles (aerosols:14-73)
   uint32_t flags;

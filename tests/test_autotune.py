@@ -49,3 +49,22 @@ def test_every_variant_computes_the_same_step(tg):
             a, b = out[k], ref[k]
             # same arithmetic; only the register allocation differs
             assert np.allclose(a, b, rtol=1e-6, atol=1e-30), (v, k, float(np.abs(a - b).max()))
+
+
+def test_graph_replay_matches_direct_launches(tg):
+    """Three steps replayed from captured CUDA graphs give the same state as three
+    directly launched steps."""
+    torch = pytest.importorskip("torch")
+    from tempo_gb300 import workloads as W
+    outs = []
+    for graphs in (False, True):
+        ctx = tg.TempoContext(build_tables=True, cfgs=tg.default_cfgs(hailaware_flag=0))
+        ctx.set_precision(tg.PREC_MIXED)
+        ctx.set_graphs(graphs)
+        f, d = _fields(W, torch)
+        for it in (1, 2, 3):
+            ctx.run_device(f, 30.0, it, diags=d)
+        torch.cuda.synchronize()
+        outs.append({k: x.cpu().numpy() for k, x in list(f.items()) + list(d.items())})
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k

@@ -84,7 +84,8 @@ def test_mixed_config1_within_bounds(ctx_nohail, oracle_mod):
     from tempo_gb300 import workloads as W
     oracle_mod.init(False)
     wl = _rounded(W.config1(ni=64, nj=16, steps=1))
-    over = dict(hailaware_flag=0)
+    over = dict(hailaware_flag=0, rain_med_vol_diam_flag=1, graupel_med_vol_diam_flag=1,
+                cloud_number_mixing_ratio_flag=1)
     fo, do = run_oracle(oracle_mod, over, wl)
     fm, dm = _run_mixed_f32(ctx_nohail, over, wl)
     bad, errs = _check(fm, dm, fo, do, wl)
@@ -110,7 +111,8 @@ def test_mixed_config2_hail_within_bounds(ctx_hail, oracle_mod):
     from tempo_gb300 import workloads as W
     oracle_mod.init(True)
     wl = _rounded(W.config2(ni=32, nj=16))
-    over = dict(hailaware_flag=1, rain_med_vol_diam_flag=1, graupel_med_vol_diam_flag=1)
+    over = dict(hailaware_flag=1, rain_med_vol_diam_flag=1, graupel_med_vol_diam_flag=1,
+                cloud_number_mixing_ratio_flag=1)
     ties = np.zeros(wl.fields["p"].shape[::2], np.int32)
     fo, do = run_oracle(oracle_mod, over, wl, ties=ties)
     fm, dm = _run_mixed_f32(ctx_hail, over, wl)
