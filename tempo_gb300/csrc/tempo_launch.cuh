@@ -32,16 +32,16 @@ cudaError_t launch_step(const StepArgs<S>& a, const TempoConsts<R>& c, const Isl
   if (ncol == 0) return cudaSuccess;
   const unsigned gcol = (unsigned)((ncol + kBlock - 1) / kBlock);
   const unsigned gpts = points_grid(a.ncol, a.nz);
-  if (ev) cudaEventRecord(ev[0], s);
+  if (ev) cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal);
   tempo_prep_kernel<R, S><<<gcol, kBlock, 0, s>>>(a, c, ci);
-  if (ev) cudaEventRecord(ev[1], s);
+  if (ev) cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal);
   cudaError_t e = points();
   if (e != cudaSuccess) return e;
-  if (ev) cudaEventRecord(ev[2], s);
+  if (ev) cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal);
   tempo_sedim_kernel<R, S><<<gcol, kBlock, 0, s>>>(a);
-  if (ev) cudaEventRecord(ev[3], s);
+  if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
   tempo_final_kernel<R, S><<<gpts, kBlock, 0, s>>>(a, c, ci);
-  if (ev) cudaEventRecord(ev[4], s);
+  if (ev) cudaEventRecordWithFlags(ev[4], s, cudaEventRecordExternal);
   return cudaGetLastError();
 }
 

@@ -17,6 +17,7 @@
 
 #include "tempo_consts.h"
 #include "tempo_dfloat.cuh"
+#include "tempo_dual.cuh"
 #include "tempo_types.h"
 
 namespace tg {
@@ -26,7 +27,13 @@ using D = double;
 // island type of a bulk type
 template <class R> struct IslandOf { using type = double; };
 template <> struct IslandOf<float> { using type = df; };
+// the tangent-linear / adjoint instantiations carry their own type as island
+template <class T, int N> struct IslandOf<Dual<T, N>> { using type = Dual<T, N>; };
 template <class R> using Isl = typename IslandOf<R>::type;
+// scalar type of the constant sets and lookup tables of a bulk type
+template <class R> struct ConstOf { using type = R; };
+template <class T, int N> struct ConstOf<Dual<T, N>> { using type = T; };
+template <class R> using Cst = typename ConstOf<R>::type;
 
 // ---------------------------------------------------------------------------------
 // math wrappers: accurate library functions for the chosen type (no fast-math)
@@ -48,6 +55,55 @@ __device__ __forceinline__ float Fabs(float x) { return fabsf(x); }
 __device__ __forceinline__ double Copysign(double a, double b) { return copysign(a, b); }
 __device__ __forceinline__ float Copysign(float a, float b) { return copysignf(a, b); }
 
+// the same functions on dual numbers: values through the scalar functions above (so
+// the value part matches the plain kernels), derivatives by the chain rule
+template <class T, int N>
+__device__ __forceinline__ Dual<T, N> Pow(const Dual<T, N>& a, const Dual<T, N>& b) {
+  const T r = Pow(a.v, b.v);
+  const T dfa = (a.v == T(0)) ? T(0) : b.v * r / a.v;
+  const T dfb = (a.v > T(0)) ? r * Log(a.v) : T(0);
+  Dual<T, N> o;
+  o.v = r;
+#pragma unroll
+  for (int i = 0; i < N; i++) o.d[i] = dfa * a.d[i] + dfb * b.d[i];
+  return o;
+}
+template <class T, int N, class U, class = typename std::enable_if<std::is_arithmetic<U>::value>::type>
+__device__ __forceinline__ Dual<T, N> Pow(const Dual<T, N>& a, U b) {
+  const T r = Pow(a.v, T(b));
+  return dual_chain(a, r, (a.v == T(0)) ? T(0) : T(b) * r / a.v);
+}
+template <class T, int N, class U, class = typename std::enable_if<std::is_arithmetic<U>::value>::type>
+__device__ __forceinline__ Dual<T, N> Pow(U a, const Dual<T, N>& b) {
+  const T r = Pow(T(a), b.v);
+  return dual_chain(b, r, (T(a) > T(0)) ? r * Log(T(a)) : T(0));
+}
+template <class T, int N> __device__ __forceinline__ Dual<T, N> Exp(const Dual<T, N>& a) {
+  const T r = Exp(a.v);
+  return dual_chain(a, r, r);
+}
+template <class T, int N> __device__ __forceinline__ Dual<T, N> Log(const Dual<T, N>& a) {
+  return dual_chain(a, Log(a.v), T(1) / a.v);
+}
+template <class T, int N> __device__ __forceinline__ Dual<T, N> Log10(const Dual<T, N>& a) {
+  return dual_chain(a, Log10(a.v), T(0.43429448190325182765) / a.v);
+}
+template <class T, int N> __device__ __forceinline__ Dual<T, N> Sqrt(const Dual<T, N>& a) {
+  const T r = Sqrt(a.v);
+  return dual_chain(a, r, r > T(0) ? T(0.5) / r : T(0));
+}
+template <class T, int N> __device__ __forceinline__ Dual<T, N> Cos(const Dual<T, N>& a) {
+  return dual_chain(a, Cos(a.v), -sin(a.v));
+}
+template <class T, int N> __device__ __forceinline__ Dual<T, N> Fabs(const Dual<T, N>& a) {
+  return a.v < T(0) ? -a : a;
+}
+template <class T, int N>
+__device__ __forceinline__ Dual<T, N> Copysign(const Dual<T, N>& a, const Dual<T, N>& b) {
+  const T r = Copysign(a.v, b.v);
+  return (r == a.v) ? a : -a;
+}
+
 // Fortran MAX/MIN on reals (first argument wins ties; no NaN special-casing)
 template <class T> __device__ __forceinline__ T Max(T a, T b) { return a > b ? a : b; }
 template <class T> __device__ __forceinline__ T Min(T a, T b) { return a < b ? a : b; }
@@ -56,6 +112,8 @@ template <class T> __device__ __forceinline__ T Min3(T a, T b, T c) { return Min
 // NINT: round half away from zero; INT: truncate toward zero
 template <class T> __device__ __forceinline__ int Nint(T x) { return (int)round(x); }
 template <class T> __device__ __forceinline__ int Int(T x) { return (int)x; }
+template <class T, int N> __device__ __forceinline__ int Nint(const Dual<T, N>& x) { return Nint(x.v); }
+template <class T, int N> __device__ __forceinline__ int Int(const Dual<T, N>& x) { return Int(x.v); }
 // real ** integer: binary powering with a reciprocal for negative exponents
 template <class T> __device__ __forceinline__ T Ipow(T x, int m) {
   unsigned n = m < 0 ? -(unsigned)m : (unsigned)m;
@@ -81,7 +139,7 @@ template <class T> __device__ __forceinline__ T ld(const T* p) { return __ldg(p)
 template <class R>
 struct Lev {
   using I = Isl<R>;
-  const TempoConsts<R>* cs;   // constant set of the bulk type
+  const TempoConsts<Cst<R>>* cs;  // constant set of the bulk type
   const IslandConsts<I>* ci;  // constants of the thermodynamic island
   // prognostic "1d" values (after the initial checks) and hydrometeor state
   R qc1d, nc1d, qr1d, nr1d, qi1d, ni1d, qs1d, qg1d, ng1d, qb1d;
@@ -160,8 +218,8 @@ template <class R> __device__ __forceinline__ int get_nuc(R nc) {  // utils:334-
   return v < 15 ? v : 15;
 }
 
-template <class R>
-__device__ __forceinline__ R poly_a(const R* s, R tc, R X) {  // utils:190-199
+template <class C, class R>
+__device__ __forceinline__ R poly_a(const C* s, R tc, R X) {  // utils:190-199
   return s[0] + s[1] * tc + s[2] * X + s[3] * tc * X + s[4] * tc * tc + s[5] * X * X +
          s[6] * tc * tc * X + s[7] * tc * X * X + s[8] * tc * tc * tc + s[9] * X * X * X;
 }
@@ -170,7 +228,7 @@ __device__ __forceinline__ R poly_a(const R* s, R tc, R X) {  // utils:190-199
 // smof/smog (initial), 2 = + smoz (final).
 template <class R>
 __device__ void snow_moments(Lev<R>& L, R tc, int which) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   R loga_, a_, b_, smo2_;
   L.smob = L.rs * c.oams;
   loga_ = poly_a(c.sa, tc, R(bm_s));
@@ -183,8 +241,8 @@ __device__ void snow_moments(Lev<R>& L, R tc, int which) {
   b_ = poly_a(c.sb, tc, c.cse[0]);
   L.smoc = a_ * Pow(smo2_, b_);
   if (which == 1) {
-    const R* sa = c.sa;
-    const R* sb = c.sb;
+    const auto* sa = c.sa;
+    const auto* sb = c.sb;
     loga_ = sa[0] + sa[1] * tc + sa[4] * tc * tc + sa[8] * tc * tc * tc;
     a_ = Pow(R(10.0), loga_);
     b_ = sb[0] + sb[1] * tc + sb[4] * tc * tc + sb[8] * tc * tc * tc;
@@ -230,7 +288,7 @@ __device__ __forceinline__ void aerosol_check(Lev<R>& L, uint32_t f, R dt) {  //
 // cloud_check_and_update (main:891-973) on (q, n) = (qc1d, nc1d) or temporaries
 template <class R>
 __device__ void cloud_check(Lev<R>& L, R& q, R& n, bool has_nc, R ncsave, R dt, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   R rho = R(L.rho);
   bool hit_limit = false;
   int nu_c;
@@ -289,7 +347,7 @@ __device__ void cloud_check(Lev<R>& L, R& q, R& n, bool has_nc, R ncsave, R dt, 
 // rain_check_and_update (main:976-1042)
 template <class R>
 __device__ void rain_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   R rho = R(L.rho);
   bool hit_limit = false;
   R lamr;
@@ -336,7 +394,7 @@ __device__ void rain_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
 // ice_check_and_update (main:1045-1107)
 template <class R>
 __device__ void ice_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   R rho = R(L.rho);
   bool hit_limit = false;
   R lami, xdi;
@@ -408,7 +466,7 @@ __device__ __forceinline__ int density_class(R ratio, R rb, R rb_lowdens_clamp) 
 // graupel_check_and_update (main:1137-1231)
 template <class R>
 __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   R rho = R(L.rho);
   bool hit_limit = false;
   R lamg;
@@ -480,7 +538,7 @@ __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R od
 // graupel_init (main:1234-1260) for one level
 template <class R>
 __device__ __forceinline__ void graupel_init(Lev<R>& L) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   if (L.qg1d > R(r1)) {
     R rho = R(L.rho);
     R rg = L.qg1d * rho;

@@ -30,24 +30,24 @@ template <class R> __device__ __forceinline__ int temperature_index(Isl<R> tempk
   it = max(1, -it);
   return min(it, ntb_t);
 }
-template <class R>
-__device__ __forceinline__ void rain_index(const TempoConsts<R>& c, R rr, R ilamr, int& idx_r, int& idx_r1) {  // :2526-2555
+template <class C, class R>
+__device__ __forceinline__ void rain_index(const TempoConsts<C>& c, R rr, R ilamr, int& idx_r, int& idx_r1) {  // :2526-2555
   idx_r = decade_index(rr, c.nir2, ntb_r);
   R lamr = R(1.) / ilamr;
   R lam_exp = lamr * Pow(c.crg[2] * c.org2 * c.org1, R(bm_r));
   R n0_exp = c.org1 * rr / c.am_r * Pow(lam_exp, c.cre[0]);
   idx_r1 = decade_index(n0_exp, c.nir3, ntb_r1);
 }
-template <class R>
-__device__ __forceinline__ void graupel_index(const TempoConsts<R>& c, R rg, R ilamg, int idx, int& idx_g, int& idx_g1) {  // main:2558-2588
+template <class C, class R>
+__device__ __forceinline__ void graupel_index(const TempoConsts<C>& c, R rg, R ilamg, int idx, int& idx_g, int& idx_g1) {  // main:2558-2588
   idx_g = decade_index(rg, c.nig2, ntb_g);
   R lamg = R(1.) / ilamg;
   R lam_exp = lamg * Pow(c.cgg[0][2] * c.ogg2 * c.ogg1, R(bm_g));
   R n0_exp = c.ogg1 * rg / c.am_g[idx - 1] * Pow(lam_exp, c.cge[0][0]);
   idx_g1 = decade_index(n0_exp, c.nig3, ntb_g1);
 }
-template <class R>
-__device__ __forceinline__ void cloud_index(const TempoConsts<R>& c, R rc, R nc, int& idx_c, int& idx_n) {  // :2591-2609
+template <class C, class R>
+__device__ __forceinline__ void cloud_index(const TempoConsts<C>& c, R rc, R nc, int& idx_c, int& idx_n) {  // :2591-2609
   idx_c = decade_index(rc, c.nic2, ntb_c);
   int in = Nint(R(1.0) + R(nbc) * Log(nc / c.t_nc1) / c.nic1);
   idx_n = max(1, min(in, nbc));
@@ -58,8 +58,8 @@ __device__ __forceinline__ void cloud_index(const TempoConsts<R>& c, R rc, R nc,
 // ---------------------------------------------------------------------------------
 // warm_rain (main:2279-2355)
 template <class R>
-__device__ void warm_rain(const Lev<R>& L, Tend<R>& t, const Tables<R>& T, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+__device__ void warm_rain(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, R odt) {
+  const TempoConsts<Cst<R>>& c = *L.cs;
   if (L.l_qr) {
     if (L.mvd_r > R(d0r)) {
       R ef_rr = Max(R(-0.1), R(1.0) - Exp(R(2300.0) * (L.mvd_r - R(1950.0e-6))));
@@ -102,8 +102,8 @@ __device__ void warm_rain(const Lev<R>& L, Tend<R>& t, const Tables<R>& T, R odt
 
 // rain_snow_rain_graupel (main:2638-2727)
 template <class R>
-__device__ void rain_snow_rain_graupel(const Lev<R>& L, Tend<R>& t, const Tables<R>& T, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+__device__ void rain_snow_rain_graupel(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, R odt) {
+  const TempoConsts<Cst<R>>& c = *L.cs;
   if (L.l_qr && L.l_qs) {
     if (L.rr >= c.r_r1 && L.rs >= c.r_s1) {
       int idx_t = temperature_index<R>(L.temp), idx_r, idx_r1;
@@ -164,8 +164,8 @@ __device__ void rain_snow_rain_graupel(const Lev<R>& L, Tend<R>& t, const Tables
 }
 
 // demott_nucleation (main:2823-2836)
-template <class R>
-__device__ __forceinline__ R demott_nucleation(const TempoConsts<R>& c, R tempc, R rho, R nifa) {
+template <class C, class R>
+__device__ __forceinline__ R demott_nucleation(const TempoConsts<C>& c, R tempc, R rho, R nifa) {
   R nifa_cc = Max(R(0.5), nifa * c.rho_not0 * R(1.e-6) / rho);
   R xni = (R(5.94e-5) * Pow(-tempc, R(3.33))) * (Pow(nifa_cc, (-(R(0.0264) * (tempc))) + R(0.0033)));
   xni = xni * rho / c.rho_not0 * R(1000.0);
@@ -173,8 +173,8 @@ __device__ __forceinline__ R demott_nucleation(const TempoConsts<R>& c, R tempc,
 }
 
 // koop_nucleation (main:2168-2195)
-template <class R>
-__device__ __forceinline__ R koop_nucleation(const TempoConsts<R>& c, R temp, R satw, R naero, R dt) {
+template <class C, class R>
+__device__ __forceinline__ R koop_nucleation(const TempoConsts<C>& c, R temp, R satw, R naero, R dt) {
   R xni = R(0.0);
   R mu_diff = R(210368.0) + (R(131.438) * temp) - (R(3.32373e6) / temp) - (R(41729.1) * Log(temp));
   R a_w_i = Exp(mu_diff / (R(r_uni) * temp));
@@ -190,9 +190,9 @@ __device__ __forceinline__ R koop_nucleation(const TempoConsts<R>& c, R temp, R 
 
 // ice_nucleation (main:2730-2820)
 template <class R>
-__device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<R>& T, R w, uint32_t f,
+__device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, R w, uint32_t f,
                                R dt, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   if (!(L.temp < t0)) return;
   R tempc = R(L.temp - t0);
   int idx_tc = max(1, min(Nint(-tempc), 45));
@@ -260,7 +260,7 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<R>& T, 
 // get_t1_subl (main:2861-2888) for one level
 template <class R>
 __device__ __forceinline__ R t1_subl_of(const Lev<R>& L) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   R otemp = R(1.0 / L.temp);
   R rvs = R(L.rho * L.qvsi);
   R rvs_p = rvs * otemp * (R(lsub) * otemp * c.orv - R(1.0));
@@ -279,9 +279,9 @@ __device__ __forceinline__ R t1_subl_of(const Lev<R>& L) {
 
 // ice_processes (main:2891-3018)
 template <class R>
-__device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<R>& T, R w, R t1_subl,
+__device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, R w, R t1_subl,
                               R odt) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   if (!(L.temp < t0)) return;
   R rvs = R(L.rho * L.qvsi);
   R rate_max = R((L.qv - L.qvsi) * L.rho) * odt * R(0.999);
@@ -368,8 +368,8 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<R>& T, R
 
 // riming (main:2358-2490); sets vtboost
 template <class R>
-__device__ void riming(Lev<R>& L, Tend<R>& t, const Tables<R>& T, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+__device__ void riming(Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, R odt) {
+  const TempoConsts<Cst<R>>& c = *L.cs;
   R tempc = R(L.temp - t0);
   L.vtboost = R(1.0);
   if (L.l_qc && L.l_qs) {
@@ -452,7 +452,7 @@ __device__ void riming(Lev<R>& L, Tend<R>& t, const Tables<R>& T, R odt) {
 // melting (main:3021-3119)
 template <class R>
 __device__ void melting(const Lev<R>& L, Tend<R>& t, R t1_subl, uint32_t f, R dt, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   if (!(L.temp > t0)) return;
   R tempc = R(L.temp - t0);
   R rvs = R(L.rho * L.qvsi);
@@ -516,8 +516,8 @@ __device__ void melting(const Lev<R>& L, Tend<R>& t, R t1_subl, uint32_t f, R dt
 }
 
 // aerosol_collection_efficiency (src/module_mp_tempo_aerosols.F90:76-118)
-template <class R>
-__device__ R aerosol_eff(const TempoConsts<R>& c, R d, R da, R visc, R rhoa, R temp, int species) {
+template <class C, class R>
+__device__ R aerosol_eff(const TempoConsts<C>& c, R d, R da, R visc, R rhoa, R temp, int species) {
   const R boltzman = R(1.3806503e-23), meanpath = R(0.0256e-6);
   R vt = R(1.0), rho_p = R(rho_w);
   if (species == 0) {  // rain
@@ -548,7 +548,7 @@ __device__ R aerosol_eff(const TempoConsts<R>& c, R d, R da, R visc, R rhoa, R t
 // aerosol_scavenging (main:3122-3193)
 template <class R>
 __device__ void aerosol_scavenging(const Lev<R>& L, Tend<R>& t, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   const R wf = R(0.04e-6), iff = R(0.8e-6);
   R temp = R(L.temp), rho = R(L.rho);
   if (L.l_qr && L.mvd_r > R(d0r)) {
@@ -703,8 +703,8 @@ __device__ void sum_tendencies(Lev<R>& L, const Tend<R>& t) {
 }
 
 // activate_cloud_number (main:2198-2276) without the land argument
-template <class R>
-__device__ R activate_cloud_number(const TempoConsts<R>& c, R temp, R w1d, R nwfa, const float* tnccn) {
+template <class C, class R>
+__device__ R activate_cloud_number(const TempoConsts<C>& c, R temp, R w1d, R nwfa, const float* tnccn) {
   R n_local = nwfa * R(1.e-6);
   if (n_local >= c.ta_na[ntb_arc - 1])
     n_local = c.ta_na[ntb_arc - 1] - R(1.0);
@@ -743,9 +743,9 @@ __device__ R activate_cloud_number(const TempoConsts<R>& c, R temp, R w1d, R nwf
 
 // cloud_condensation (main:1980-2056).  The saturation adjustment runs in double.
 template <class R>
-__device__ void cloud_condensation(const Lev<R>& L, Tend<R>& t, const Tables<R>& T, R w,
+__device__ void cloud_condensation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, R w,
                                    uint32_t f, R ncsave, R dt, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   if (Fabs(L.ssatw) < eps) return;
   using I = Isl<R>;
   R orho = R(1.0 / L.rho);
@@ -799,7 +799,7 @@ __device__ void cloud_condensation(const Lev<R>& L, Tend<R>& t, const Tables<R>&
 // rain_evaporation (main:2059-2121)
 template <class R>
 __device__ void rain_evaporation(const Lev<R>& L, Tend<R>& t, R odt) {
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   if (!L.l_qr) return;
   if (!((L.ssatw < -eps) && t.prw_vcd <= R(0.0))) return;
   R orho = R(1.0 / L.rho);
@@ -840,7 +840,7 @@ __device__ void rain_evaporation(const Lev<R>& L, Tend<R>& t, R odt) {
 // ---------------------------------------------------------------------------------
 template <class R>
 __device__ R reflectivity_10cm(const Lev<R>& L) {  // diags:59-121 without melting
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   R ze_r = R(1.e-22), ze_s = R(1.e-22), ze_g = R(1.e-22);
   if (L.l_qr) {
     R lamr = R(1.0) / L.ilamr;
@@ -861,7 +861,7 @@ __device__ R reflectivity_10cm(const Lev<R>& L) {  // diags:59-121 without melti
 
 template <class R>
 __device__ R max_hail_diam(const Lev<R>& L) {  // diags:398-438
-  const TempoConsts<R>& c = *L.cs;
+  const TempoConsts<Cst<R>>& c = *L.cs;
   const R threshold_conc = R(0.0005);
   if (!(L.rg / R(L.rho) >= R(1.e-6))) return R(0.0);
   if (rho_gd(L.idx_bg) < 350.0) return R(0.0);

@@ -32,6 +32,43 @@ namespace tg {
 
 template <class I, class S> __device__ __forceinline__ I ldi(const S* p) { return I(*p); }
 
+// Inputs of a point that carry derivatives in the tangent-linear and adjoint kernels
+enum InId : int { IN_T, IN_QV, IN_QC, IN_NC, IN_QR, IN_NR, IN_QI, IN_NI, IN_QS, IN_QG, IN_NG, IN_QB, IN_N };
+// Inputs of a point of phase C (final kernel) that carry derivatives
+enum CInId : int {
+  C_T1D, C_TTEN, C_QV, C_RHO, C_QC, C_NC, C_QR, C_NR, C_QI, C_NI, C_QS, C_QG, C_NG, C_QB,
+  C_TQR, C_TNR, C_TQG, C_TNG, C_TQB, C_TQS, C_TQI, C_TNI, C_TQC, C_TNC, C_N
+};
+// Array outputs of a point
+enum ArrId : int { A_T, A_QV, A_QC, A_NC, A_QR, A_NR, A_QI, A_NI, A_QS, A_QG, A_NG, A_QB, A_NWFA, A_NIFA, A_N };
+
+// Forward I/O policy: a point reads the step's arrays and stores its outputs where the
+// step keeps them.  The derivative kernels substitute policies that seed input
+// directions and contract outputs with their adjoints.
+template <class S>
+struct FwdIO {
+  const StepArgs<S>& a;
+  template <class R, class X> __device__ __forceinline__ R in(const X& v, int) const { return R(v); }
+  template <class V> __device__ __forceinline__ void arr(int id, long e, const V& v) const {
+    S* p = id == A_T ? a.t : id == A_QV ? a.qv : id == A_QC ? a.qc : id == A_NC ? a.nc
+         : id == A_QR ? a.qr : id == A_NR ? a.nr : id == A_QI ? a.qi : id == A_NI ? a.ni
+         : id == A_QS ? a.qs : id == A_QG ? a.qg : id == A_NG ? a.ng : id == A_QB ? a.qb
+         : id == A_NWFA ? a.nwfa : a.nifa;
+    p[e] = S(v);
+  }
+  template <class V> __device__ __forceinline__ void th(long e, const V& v) const { a.th[e] = S(v); }
+  template <class X> __device__ __forceinline__ void sd(X* base, long idx, const X& v) const { base[idx] = v; }
+  template <class X> __device__ __forceinline__ void sr(X* base, long idx, const X& v) const { base[idx] = v; }
+  __device__ __forceinline__ void pmask(long o, uint8_t m) const { a.pmask[o] = m; }
+  template <class V> __device__ __forceinline__ void diag3(S* p, long e3, const V& v) const {
+    if (p) p[e3] = S(v);
+  }
+  template <class V> __device__ __forceinline__ void diag2(S* p, long t2, const V& v) const {
+    if (p) p[t2] = S(v);
+  }
+  static constexpr bool forward = true;
+};
+
 // the time step in the bulk type, its reciprocal, and the time step in the island type
 // (host-computed, so that no kernel of the mixed form converts or divides in FP64)
 template <class R, class S> __device__ __forceinline__ R step_dt(const StepArgs<S>& a) {
@@ -73,23 +110,24 @@ __device__ __forceinline__ R ncsave_of(const StepArgs<S>& a, const ColGeom& g) {
   return R(a.nc_single);
 }
 
-template <class R, class S>
-__device__ __forceinline__ void load_level(const StepArgs<S>& a, long e, Lev<R>& L) {
+template <class R, class S, class IO>
+__device__ __forceinline__ void load_level(const StepArgs<S>& a, long e, Lev<R>& L, const IO& io) {
   using I = Isl<R>;
   const uint32_t f = a.flags;
-  L.t1d = (f & F_USE_T) ? ldi<I>(a.t + e) : ldi<I>(a.th + e) * ldi<I>(a.pii + e);
-  L.qv1d = ldi<I>(a.qv + e);
+  L.t1d = (f & F_USE_T) ? io.template in<I>(a.t[e], IN_T)
+                        : io.template in<I>(a.th[e], IN_T) * ldi<I>(a.pii + e);
+  L.qv1d = io.template in<I>(a.qv[e], IN_QV);
   L.pres = R(a.p[e]);
-  L.qc1d = R(a.qc[e]);
-  L.qr1d = R(a.qr[e]);
-  L.qi1d = R(a.qi[e]);
-  L.qs1d = R(a.qs[e]);
-  L.qg1d = R(a.qg[e]);
-  L.ni1d = R(a.ni[e]);
-  L.nr1d = R(a.nr[e]);
-  L.nc1d = (f & F_NC) ? R(a.nc[e]) : R(0);
-  L.ng1d = (f & F_HAIL) ? R(a.ng[e]) : R(0);
-  L.qb1d = (f & F_HAIL) ? R(a.qb[e]) : R(0);
+  L.qc1d = io.template in<R>(a.qc[e], IN_QC);
+  L.qr1d = io.template in<R>(a.qr[e], IN_QR);
+  L.qi1d = io.template in<R>(a.qi[e], IN_QI);
+  L.qs1d = io.template in<R>(a.qs[e], IN_QS);
+  L.qg1d = io.template in<R>(a.qg[e], IN_QG);
+  L.ni1d = io.template in<R>(a.ni[e], IN_NI);
+  L.nr1d = io.template in<R>(a.nr[e], IN_NR);
+  L.nc1d = (f & F_NC) ? io.template in<R>(a.nc[e], IN_NC) : R(0);
+  L.ng1d = (f & F_HAIL) ? io.template in<R>(a.ng[e], IN_NG) : R(0);
+  L.qb1d = (f & F_HAIL) ? io.template in<R>(a.qb[e], IN_QB) : R(0);
   L.temp = L.t1d;
   L.qv = Max(I(min_qv), L.qv1d);
   L.rho = rho_of(*L.ci, I(L.pres), L.temp, L.qv);
@@ -116,19 +154,20 @@ __device__ __forceinline__ void initial_checks(Lev<R>& L, uint32_t f, R ncsave, 
   graupel_check(L, L.qg1d, L.ng1d, L.qb1d, (f & F_HAIL) != 0, dt, odt);
 }
 
-template <class R, class S>
-__device__ __forceinline__ void store_checked(const StepArgs<S>& a, long e, const Lev<R>& L) {
-  a.qc[e] = S(L.qc1d);
-  a.qr[e] = S(L.qr1d);
-  a.nr[e] = S(L.nr1d);
-  a.qi[e] = S(L.qi1d);
-  a.ni[e] = S(L.ni1d);
-  a.qs[e] = S(L.qs1d);
-  a.qg[e] = S(L.qg1d);
-  if (a.flags & F_NC) a.nc[e] = S(L.nc1d);
+template <class R, class S, class IO>
+__device__ __forceinline__ void store_checked(const StepArgs<S>& a, long e, const Lev<R>& L,
+                                              const IO& io) {
+  io.arr(A_QC, e, L.qc1d);
+  io.arr(A_QR, e, L.qr1d);
+  io.arr(A_NR, e, L.nr1d);
+  io.arr(A_QI, e, L.qi1d);
+  io.arr(A_NI, e, L.ni1d);
+  io.arr(A_QS, e, L.qs1d);
+  io.arr(A_QG, e, L.qg1d);
+  if (a.flags & F_NC) io.arr(A_NC, e, L.nc1d);
   if (a.flags & F_HAIL) {
-    a.ng[e] = S(L.ng1d);
-    a.qb[e] = S(L.qb1d);
+    io.arr(A_NG, e, L.ng1d);
+    io.arr(A_QB, e, L.qb1d);
   }
 }
 
@@ -137,7 +176,7 @@ __device__ __forceinline__ void store_checked(const StepArgs<S>& a, long e, cons
 // ---------------------------------------------------------------------------------
 template <class R, class S>
 __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__ StepArgs<S> a,
-                                                          const __grid_constant__ TempoConsts<R> cst,
+                                                          const __grid_constant__ TempoConsts<Cst<R>> cst,
                                                           const __grid_constant__ IslandConsts<Isl<R>> ci) {
   using I = Isl<R>;
   const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -210,9 +249,10 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
     Lev<R> L;
     L.cs = &cst;
     L.ci = &ci;
-    load_level(a, e, L);
+    const FwdIO<S> io{a};
+    load_level(a, e, L, io);
     initial_checks(L, f, ncsave, do_ginit, dt, odt);
-    store_checked(a, e, L);
+    store_checked(a, e, L, io);
   }
   const long t2 = g.tile2;
   if (a.rain_precip) a.rain_precip[t2] = S(0);
@@ -241,7 +281,7 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
 // (main:420-522); 1 = saturation adjustment (main:530-560); 2 = rain evaporation
 // (main:563-588).
 template <class R>
-__device__ __forceinline__ void points_stage(int stage, Lev<R>& L, Tend<R>& td, const Tables<R>& T,
+__device__ __forceinline__ void points_stage(int stage, Lev<R>& L, Tend<R>& td, const Tables<Cst<R>>& T,
                                              const IslandConsts<Isl<R>>& ci, uint32_t f, R w, R dt,
                                              R odt, Isl<R> dti, R ncsave, R ncsave_cond, R nwfa_in,
                                              R nifa_in) {
@@ -330,18 +370,14 @@ __host__ __device__ constexpr int points_min_blocks(int v) {
 // ---------------------------------------------------------------------------------
 // points: phase A at one (level, active slot)
 // ---------------------------------------------------------------------------------
-template <class R, class S, int V>
-__global__ void __launch_bounds__(128, points_min_blocks(V)) tempo_points_kernel(const __grid_constant__ StepArgs<S> a,
-                                                            const __grid_constant__ Tables<R> T,
-                                                            const __grid_constant__ TempoConsts<R> cst,
-                                                            const __grid_constant__ IslandConsts<Isl<R>> ci) {
+// Phase A at point (level k, active slot s); outputs go through the I/O policy.
+template <class R, class S, int V, class IO>
+__device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<Cst<R>>& T,
+                                             const TempoConsts<Cst<R>>& cst,
+                                             const IslandConsts<Isl<R>>& ci, int k, long s,
+                                             const IO& io) {
   using I = Isl<R>;
-  const long nact = (long)*a.nact;
-  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int nz = a.nz;
-  if (p >= nact * nz) return;
-  const int k = (int)(p / nact);
-  const long s = p - (long)k * nact;
   const long c = a.act[s];
   const ColGeom g = col_geom(a, c);
   const long e = g.base + (long)k * a.NI;
@@ -359,7 +395,7 @@ __global__ void __launch_bounds__(128, points_min_blocks(V)) tempo_points_kernel
   Lev<R> L;
   L.cs = &cst;
   L.ci = &ci;
-  load_level(a, e, L);
+  load_level(a, e, L, io);
   const R w = R(a.w[e]);
   R nwfa_in, nifa_in;
   if (has_nwfa && has_nifa) {
@@ -464,54 +500,66 @@ __global__ void __launch_bounds__(128, points_min_blocks(V)) tempo_points_kernel
     vtc = L.rhof * R(av_c) * cc.ccg[nu_c - 1][4] * cc.ocg2[nu_c - 1] * pb;
     vtnc = L.rhof * R(av_c) * cc.ccg[nu_c - 1][3] * cc.ocg1[nu_c - 1] * pb;
   }
-  a.pmask[o] = (L.l_qr ? PM_QR : 0) | (L.l_qg ? PM_QG : 0) | (L.l_qs ? PM_QS : 0) |
-               (L.l_qi ? PM_QI : 0) | (L.l_qc ? PM_QC : 0);
+  io.pmask(o, (L.l_qr ? PM_QR : 0) | (L.l_qg ? PM_QG : 0) | (L.l_qs ? PM_QS : 0) |
+               (L.l_qi ? PM_QI : 0) | (L.l_qc ? PM_QC : 0));
 
-  sd[SD_TTEN * fsd + o] = L.tten;
-  sd[SD_QV * fsd + o] = L.qv;
-  sd[SD_RHO * fsd + o] = L.rho;
-  sd[SD_XRR * fsd + o] = I(L.rr);
-  sd[SD_XNR * fsd + o] = I(L.nr);
-  sd[SD_XRG * fsd + o] = I(L.rg);
-  sd[SD_XNG * fsd + o] = I(L.ng);
-  sd[SD_XRB * fsd + o] = I(L.rb);
-  sd[SD_XRS * fsd + o] = I(L.rs);
-  sd[SD_XRI * fsd + o] = I(L.ri);
-  sd[SD_XNI * fsd + o] = I(L.ni);
-  sd[SD_XRC * fsd + o] = I(L.rc);
-  sd[SD_XNC * fsd + o] = I(L.nc);
-  sd[SD_TQR * fsd + o] = I(L.qrten);
-  sd[SD_TNR * fsd + o] = I(L.nrten);
-  sd[SD_TQG * fsd + o] = I(L.qgten);
-  sd[SD_TNG * fsd + o] = I(L.ngten);
-  sd[SD_TQB * fsd + o] = I(L.qbten);
-  sd[SD_TQS * fsd + o] = I(L.qsten);
-  sd[SD_TQI * fsd + o] = I(L.qiten);
-  sd[SD_TNI * fsd + o] = I(L.niten);
-  sd[SD_TQC * fsd + o] = I(L.qcten);
-  sd[SD_TNC * fsd + o] = I(L.ncten);
-  if constexpr (!std::is_same<I, double>::value) {
+  io.sd(sd, SD_TTEN * fsd + o, I(L.tten));
+  io.sd(sd, SD_QV * fsd + o, I(L.qv));
+  io.sd(sd, SD_RHO * fsd + o, I(L.rho));
+  io.sd(sd, SD_XRR * fsd + o, I(I(L.rr)));
+  io.sd(sd, SD_XNR * fsd + o, I(I(L.nr)));
+  io.sd(sd, SD_XRG * fsd + o, I(I(L.rg)));
+  io.sd(sd, SD_XNG * fsd + o, I(I(L.ng)));
+  io.sd(sd, SD_XRB * fsd + o, I(I(L.rb)));
+  io.sd(sd, SD_XRS * fsd + o, I(I(L.rs)));
+  io.sd(sd, SD_XRI * fsd + o, I(I(L.ri)));
+  io.sd(sd, SD_XNI * fsd + o, I(I(L.ni)));
+  io.sd(sd, SD_XRC * fsd + o, I(I(L.rc)));
+  io.sd(sd, SD_XNC * fsd + o, I(I(L.nc)));
+  io.sd(sd, SD_TQR * fsd + o, I(I(L.qrten)));
+  io.sd(sd, SD_TNR * fsd + o, I(I(L.nrten)));
+  io.sd(sd, SD_TQG * fsd + o, I(I(L.qgten)));
+  io.sd(sd, SD_TNG * fsd + o, I(I(L.ngten)));
+  io.sd(sd, SD_TQB * fsd + o, I(I(L.qbten)));
+  io.sd(sd, SD_TQS * fsd + o, I(I(L.qsten)));
+  io.sd(sd, SD_TQI * fsd + o, I(I(L.qiten)));
+  io.sd(sd, SD_TNI * fsd + o, I(I(L.niten)));
+  io.sd(sd, SD_TQC * fsd + o, I(I(L.qcten)));
+  io.sd(sd, SD_TNC * fsd + o, I(I(L.ncten)));
+  if constexpr (std::is_same<I, df>::value) {
     // the mixed form's sedimentation multiplies by these instead of dividing per sweep
     const I odz = 1.0 / ldi<I>(a.dz + e);
-    sd[SD_ODZ * fsd + o] = odz;
-    sd[SD_OZR * fsd + o] = odz / L.rho;
+    io.sd(sd, SD_ODZ * fsd + o, I(odz));
+    io.sd(sd, SD_OZR * fsd + o, I(odz / L.rho));
   }
-  sr[SR_VTR * fsd + o] = vtr;
-  sr[SR_VTNR * fsd + o] = vtnr;
-  sr[SR_VTG * fsd + o] = vtg;
-  sr[SR_VTNG * fsd + o] = vtng;
-  sr[SR_VTSA * fsd + o] = vsa;
-  sr[SR_VTSB * fsd + o] = vsb;
-  sr[SR_VTI * fsd + o] = vti;
-  sr[SR_VTNI * fsd + o] = vtni;
-  sr[SR_VTC * fsd + o] = vtc;
-  sr[SR_VTNC * fsd + o] = vtnc;
+  io.sr(sr, SR_VTR * fsd + o, R(vtr));
+  io.sr(sr, SR_VTNR * fsd + o, R(vtnr));
+  io.sr(sr, SR_VTG * fsd + o, R(vtg));
+  io.sr(sr, SR_VTNG * fsd + o, R(vtng));
+  io.sr(sr, SR_VTSA * fsd + o, R(vsa));
+  io.sr(sr, SR_VTSB * fsd + o, R(vsb));
+  io.sr(sr, SR_VTI * fsd + o, R(vti));
+  io.sr(sr, SR_VTNI * fsd + o, R(vtni));
+  io.sr(sr, SR_VTC * fsd + o, R(vtc));
+  io.sr(sr, SR_VTNC * fsd + o, R(vtnc));
 
   // outputs final after phase A: checked prognostics, qv, aerosols (main:738-748)
-  store_checked(a, e, L);
-  a.qv[e] = S(Max(I(min_qv), (L.qv1d + L.qvten * dti)));
-  if (has_nwfa) a.nwfa[e] = S(Max(R(nwfa_default), Min(R(aero_max), (nwfa_in + L.nwfaten * dt))));
-  if (has_nifa) a.nifa[e] = S(Max(R(nifa_default), Min(R(aero_max), (nifa_in + L.nifaten * dt))));
+  store_checked(a, e, L, io);
+  io.arr(A_QV, e, Max(I(min_qv), (L.qv1d + L.qvten * dti)));
+  if (has_nwfa) io.arr(A_NWFA, e, Max(R(nwfa_default), Min(R(aero_max), (nwfa_in + L.nwfaten * dt))));
+  if (has_nifa) io.arr(A_NIFA, e, Max(R(nifa_default), Min(R(aero_max), (nifa_in + L.nifaten * dt))));
+}
+
+template <class R, class S, int V>
+__global__ void __launch_bounds__(128, points_min_blocks(V)) tempo_points_kernel(const __grid_constant__ StepArgs<S> a,
+                                                            const __grid_constant__ Tables<Cst<R>> T,
+                                                            const __grid_constant__ TempoConsts<Cst<R>> cst,
+                                                            const __grid_constant__ IslandConsts<Isl<R>> ci) {
+  const long nact = (long)*a.nact;
+  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nact * a.nz) return;
+  const int k = (int)(p / nact);
+  points_point<R, S, V>(a, T, cst, ci, k, p - (long)k * nact, FwdIO<S>{a});
 }
 
 // ---------------------------------------------------------------------------------
@@ -699,17 +747,13 @@ __device__ __forceinline__ void atomic_max_nonneg(double* p, double v) {
 // ---------------------------------------------------------------------------------
 // final: phase C at one (level, active slot)
 // ---------------------------------------------------------------------------------
-template <class R, class S>
-__global__ void __launch_bounds__(128) tempo_final_kernel(const __grid_constant__ StepArgs<S> a,
-                                                           const __grid_constant__ TempoConsts<R> cst,
-                                                           const __grid_constant__ IslandConsts<Isl<R>> ci) {
+// Phase C at point (level k, active slot s); outputs go through the I/O policy.
+template <class R, class S, class IO>
+__device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoConsts<Cst<R>>& cst,
+                                            const IslandConsts<Isl<R>>& ci, int k, long s,
+                                            const IO& io) {
   using I = Isl<R>;
-  const long nact = (long)*a.nact;
-  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int nz = a.nz;
-  if (p >= nact * nz) return;
-  const int k = (int)(p / nact);
-  const long s = p - (long)k * nact;
   const ColGeom g = col_geom(a, a.act[s]);
   const long e = g.base + (long)k * a.NI;
   const uint32_t f = a.flags;
@@ -723,24 +767,25 @@ __global__ void __launch_bounds__(128) tempo_final_kernel(const __grid_constant_
   Lev<R> L;
   L.cs = &cst;
   L.ci = &ci;
-  L.t1d = (f & F_USE_T) ? ldi<I>(a.t + e) : ldi<I>(a.th + e) * ldi<I>(a.pii + e);
+  L.t1d = (f & F_USE_T) ? io.template in<I>(a.t[e], C_T1D)
+                        : io.template in<I>(a.th[e], C_T1D) * ldi<I>(a.pii + e);
   L.pres = R(a.p[e]);
-  L.tten = sd[SD_TTEN * fsd + o];
-  L.qv = sd[SD_QV * fsd + o];
-  L.rho = sd[SD_RHO * fsd + o];
+  L.tten = io.template in<I>(sd[SD_TTEN * fsd + o], C_TTEN);
+  L.qv = io.template in<I>(sd[SD_QV * fsd + o], C_QV);
+  L.rho = io.template in<I>(sd[SD_RHO * fsd + o], C_RHO);
   L.temp = L.t1d + L.tten * dti;
   const R ocp = R(1.0) / (R(cp) * (R(1.0) + R(0.887) * R(L.qv)));
   const R lvap = R(lvap0) + (R(2106.0) - R(4218.0)) * R(L.temp - t0);
-  L.qc1d = R(a.qc[e]);
-  L.nc1d = has_nc ? R(a.nc[e]) : R(0);
-  L.qr1d = R(a.qr[e]);
-  L.nr1d = R(a.nr[e]);
-  L.qi1d = R(a.qi[e]);
-  L.ni1d = R(a.ni[e]);
-  L.qs1d = R(a.qs[e]);
-  L.qg1d = R(a.qg[e]);
-  L.ng1d = hail ? R(a.ng[e]) : R(0);
-  L.qb1d = hail ? R(a.qb[e]) : R(0);
+  L.qc1d = io.template in<R>(a.qc[e], C_QC);
+  L.nc1d = has_nc ? io.template in<R>(a.nc[e], C_NC) : R(0);
+  L.qr1d = io.template in<R>(a.qr[e], C_QR);
+  L.nr1d = io.template in<R>(a.nr[e], C_NR);
+  L.qi1d = io.template in<R>(a.qi[e], C_QI);
+  L.ni1d = io.template in<R>(a.ni[e], C_NI);
+  L.qs1d = io.template in<R>(a.qs[e], C_QS);
+  L.qg1d = io.template in<R>(a.qg[e], C_QG);
+  L.ng1d = hail ? io.template in<R>(a.ng[e], C_NG) : R(0);
+  L.qb1d = hail ? io.template in<R>(a.qb[e], C_QB) : R(0);
   L.qrten = R(sd[SD_TQR * fsd + o]);
   L.nrten = R(sd[SD_TNR * fsd + o]);
   L.qgten = R(sd[SD_TQG * fsd + o]);
@@ -778,9 +823,9 @@ __global__ void __launch_bounds__(128) tempo_final_kernel(const __grid_constant_
   }
   const I tnew = L.t1d + L.tten * dti;
   if (f & F_USE_T)
-    a.t[e] = S(tnew);
+    io.arr(A_T, e, tnew);
   else
-    a.th[e] = S(tnew / ldi<I>(a.pii + e));
+    io.th(e, tnew / ldi<I>(a.pii + e));
   // final checks (main:750-781)
   cloud_check(L, L.qc1d, L.nc1d, has_nc, ncsave, dt, odt);
   rain_check(L, L.qr1d, L.nr1d, dt, odt);
@@ -788,18 +833,20 @@ __global__ void __launch_bounds__(128) tempo_final_kernel(const __grid_constant_
   snow_check(L, L.qs1d, dt, odt);
   if (L.l_qs) snow_moments(L, R(Min(I(-0.1), L.temp - t0)), 2);
   graupel_check(L, L.qg1d, L.ng1d, L.qb1d, hail, dt, odt);
-  store_checked(a, e, L);
+  store_checked(a, e, L, io);
   // diagnostics (main:796-863)
   const long e3 = tile3_of(a, g, k);
-  if (a.ncmr) a.ncmr[e3] = S(L.nc * R(L.rho));
-  if (a.mvd_r) a.mvd_r[e3] = S(L.mvd_r);
-  if (a.mvd_g) a.mvd_g[e3] = S(L.mvd_g);
+  io.diag3(a.ncmr, e3, L.nc * R(L.rho));
+  io.diag3(a.mvd_r, e3, L.mvd_r);
+  io.diag3(a.mvd_g, e3, L.mvd_g);
   S mhd = S(0);
-  if (f & F_MHD) {
-    mhd = S(max_hail_diam(L));
-    if (a.mhd_col && mhd > S(0)) atomic_max_nonneg(a.mhd_col + g.tile2, mhd);
+  if constexpr (IO::forward && !IsDual<S>::value) {  // a maximum over levels: no derivative
+    if (f & F_MHD) {
+      mhd = S(max_hail_diam(L));
+      if (a.mhd_col && mhd > S(0)) atomic_max_nonneg(a.mhd_col + g.tile2, mhd);
+    }
   }
-  if (a.refl10cm) a.refl10cm[e3] = S(reflectivity_10cm(L));
+  if (a.refl10cm) io.diag3(a.refl10cm, e3, reflectivity_10cm(L));
   if (f & F_RE) {  // effective_radius (diags:13-56)
     R rec = R(0), rei = R(0), res = R(0);
     if (L.l_qc) {
@@ -808,13 +855,13 @@ __global__ void __launch_bounds__(128) tempo_final_kernel(const __grid_constant_
     }
     if (L.l_qi) rei = Max(R(2.51e-6), Min(R(0.5) * (R(3.0) + R(mu_i)) * L.ilami, R(125.e-6)));
     if (L.l_qs) res = Max(R(5.01e-6), Min(R(0.5) * (L.smoc / L.smob), R(999.e-6)));
-    if (a.re_cloud) a.re_cloud[e3] = S(rec);
-    if (a.re_ice) a.re_ice[e3] = S(rei);
-    if (a.re_snow) a.re_snow[e3] = S(res);
+    io.diag3(a.re_cloud, e3, rec);
+    io.diag3(a.re_ice, e3, rei);
+    io.diag3(a.re_snow, e3, res);
   } else {
-    if (a.re_cloud) a.re_cloud[e3] = S(0);
-    if (a.re_ice) a.re_ice[e3] = S(0);
-    if (a.re_snow) a.re_snow[e3] = S(0);
+    io.diag3(a.re_cloud, e3, R(0));
+    io.diag3(a.re_ice, e3, R(0));
+    io.diag3(a.re_snow, e3, R(0));
   }
   if (k != 0) return;
   // column diagnostics on the lowest level (main:785-794; driver:452-484)
@@ -824,13 +871,24 @@ __global__ void __launch_bounds__(128) tempo_final_kernel(const __grid_constant_
   const I ffrac = (prec_i + prec_s + prec_g) / (prec_i + prec_s + prec_g + prec_r + r1);
   const I frz = ((L.temp - t0) < -0.5) ? prec_r + prec_c : I(0.0);
   const long t2 = g.tile2;
-  if (a.rain_precip) a.rain_precip[t2] = S(prec_r);
-  if (a.ice_precip) a.ice_precip[t2] = S(prec_i);
-  if (a.snow_precip) a.snow_precip[t2] = S(prec_s);
-  if (a.graupel_precip) a.graupel_precip[t2] = S(prec_g);
-  if (a.frozen_fraction) a.frozen_fraction[t2] = S(ffrac);
-  if (a.frz_rain) a.frz_rain[t2] = S(frz);
-  if (a.mhd_sfc) a.mhd_sfc[t2] = mhd;
+  io.diag2(a.rain_precip, t2, prec_r);
+  io.diag2(a.ice_precip, t2, prec_i);
+  io.diag2(a.snow_precip, t2, prec_s);
+  io.diag2(a.graupel_precip, t2, prec_g);
+  io.diag2(a.frozen_fraction, t2, ffrac);
+  io.diag2(a.frz_rain, t2, frz);
+  io.diag2(a.mhd_sfc, t2, mhd);
+}
+
+template <class R, class S>
+__global__ void __launch_bounds__(128) tempo_final_kernel(const __grid_constant__ StepArgs<S> a,
+                                                           const __grid_constant__ TempoConsts<Cst<R>> cst,
+                                                           const __grid_constant__ IslandConsts<Isl<R>> ci) {
+  const long nact = (long)*a.nact;
+  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nact * a.nz) return;
+  const int k = (int)(p / nact);
+  final_point<R, S>(a, cst, ci, k, p - (long)k * nact, FwdIO<S>{a});
 }
 
 }  // namespace tg

@@ -1,30 +1,28 @@
 """The mixed-precision form (FP32 bulk, double-float islands) against the FP64 oracle.
 
-Per-field max and RMS relative error (relative to the larger of the oracle's value,
-the field's value before the step and the reference's existence threshold),
-column water budget and 10-cm reflectivity in dBZ, on the stretched-grid workload
-(config-1 generator) and the hail-aware deep-convection workload (config-2
-generator).  Bounds are stated per field below.  FP32 process rates move values by
-about 1e-7 relative; larger differences come from threshold branches (existence
+Per field, the fraction of points whose relative error (relative to the larger of the
+oracle's value, the field's value before the step and the reference's existence
+threshold) exceeds 1e-5 and 1e-2; the column water budget; 10-cm reflectivity in
+dBZ -- on the stretched-grid workload (config-1 generator) and the hail-aware
+deep-convection workload (config-2 generator).  FP32 process rates move values by
+about 1e-7 relative; the larger differences come from threshold branches (existence
 limits, table bin edges) that an FP32 value crosses where the FP64 one does not, so
-RMS is held tighter than the maximum.
+the bounds are on how rare those points are.
 """
 import numpy as np
 import pytest
 
-from parity_util import DIAG2, FLOOR, compare, make_diags, rel_err, run_oracle
+from parity_util import DIAG2, FLOOR, make_diags, rel_err, run_oracle
 
 pytestmark = pytest.mark.gpu
 
-# (max, rms) relative-error bounds per field
-BOUNDS = {
-    "t": (1e-6, 1e-7), "qv": (1e-5, 1e-6),
-    "qc": (5e-2, 1e-4), "qr": (5e-2, 1e-4), "qi": (1e-3, 1e-5), "qs": (1e-3, 1e-5),
-    "qg": (5e-2, 3e-4), "ni": (1e-2, 1e-5), "nr": (5e-2, 1e-4), "nc": (5e-1, 2e-3),
-    "nwfa": (5e-2, 2e-4), "nifa": (1e-3, 1e-5), "ng": (5e-2, 1e-4), "qb": (5e-2, 1e-4),
-}
-DIAG_BOUNDS = (1e-1, 1e-3)   # diagnostics other than reflectivity
-REFL_DBZ = (0.5, 1e-2)       # (max, rms) absolute dBZ
+# Per field: at most FRAC_5 of the points beyond 1e-5 relative error, and at most
+# FRAC_2 beyond 1e-2 (an FP32 value crossing an existence limit or a table bin edge
+# that the FP64 value does not: a species present in one run and absent in the other).
+FRAC_5 = {"t": 1e-3, "qv": 1e-3}
+FRAC_5_DEFAULT = 5e-2
+FRAC_2 = 2e-3
+REFL_DBZ = (0.1, 2e-3)       # |d dBZ| > 0.1 on at most 0.2 % of the points
 
 
 def _run_mixed_f32(ctx, over, wl, itimestep=1):
@@ -44,19 +42,30 @@ def _column_water(f, rho, dz):
     return (q.astype(np.float64) * rho * dz).sum(axis=1)   # kg m-2 per column
 
 
+def _fractions(a, b, floor, scale=None):
+    e = rel_err(a, b, floor, scale)
+    return float((e > 1e-5).mean()), float((e > 1e-2).mean())
+
+
 def _check(fm, dm, fo, do, wl):
     # the FP32 inputs are the FP64 inputs rounded: compare on the oracle run from
     # those same rounded inputs
-    errs = compare(fm, {k: v for k, v in dm.items() if k != "refl10cm"}, fo,
-                   {k: v for k, v in do.items() if k != "refl10cm"}, inputs=wl.fields)
-    bad = []
-    for n, (mx, rms) in errs.items():
-        bmx, brms = BOUNDS.get(n, DIAG_BOUNDS)
-        if mx > bmx or rms > brms:
-            bad.append((n, mx, rms))
+    bad, errs = [], {}
+    for n in ("t", "qv", "qc", "qr", "qi", "qs", "qg", "ni", "nr", "nc", "ng", "qb"):
+        if n in fm and n in fo:
+            f5, f2 = _fractions(fm[n], fo[n], FLOOR[n], wl.fields.get(n))
+            errs[n] = (f5, f2)
+            if f5 > FRAC_5.get(n, FRAC_5_DEFAULT) or f2 > FRAC_2:
+                bad.append((n, f5, f2))
+    for n in dm:
+        if n in do and n != "refl10cm":
+            f5, f2 = _fractions(dm[n], do[n], FLOOR[n])
+            errs[n] = (f5, f2)
+            if f2 > FRAC_2:
+                bad.append((n, f5, f2))
     e = np.abs(dm["refl10cm"].astype(np.float64) - do["refl10cm"])
-    if e.max() > REFL_DBZ[0] or np.sqrt((e * e).mean()) > REFL_DBZ[1]:
-        bad.append(("refl10cm_dbz", float(e.max()), float(np.sqrt((e * e).mean()))))
+    if (e > REFL_DBZ[0]).mean() > REFL_DBZ[1]:
+        bad.append(("refl10cm_dbz", float(e.max()), float((e > REFL_DBZ[0]).mean())))
     # water budget: sum of water over the column plus surface precipitation (mm =
     # kg m-2), with the input density and layer depths for both runs
     from tempo_gb300.workloads import RD
