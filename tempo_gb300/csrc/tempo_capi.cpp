@@ -467,7 +467,8 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   const size_t act_bytes = al(npad * sizeof(int));
   const size_t pm_bytes = al(nzs * npad);
   const size_t cm_bytes = al(npad);
-  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + 256;
+  const size_t hg_bytes = al(nzs * npad * rsz);
+  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes + 256;
   if (int rc = ensure_scratch(c, total)) return rc;
   char* sp = (char*)c->scratch;
   a.sd = sp;
@@ -482,6 +483,8 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   sp += pm_bytes;
   a.cmask = (uint8_t*)sp;
   sp += cm_bytes;
+  a.hgt = sp;
+  sp += hg_bytes;
   a.nact = (unsigned int*)sp;
   a.stats = c->d_stats;
   c->last_cols = a.ncol;

@@ -218,8 +218,9 @@ template <class R> __device__ __forceinline__ int get_nuc(R nc) {  // utils:334-
   return v < 15 ? v : 15;
 }
 
-template <class C, class R>
-__device__ __forceinline__ R poly_a(const C* s, R tc, R X) {  // utils:190-199
+template <class C, class R, class XT>
+__device__ __forceinline__ R poly_a(const C* s, R tc, XT Xin) {
+  const R X = R(Xin);  // utils:190-199
   return s[0] + s[1] * tc + s[2] * X + s[3] * tc * X + s[4] * tc * tc + s[5] * X * X +
          s[6] * tc * tc * X + s[7] * tc * X * X + s[8] * tc * tc * tc + s[9] * X * X * X;
 }

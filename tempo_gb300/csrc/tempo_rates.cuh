@@ -109,7 +109,7 @@ __device__ void rain_snow_rain_graupel(const Lev<R>& L, Tend<R>& t, const Tables
       int idx_t = temperature_index<R>(L.temp), idx_r, idx_r1;
       rain_index(c, L.rr, L.ilamr, idx_r, idx_r1);
       int idx_s = decade_index(L.rs, c.nis2, ntb_s);
-      const R* e = T.qs + 12L * ((idx_s - 1) + (long)(idx_t - 1) * ntb_s +
+      const Cst<R>* e = T.qs + 12L * ((idx_s - 1) + (long)(idx_t - 1) * ntb_s +
                                  (long)(idx_r1 - 1) * ntb_s * ntb_t +
                                  (long)(idx_r - 1) * ntb_s * ntb_t * ntb_r1);
       R tcs_racs1 = ld(e + 0), tmr_racs1 = ld(e + 1), tmr_racs2 = ld(e + 3);
@@ -139,7 +139,7 @@ __device__ void rain_snow_rain_graupel(const Lev<R>& L, Tend<R>& t, const Tables
       int idx_r, idx_r1, idx_g, idx_g1;
       rain_index(c, L.rr, L.ilamr, idx_r, idx_r1);
       graupel_index(c, L.rg, L.ilamg, ig, idx_g, idx_g1);
-      const R* e = T.qg + 5L * ((idx_g1 - 1) + (long)(idx_g - 1) * ntb_g1 +
+      const Cst<R>* e = T.qg + 5L * ((idx_g1 - 1) + (long)(idx_g - 1) * ntb_g1 +
                                 (long)(ig - 1) * ntb_g1 * ntb_g +
                                 (long)(idx_r1 - 1) * ntb_g1 * ntb_g * nrhg +
                                 (long)(idx_r - 1) * ntb_g1 * ntb_g * nrhg * ntb_r1);
@@ -207,7 +207,7 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
   if (L.rr > c.r_r1) {
     int idx_r, idx_r1;
     rain_index(c, L.rr, L.ilamr, idx_r, idx_r1);
-    const R* e = T.qrfz + 4L * ((idx_r - 1) + (long)(idx_r1 - 1) * ntb_r +
+    const Cst<R>* e = T.qrfz + 4L * ((idx_r - 1) + (long)(idx_r1 - 1) * ntb_r +
                                 (long)(idx_tc - 1) * ntb_r * ntb_r1 +
                                 (long)(idx_in - 1) * ntb_r * ntb_r1 * ntb_t1);
     t.prg_rfz = ld(e + 2) * odt;
@@ -225,7 +225,7 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
   if (L.rc > c.r_c1) {
     int idx_c, idx_n;
     cloud_index(c, L.rc, L.nc, idx_c, idx_n);
-    const R* e = T.qcfz + 2L * ((idx_c - 1) + (long)(idx_n - 1) * ntb_c +
+    const Cst<R>* e = T.qcfz + 2L * ((idx_c - 1) + (long)(idx_n - 1) * ntb_c +
                                 (long)(idx_tc - 1) * ntb_c * nbc +
                                 (long)(idx_in - 1) * ntb_c * nbc * ntb_t1);
     t.pri_wfz = ld(e + 0) * odt;
@@ -288,7 +288,7 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>&
   R ssati = R(L.ssati);
   if (L.l_qi) {
     int idx_i = decade_index(L.ri, c.nii2, ntb_i), idx_i1 = decade_index(L.ni, c.nii3, ntb_i1);
-    R xdi = Max(c.d0i, (R(bm_i) + R(mu_i) + R(1.)) * L.ilami);
+    R xdi = Max(R(c.d0i), (R(bm_i) + R(mu_i) + R(1.)) * L.ilami);
     R xmi = c.am_i * Pow(xdi, R(bm_i));
     R oxmi = R(1.0) / xmi;
     t.pri_ide = R(c_cube) * t1_subl * L.diffu * ssati * rvs * c.oig1 * c.cig[4] * L.ni * L.ilami;
@@ -316,7 +316,7 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>&
       t.pni_iau = Min(L.ni * R(.95) * odt, t.pni_iau);
     }
     // main:2959-2962 recompute the same xdi/xmi from ilami
-    xdi = Max(c.d0i, (R(bm_i) + R(mu_i) + R(1.)) * L.ilami);
+    xdi = Max(R(c.d0i), (R(bm_i) + R(mu_i) + R(1.)) * L.ilami);
     xmi = c.am_i * Pow(xdi, R(bm_i));
     oxmi = R(1.) / xmi;
     if (L.rs >= c.r_s1) {

@@ -57,6 +57,13 @@ struct FwdIO {
     p[e] = S(v);
   }
   template <class V> __device__ __forceinline__ void th(long e, const V& v) const { a.th[e] = S(v); }
+  // scratch read of element type E as type O (seeded direction id in derivative policies)
+  template <class O, class E> __device__ __forceinline__ O sdin(long idx, int) const {
+    return O(reinterpret_cast<const E*>(a.sd)[idx]);
+  }
+  template <class E> __device__ __forceinline__ E scin(long idx) const {
+    return reinterpret_cast<const E*>(a.sc)[idx];
+  }
   template <class X> __device__ __forceinline__ void sd(X* base, long idx, const X& v) const { base[idx] = v; }
   template <class X> __device__ __forceinline__ void sr(X* base, long idx, const X& v) const { base[idx] = v; }
   __device__ __forceinline__ void pmask(long o, uint8_t m) const { a.pmask[o] = m; }
@@ -72,13 +79,15 @@ struct FwdIO {
 // the time step in the bulk type, its reciprocal, and the time step in the island type
 // (host-computed, so that no kernel of the mixed form converts or divides in FP64)
 template <class R, class S> __device__ __forceinline__ R step_dt(const StepArgs<S>& a) {
-  if constexpr (sizeof(R) == sizeof(double)) return a.dt; else return a.dt_hi;
+  if constexpr (std::is_same<Cst<R>, double>::value) return R(a.dt); else return R(a.dt_hi);
 }
 template <class R, class S> __device__ __forceinline__ R step_odt(const StepArgs<S>& a) {
-  if constexpr (sizeof(R) == sizeof(double)) return a.odt; else return a.odt_f;
+  if constexpr (std::is_same<Cst<R>, double>::value) return R(a.odt); else return R(a.odt_f);
 }
 template <class R, class S> __device__ __forceinline__ Isl<R> step_dti(const StepArgs<S>& a) {
-  if constexpr (sizeof(R) == sizeof(double)) return a.dt; else return df(a.dt_hi, a.dt_lo);
+  if constexpr (std::is_same<Isl<R>, df>::value) return df(a.dt_hi, a.dt_lo);
+  else if constexpr (std::is_same<Cst<R>, double>::value) return Isl<R>(a.dt);
+  else return Isl<R>(a.dt_hi);
 }
 
 // geometry of column c of the tile
@@ -231,13 +240,13 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
     if (!(f & F_NWFA) || !(f & F_NIFA)) {
       // heights for the aerosol initial profiles (init_*_friendly_aerosols,
       // aerosols:14-73): hgt(1) = 0, and level 1 takes hgt(2)
-      I* hgt = reinterpret_cast<I*>(a.sd) + (long)SD_HGT * nz * a.ncol_pad + s;
+      Cst<R>* hgt = reinterpret_cast<Cst<R>*>(a.hgt) + s;
       I h = I(0.0);
       for (int k = 1; k < nz; k++) {
         h = h + ldi<I>(a.dz + g.base + (long)k * a.NI);
-        hgt[(long)k * a.ncol_pad] = h;
+        hgt[(long)k * a.ncol_pad] = Cst<R>(h);
       }
-      hgt[0] = (nz > 1) ? ldi<I>(a.dz + g.base + a.NI) : I(0.0);
+      hgt[0] = (nz > 1) ? Cst<R>(ldi<I>(a.dz + g.base + a.NI)) : Cst<R>(0.0);
     }
     return;
   }
@@ -402,7 +411,7 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
     nwfa_in = R(a.nwfa[e]);
     nifa_in = R(a.nifa[e]);
   } else {
-    const R hk = R(sd[SD_HGT * fsd + o]);
+    const R hk = R(reinterpret_cast<const Cst<R>*>(a.hgt)[o]);
     nwfa_in = has_nwfa ? R(a.nwfa[e]) : R(naccn1) + R(naccn0) * Exp(-(hk / R(1000.0)) * R(a.niccn3));
     nifa_in = has_nifa ? R(a.nifa[e]) : R(nain1) + R(nain0) * Exp(-(hk / R(1000.0)) * R(a.niin3));
   }
@@ -442,7 +451,7 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   }
 
   // fall-speed candidates (main:1770-1977), unfilled; < 0 marks "absent"
-  const TempoConsts<R>& cc = cst;
+  const TempoConsts<Cst<R>>& cc = cst;
   R vtr = R(-1), vtnr = R(-1), vtg = R(-1), vtng = R(-1), vsa = R(-1), vsb = R(0);
   R vti = R(-1), vtni = R(-1), vtc = R(0), vtnc = R(0);
   if (L.rr > R(r1)) {
@@ -638,7 +647,7 @@ __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant_
     const R* vt = sr + fv * fsd;
     const I osteps = 1.0 / I(steps);
     const I lim = I(limit);
-    if constexpr (!std::is_same<I, double>::value) {
+    if constexpr (std::is_same<I, df>::value) {
       // mixed form: the same fluxes and order, with the per-level factors 1/dz and
       // 1/(dz rho) precomputed in the points kernel
       const I* odz = sd + SD_ODZ * fsd;
@@ -762,7 +771,6 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
   const I dti = step_dti<R>(a);
   const R ncsave = ncsave_of<R>(a, g);
   const long cs = a.ncol_pad, fsd = (long)nz * cs, o = (long)k * cs + s;
-  const I* sd = reinterpret_cast<const I*>(a.sd);
 
   Lev<R> L;
   L.cs = &cst;
@@ -770,9 +778,9 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
   L.t1d = (f & F_USE_T) ? io.template in<I>(a.t[e], C_T1D)
                         : io.template in<I>(a.th[e], C_T1D) * ldi<I>(a.pii + e);
   L.pres = R(a.p[e]);
-  L.tten = io.template in<I>(sd[SD_TTEN * fsd + o], C_TTEN);
-  L.qv = io.template in<I>(sd[SD_QV * fsd + o], C_QV);
-  L.rho = io.template in<I>(sd[SD_RHO * fsd + o], C_RHO);
+  L.tten = io.template sdin<I, I>(SD_TTEN * fsd + o, C_TTEN);
+  L.qv = io.template sdin<I, I>(SD_QV * fsd + o, C_QV);
+  L.rho = io.template sdin<I, I>(SD_RHO * fsd + o, C_RHO);
   L.temp = L.t1d + L.tten * dti;
   const R ocp = R(1.0) / (R(cp) * (R(1.0) + R(0.887) * R(L.qv)));
   const R lvap = R(lvap0) + (R(2106.0) - R(4218.0)) * R(L.temp - t0);
@@ -786,16 +794,16 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
   L.qg1d = io.template in<R>(a.qg[e], C_QG);
   L.ng1d = hail ? io.template in<R>(a.ng[e], C_NG) : R(0);
   L.qb1d = hail ? io.template in<R>(a.qb[e], C_QB) : R(0);
-  L.qrten = R(sd[SD_TQR * fsd + o]);
-  L.nrten = R(sd[SD_TNR * fsd + o]);
-  L.qgten = R(sd[SD_TQG * fsd + o]);
-  L.ngten = R(sd[SD_TNG * fsd + o]);
-  L.qbten = R(sd[SD_TQB * fsd + o]);
-  L.qsten = R(sd[SD_TQS * fsd + o]);
-  L.qiten = R(sd[SD_TQI * fsd + o]);
-  L.niten = R(sd[SD_TNI * fsd + o]);
-  L.qcten = R(sd[SD_TQC * fsd + o]);
-  L.ncten = R(sd[SD_TNC * fsd + o]);
+  L.qrten = io.template sdin<R, I>(SD_TQR * fsd + o, C_TQR);
+  L.nrten = io.template sdin<R, I>(SD_TNR * fsd + o, C_TNR);
+  L.qgten = io.template sdin<R, I>(SD_TQG * fsd + o, C_TQG);
+  L.ngten = io.template sdin<R, I>(SD_TNG * fsd + o, C_TNG);
+  L.qbten = io.template sdin<R, I>(SD_TQB * fsd + o, C_TQB);
+  L.qsten = io.template sdin<R, I>(SD_TQS * fsd + o, C_TQS);
+  L.qiten = io.template sdin<R, I>(SD_TQI * fsd + o, C_TQI);
+  L.niten = io.template sdin<R, I>(SD_TNI * fsd + o, C_TNI);
+  L.qcten = io.template sdin<R, I>(SD_TQC * fsd + o, C_TQC);
+  L.ncten = io.template sdin<R, I>(SD_TNC * fsd + o, C_TNC);
   L.smob = L.smoc = L.smo2 = L.smoz = R(0);
   if (!(f & F_NOMICRO)) {  // freeze_cloud_melt_ice (main:2124-2165)
     R xri = Max(R(0.0), L.qi1d + L.qiten * dt);
@@ -865,9 +873,9 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
   }
   if (k != 0) return;
   // column diagnostics on the lowest level (main:785-794; driver:452-484)
-  const I* sc = reinterpret_cast<const I*>(a.sc) + s;
-  const I prec_r = sc[SC_PR * cs], prec_g = sc[SC_PG * cs], prec_s = sc[SC_PS * cs],
-          prec_i = sc[SC_PI * cs], prec_c = sc[SC_PC * cs];
+  const I prec_r = io.template scin<I>(SC_PR * cs + s), prec_g = io.template scin<I>(SC_PG * cs + s),
+          prec_s = io.template scin<I>(SC_PS * cs + s), prec_i = io.template scin<I>(SC_PI * cs + s),
+          prec_c = io.template scin<I>(SC_PC * cs + s);
   const I ffrac = (prec_i + prec_s + prec_g) / (prec_i + prec_s + prec_g + prec_r + r1);
   const I frz = ((L.temp - t0) < -0.5) ? prec_r + prec_c : I(0.0);
   const long t2 = g.tile2;

@@ -41,14 +41,11 @@ enum : uint32_t {
   F_DT_RIME = 1u << 16  // dt > timestep_conversion_rime_to_rain
 };
 
-// per-point scratch fields in the island type (thermodynamic and sedimentation islands);
-// SD_HGT (height of the level for the aerosol profiles) is written only when nwfa or
-// nifa is absent
+// per-point scratch fields in the island type (thermodynamic and sedimentation islands)
 enum SDField : int {
   SD_TTEN, SD_QV, SD_RHO,
   SD_XRR, SD_XNR, SD_XRG, SD_XNG, SD_XRB, SD_XRS, SD_XRI, SD_XNI, SD_XRC, SD_XNC,
   SD_TQR, SD_TNR, SD_TQG, SD_TNG, SD_TQB, SD_TQS, SD_TQI, SD_TNI, SD_TQC, SD_TNC,
-  SD_HGT,
   SD_ODZ, SD_OZR,  // 1 / dz and 1 / (dz rho) of the level (mixed form: sedimentation factors)
   SD_N
 };
@@ -91,6 +88,8 @@ struct StepArgs {
   void* sd;           // Isl<R>[SD_N][nz][ncol_pad]
   void* sr;           // R[SR_N][nz][ncol_pad]
   void* sc;           // Isl<R>[SC_N][ncol_pad]
+  void* hgt;          // Cst<R>[nz][ncol_pad]: level heights for the aerosol initial profiles
+                      // (written only when nwfa or nifa is absent)
   int* act;           // [ncol_pad] column of each active slot
   unsigned int* nact; // active-slot counter (zero before prep)
   uint8_t* pmask;     // [nz][ncol_pad]
