@@ -81,6 +81,16 @@ typedef enum {
 
 typedef struct tempo_ctx tempo_ctx_t;
 
+/* Device pointers to one state of the column step, in the layout of tempo_run's
+ * arrays; the element type is given by the call (double or float).  NULL = absent
+ * (the optional arguments of tempo_run). */
+typedef struct {
+  void *t, *th;
+  const void *pii, *p, *w, *dz;
+  void *qv, *qc, *qr, *qi, *qs, *qg, *ni, *nr, *nc, *nwfa, *nifa, *ng, *qb;
+  const int *land_input;
+} tempo_state_t;
+
 /* Library identification; never fails. */
 const char *tempo_version(void);
 /* Thread-local message of the last failing call ("" if none). */
@@ -210,6 +220,31 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, f
                              int jme, int kms, int kme, int its, int ite, int jts, int jte,
                              int kts, int kte, tempo_diags_t *tempo_diags, void *stream,
                              int reps, float *times_ms, int count, int *chosen);
+/* No reference counterpart.  Tangent-linear step on device arrays: x is advanced by one
+ * step exactly as tempo_run_dev_c does (fp64 != 0: the FP64 step on doubles; else the
+ * all-FP32 step on floats), and dx, the tangent of the differentiated inputs (t or th,
+ * qv, qc, nc, qr, nr, qi, ni, qs, qg and, hail-aware, ng and qb; NULL entries = zero),
+ * is replaced by the tangent of the outputs.  ddiags receives the tangents of the
+ * requested diagnostics.  Branches, clips and table bins are those of the trajectory
+ * from x.  Returns after the step has finished. */
+int tempo_tl_dev_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double dt, int itimestep,
+                   int fp64, tempo_state_t *x, tempo_state_t *dx, tempo_diags_t *tempo_diags,
+                   tempo_diags_t *tangent_diags, int ims, int ime, int jms, int jme, int kms,
+                   int kme, int its, int ite, int jts, int jte, int kts, int kte, void *stream);
+
+/* No reference counterpart.  Adjoint step on device arrays: x is the state before the
+ * step (not modified); lam holds on entry the adjoints of the step's outputs (same
+ * fields as dx of tempo_tl_dev_c; NULL entries = zero) and on return the adjoints of
+ * its inputs; lam_diags (optional) gives the adjoints of the surface precipitation
+ * (rain, ice, snow, graupel) and of refl10cm (dBZ).  Needs device memory for the
+ * recomputed trajectory and checkpoints (about 10x the state).  Returns after the
+ * adjoint has finished. */
+int tempo_adjoint_dev_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double dt,
+                        int itimestep, int fp64, const tempo_state_t *x, tempo_state_t *lam,
+                        const tempo_diags_t *lam_diags, int ims, int ime, int jms, int jme,
+                        int kms, int kme, int its, int ite, int jts, int jte, int kts, int kte,
+                        void *stream);
+
 /* No reference counterpart.  Selects the per-level kernel variant directly (0..7). */
 int tempo_set_points_variant(tempo_ctx_t *ctx, int variant);
 

@@ -30,6 +30,8 @@ UNITS = [
     ("tempo_points_f32.cu", ["-DTEMPO_VARIANT_SET=0"], "tempo_points_f32_lo"),
     ("tempo_points_f32.cu", ["-DTEMPO_VARIANT_SET=1"], "tempo_points_f32_hi"),
     ("tempo_tables.cu", ["-fmad=false"], "tempo_tables"),
+    ("tempo_deriv_f64.cu", ["-fmad=false"], "tempo_deriv_f64"),
+    ("tempo_deriv_f32.cu", [], "tempo_deriv_f32"),
 ]
 HOST_UNITS = ["tempo_capi.cpp", "tempo_host_init.cpp"]
 

@@ -358,9 +358,10 @@ struct RunArrays {
 };
 
 // Validates the argument list and launches the step on device arrays.
+// Validates a run's arguments and fills the step arguments (everything but scratch).
 template <class S>
-int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, const RunArrays<S>& A,
-            const Bounds& b, const tempo_diags_t* dg, cudaStream_t s) {
+int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, const RunArrays<S>& A,
+               const Bounds& b, const tempo_diags_t* dg, StepArgs<S>& a) {
   if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
   if (!cfg) return fail(TEMPO_ERR_ARG, "NULL tempo_cfgs");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(TEMPO_ERR_ARG, "dt must be > 0 (got %g)", dt);
@@ -394,7 +395,7 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   if (A.t) f |= F_USE_T;
   if (dt > timestep_conversion_rime_to_rain) f |= F_DT_RIME;
 
-  StepArgs<S> a{};
+  a = StepArgs<S>{};
   a.t = A.t;
   a.th = A.th;
   a.pii = A.pii;
@@ -455,6 +456,14 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   // aerosols:14-73; h_01 = 0.8 km), host libm as in the reference
   a.niccn3 = -1.0 * std::log(naccn1 / naccn0) / 0.8;
   a.niin3 = -1.0 * std::log(nain1 / nain0) / 0.8;
+  return TEMPO_OK;
+}
+
+template <class S>
+int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, const RunArrays<S>& A,
+            const Bounds& b, const tempo_diags_t* dg, cudaStream_t s) {
+  StepArgs<S> a;
+  if (int rc = build_args(c, cfg, dt, itimestep, A, b, dg, a)) return rc;
   const bool mixed = c->precision == TEMPO_PREC_MIXED;
   // scratch: island-type point fields (double or double-float, 8 bytes either way),
   // bulk-type fall speeds, per-slot sums, slot map, masks and the slot counter
@@ -897,6 +906,289 @@ int tempo_set_points_variant(tempo_ctx_t* c, int variant) {
   if (variant < 0 || variant >= kPointsVariants) return fail(TEMPO_ERR_ARG, "variant %d outside [0, %d)", variant, kPointsVariants);
   c->points_variant = variant;
   return TEMPO_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// device buffers released when the scope ends (after a stream synchronisation)
+struct DevBufs {
+  std::vector<void*> p;
+  ~DevBufs() {
+    for (void* q : p) cudaFree(q);
+  }
+  template <class X>
+  X* alloc(size_t n) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, (n ? n : 1) * sizeof(X)) != cudaSuccess) return nullptr;
+    p.push_back(q);
+    return (X*)q;
+  }
+};
+
+template <class T>
+RunArrays<T> arrays_of(const tempo_state_t* x) {
+  return RunArrays<T>{(T*)x->t,  (T*)x->th, (const T*)x->pii, (const T*)x->p, (const T*)x->w,
+                      (const T*)x->dz, (T*)x->qv, (T*)x->qc, (T*)x->qr, (T*)x->qi, (T*)x->qs,
+                      (T*)x->qg, (T*)x->ni, (T*)x->nr, (T*)x->nc, (T*)x->nwfa, (T*)x->nifa,
+                      (T*)x->ng, (T*)x->qb, x->land_input};
+}
+
+// scalar fields of the step arguments (all but pointers)
+template <class A, class B>
+void copy_scalars(A& d, const B& s) {
+  d.NI = s.NI; d.NK = s.NK; d.i0 = s.i0; d.k0 = s.k0; d.j0 = s.j0; d.ti = s.ti; d.tj = s.tj;
+  d.nz = s.nz; d.ncol = s.ncol; d.ncol_pad = s.ncol_pad; d.dt = s.dt; d.odt = s.odt;
+  d.dt_hi = s.dt_hi; d.dt_lo = s.dt_lo; d.odt_f = s.odt_f; d.nc_single = s.nc_single;
+  d.niccn3 = s.niccn3; d.niin3 = s.niin3; d.flags = s.flags; d.land = s.land;
+}
+
+template <class T> const TempoConsts<T>& consts_of(const tempo_ctx* c);
+template <> const TempoConsts<double>& consts_of<double>(const tempo_ctx* c) { return c->c64; }
+template <> const TempoConsts<float>& consts_of<float>(const tempo_ctx* c) { return c->c32; }
+template <class T> Tables<T> tables_of(const tempo_ctx* c);
+template <> Tables<double> tables_of<double>(const tempo_ctx* c) {
+  return Tables<double>{c->t64.t_efrw, c->t64.t_efsw, c->t64.tnc_wev, c->t64.tps_iaus, c->t64.tni_iaus,
+                        c->t64.tpi_ide, c->t64.tnccn, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
+}
+template <> Tables<float> tables_of<float>(const tempo_ctx* c) {
+  return Tables<float>{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
+                       c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
+}
+
+// Packed (value, tangent) copies of a state and the step's scratch for Dual<T, 1>.
+template <class T>
+struct DualStep {
+  using D1 = Dual<T, 1>;
+  StepArgs<D1> a{};
+  D1* f[19] = {};  // t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb
+  D1* dg[15] = {};
+  size_t ext = 0, n2 = 0, n3 = 0;
+
+  int setup(tempo_ctx* c, const StepArgs<T>& ap, const Bounds& b, const RunArrays<T>& X,
+            const RunArrays<T>* dX, DevBufs& B, cudaStream_t s) {
+    copy_scalars(a, ap);
+    ext = (size_t)(b.ime - b.ims + 1) * (b.kme - b.kms + 1) * (b.jme - b.jms + 1);
+    n2 = (size_t)ap.ti * ap.tj;
+    n3 = n2 * ap.nz;
+    const T* xs[19] = {X.t, X.th, X.pii, X.p, X.w, X.dz, X.qv, X.qc, X.qr, X.qi, X.qs, X.qg,
+                       X.ni, X.nr, X.nc, X.nwfa, X.nifa, X.ng, X.qb};
+    const T* ds[19] = {};
+    if (dX) {
+      const T* d2[19] = {dX->t, dX->th, nullptr, nullptr, nullptr, nullptr, dX->qv, dX->qc,
+                         dX->qr, dX->qi, dX->qs, dX->qg, dX->ni, dX->nr, dX->nc, nullptr,
+                         nullptr, dX->ng, dX->qb};
+      for (int i = 0; i < 19; i++) ds[i] = d2[i];
+    }
+    for (int i = 0; i < 19; i++) {
+      if (!xs[i]) continue;
+      if (!(f[i] = B.alloc<D1>(ext))) return fail(TEMPO_ERR_NOMEM, "derivative step: state copy");
+      if (DerivOps<T>::pack(f[i], xs[i], ds[i], (long)ext, s) != cudaSuccess)
+        return fail(TEMPO_ERR_CUDA, "derivative step: pack");
+    }
+    a.t = f[0]; a.th = f[1]; a.pii = f[2]; a.p = f[3]; a.w = f[4]; a.dz = f[5]; a.qv = f[6];
+    a.qc = f[7]; a.qr = f[8]; a.qi = f[9]; a.qs = f[10]; a.qg = f[11]; a.ni = f[12]; a.nr = f[13];
+    a.nc = f[14]; a.nwfa = f[15]; a.nifa = f[16]; a.ng = f[17]; a.qb = f[18];
+    T* const* dp = (T* const*)&ap.rain_precip;  // the 15 diagnostic pointers, in order
+    D1** dd = (D1**)&a.rain_precip;
+    for (int i = 0; i < 15; i++) {
+      if (!dp[i]) continue;
+      if (!(dg[i] = B.alloc<D1>(i < 8 ? n2 : n3))) return fail(TEMPO_ERR_NOMEM, "derivative step: diagnostics");
+      if (DerivOps<T>::pack(dg[i], nullptr, nullptr, (long)(i < 8 ? n2 : n3), s) != cudaSuccess)
+        return fail(TEMPO_ERR_CUDA, "derivative step: pack");
+      dd[i] = dg[i];
+    }
+    const size_t npad = (size_t)a.ncol_pad, nzs = (size_t)a.nz;
+    if (!(a.sd = B.alloc<D1>((size_t)SD_N * nzs * npad)) || !(a.sr = B.alloc<D1>((size_t)SR_N * nzs * npad)) ||
+        !(a.sc = B.alloc<D1>((size_t)SC_N * npad)) || !(a.act = B.alloc<int>(npad)) ||
+        !(a.pmask = B.alloc<uint8_t>(nzs * npad)) || !(a.cmask = B.alloc<uint8_t>(npad)) ||
+        !(a.hgt = B.alloc<T>(nzs * npad)) || !(a.nact = B.alloc<unsigned>(1)))
+      return fail(TEMPO_ERR_NOMEM, "derivative step: scratch");
+    a.stats = c->d_stats;
+    if (cudaMemsetAsync(a.nact, 0, sizeof(unsigned), s) != cudaSuccess ||
+        cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s) != cudaSuccess)
+      return fail(TEMPO_ERR_CUDA, "derivative step: counters");
+    return TEMPO_OK;
+  }
+};
+
+template <class T>
+int tl_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, tempo_state_t* x,
+           tempo_state_t* dx, tempo_diags_t* dgs, tempo_diags_t* ddg, const Bounds& b, cudaStream_t s) {
+  if (!x) return fail(TEMPO_ERR_ARG, "NULL state");
+  const RunArrays<T> X = arrays_of<T>(x);
+  StepArgs<T> ap;
+  if (int rc = build_args(c, cfg, dt, itimestep, X, b, dgs, ap)) return rc;
+  if (cfg->max_hail_diameter_flag) ap.mhd_sfc = ap.mhd_col = nullptr;  // not differentiable
+  CUDA_TRY(cudaSetDevice(c->device));
+  DevBufs B;
+  DualStep<T> st;
+  const RunArrays<T> DX = dx ? arrays_of<T>(dx) : RunArrays<T>{};
+  if (int rc = st.setup(c, ap, b, X, dx ? &DX : nullptr, B, s)) return rc;
+  IslandConsts<Dual<T, 1>> ci;
+  make_island_consts(c->c64, &ci);
+  CUDA_TRY(DerivOps<T>::tl_step(st.a, tables_of<T>(c), consts_of<T>(c), ci, s, 0));
+  T* xs[19] = {X.t, X.th, nullptr, nullptr, nullptr, nullptr, X.qv, X.qc, X.qr, X.qi, X.qs, X.qg,
+               X.ni, X.nr, X.nc, X.nwfa, X.nifa, X.ng, X.qb};
+  T* ds[19] = {};
+  if (dx) {
+    T* d2[19] = {DX.t, DX.th, nullptr, nullptr, nullptr, nullptr, DX.qv, DX.qc, DX.qr, DX.qi, DX.qs,
+                 DX.qg, DX.ni, DX.nr, DX.nc, nullptr, nullptr, DX.ng, DX.qb};
+    for (int i = 0; i < 19; i++) ds[i] = d2[i];
+  }
+  for (int i = 0; i < 19; i++)
+    if (st.f[i] && (xs[i] || ds[i])) CUDA_TRY(DerivOps<T>::unpack(xs[i], ds[i], st.f[i], (long)st.ext, s));
+  T* const* dp = (T* const*)&ap.rain_precip;
+  T* const* tp = ddg ? (T* const*)ddg : nullptr;
+  for (int i = 0; i < 15; i++)
+    if (st.dg[i]) CUDA_TRY(DerivOps<T>::unpack(dp[i], tp ? tp[i] : nullptr, st.dg[i],
+                                               (long)(i < 8 ? st.n2 : st.n3), s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  c->last_cols = ap.ncol;
+  c->launches = kStepLaunches;
+  return TEMPO_OK;
+}
+
+template <class T>
+int adjoint_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, const tempo_state_t* x,
+                tempo_state_t* lam, const tempo_diags_t* ldg, const Bounds& b, cudaStream_t s) {
+  if (!x || !lam) return fail(TEMPO_ERR_ARG, "NULL state or adjoint");
+  const RunArrays<T> X = arrays_of<T>(x);
+  StepArgs<T> ap;
+  if (int rc = build_args(c, cfg, dt, itimestep, X, b, nullptr, ap)) return rc;
+  CUDA_TRY(cudaSetDevice(c->device));
+  DevBufs B;
+  using D1 = Dual<T, 1>;
+  // 1. forward trajectory on packed copies (zero tangents): prep and phase A
+  DualStep<T> st;
+  if (int rc = st.setup(c, ap, b, X, nullptr, B, s)) return rc;
+  IslandConsts<Dual<T, 1>> ci1;
+  make_island_consts(c->c64, &ci1);
+  const Tables<T> TT = tables_of<T>(c);
+  const TempoConsts<T>& cst = consts_of<T>(c);
+  CUDA_TRY(DerivOps<T>::tl_step(st.a, TT, cst, ci1, s, 1));
+  // 2. snapshots: scratch before sedimentation, state after phase A (plain values)
+  const size_t npad = (size_t)ap.ncol_pad, nzs = (size_t)ap.nz;
+  const size_t nsd = (size_t)SD_N * nzs * npad, nsr = (size_t)SR_N * nzs * npad;
+  D1* sd_pre = B.alloc<D1>(nsd);
+  D1* sr_pre = B.alloc<D1>(nsr);
+  if (!sd_pre || !sr_pre) return fail(TEMPO_ERR_NOMEM, "adjoint: scratch snapshot");
+  CUDA_TRY(cudaMemcpyAsync(sd_pre, st.a.sd, nsd * sizeof(D1), cudaMemcpyDeviceToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(sr_pre, st.a.sr, nsr * sizeof(D1), cudaMemcpyDeviceToDevice, s));
+  StepArgs<T> aC = ap;  // phase C reads the state after phase A
+  {
+    const int idx[11] = {6, 7, 8, 9, 10, 11, 12, 13, 14, 17, 18};  // qv qc qr qi qs qg ni nr nc ng qb
+    T** dst[11] = {&aC.qv, &aC.qc, &aC.qr, &aC.qi, &aC.qs, &aC.qg, &aC.ni, &aC.nr, &aC.nc, &aC.ng, &aC.qb};
+    for (int i = 0; i < 11; i++) {
+      if (!st.f[idx[i]]) {
+        *dst[i] = nullptr;
+        continue;
+      }
+      T* q = B.alloc<T>(st.ext);
+      if (!q) return fail(TEMPO_ERR_NOMEM, "adjoint: state snapshot");
+      CUDA_TRY(DerivOps<T>::unpack(q, nullptr, st.f[idx[i]], (long)st.ext, s));
+      *dst[i] = q;
+    }
+  }
+  // 3. sedimentation of the trajectory; its substep counts size the checkpoints
+  CUDA_TRY(DerivOps<T>::tl_step(st.a, TT, cst, ci1, s, 2));
+  unsigned long long sub[8];
+  CUDA_TRY(cudaMemcpyAsync(sub, c->d_stats, sizeof sub, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  unsigned long long smax = 1;
+  for (int i = 1; i <= 5; i++) smax = std::max(smax, sub[i]);
+  SedWork W;
+  W.nck = (int)((smax + 3) / 4);
+  W.rows = SedWork::rows_for(W.nck, (int)nzs);
+  // 4. adjoint storage
+  T* lam_sd = B.alloc<T>(nsd);
+  T* lam_sr = B.alloc<T>(nsr);
+  T* work = B.alloc<T>((size_t)W.rows * npad);
+  uint8_t* colflag = B.alloc<uint8_t>((size_t)ap.ncol);
+  if (!lam_sd || !lam_sr || !work || !colflag) return fail(TEMPO_ERR_NOMEM, "adjoint: workspace");
+  CUDA_TRY(cudaMemsetAsync(lam_sd, 0, nsd * sizeof(T), s));
+  CUDA_TRY(cudaMemsetAsync(lam_sr, 0, nsr * sizeof(T), s));
+  AdjArgs<T> j{};
+  const RunArrays<T> L = arrays_of<T>(lam);
+  j.lam[A_T] = L.t;
+  j.lam_th = L.th;
+  j.lam[A_QV] = L.qv;
+  j.lam[A_QC] = L.qc;
+  j.lam[A_NC] = L.nc;
+  j.lam[A_QR] = L.qr;
+  j.lam[A_NR] = L.nr;
+  j.lam[A_QI] = L.qi;
+  j.lam[A_NI] = L.ni;
+  j.lam[A_QS] = L.qs;
+  j.lam[A_QG] = L.qg;
+  j.lam[A_NG] = L.ng;
+  j.lam[A_QB] = L.qb;
+  if (ldg) {
+    j.lam_refl = (T*)ldg->refl10cm;
+    j.lam_precip[0] = (T*)ldg->rain_precip;
+    j.lam_precip[1] = (T*)ldg->ice_liquid_equiv_precip;
+    j.lam_precip[2] = (T*)ldg->snow_liquid_equiv_precip;
+    j.lam_precip[3] = (T*)ldg->graupel_liquid_equiv_precip;
+  }
+  j.lam_sd = lam_sd;
+  j.lam_sr = lam_sr;
+  j.colflag = colflag;
+  // shared step bookkeeping of the trajectory
+  for (StepArgs<T>* q : {&aC, &ap}) {
+    q->act = st.a.act;
+    q->nact = st.a.nact;
+    q->pmask = st.a.pmask;
+    q->cmask = st.a.cmask;
+    q->hgt = st.a.hgt;
+    q->stats = c->d_stats;
+    q->sd = q->sr = q->sc = nullptr;
+  }
+  // the reflectivity's adjoint is read where phase C produces it
+  aC.refl10cm = (cfg->refl10cm_flag && j.lam_refl) ? j.lam_refl : nullptr;
+  // 5. reverse: phase C, sedimentation, phase A, early-exit columns
+  j.psd = (const D1*)st.a.sd;
+  j.psc = (const D1*)st.a.sc;
+  IslandConsts<Dual<T, C_N>> ciC;
+  make_island_consts(c->c64, &ciC);
+  CUDA_TRY(DerivOps<T>::adj_final(aC, cst, ciC, j, s));
+  j.psd = sd_pre;
+  j.psr = sr_pre;
+  CUDA_TRY(DerivOps<T>::adj_sedim(aC, j, work, W, s));
+  IslandConsts<Dual<T, IN_N>> ciA;
+  make_island_consts(c->c64, &ciA);
+  CUDA_TRY(DerivOps<T>::adj_points(ap, TT, cst, ciA, j, s));
+  CUDA_TRY(DerivOps<T>::colflag(colflag, st.a.act, st.a.nact, ap.ncol, s));
+  CUDA_TRY(DerivOps<T>::adj_early(ap, cst, ciA, j, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  c->last_cols = ap.ncol;
+  return TEMPO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tempo_tl_dev_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, double dt, int itimestep, int fp64,
+                   tempo_state_t* x, tempo_state_t* dx, tempo_diags_t* diags, tempo_diags_t* tdiags,
+                   int ims, int ime, int jms, int jme, int kms, int kme, int its, int ite, int jts,
+                   int jte, int kts, int kte, void* stream) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  const Bounds b{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte};
+  cudaStream_t s = (cudaStream_t)stream;
+  return fp64 ? tl_dev<double>(c, cfg, dt, itimestep, x, dx, diags, tdiags, b, s)
+              : tl_dev<float>(c, cfg, dt, itimestep, x, dx, diags, tdiags, b, s);
+}
+
+int tempo_adjoint_dev_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, double dt, int itimestep, int fp64,
+                        const tempo_state_t* x, tempo_state_t* lam, const tempo_diags_t* lam_diags,
+                        int ims, int ime, int jms, int jme, int kms, int kme, int its, int ite,
+                        int jts, int jte, int kts, int kte, void* stream) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  const Bounds b{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte};
+  cudaStream_t s = (cudaStream_t)stream;
+  return fp64 ? adjoint_dev<double>(c, cfg, dt, itimestep, x, lam, lam_diags, b, s)
+              : adjoint_dev<float>(c, cfg, dt, itimestep, x, lam, lam_diags, b, s);
 }
 
 int tempo_aerosol_surface_emissions_dev_c(tempo_ctx_t* c, double dt, double* nwfa,

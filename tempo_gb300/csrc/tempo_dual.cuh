@@ -14,6 +14,12 @@
 
 #include <type_traits>
 
+#if defined(__CUDACC__)
+#define TG_UNROLL _Pragma("unroll")
+#else
+#define TG_UNROLL
+#endif
+
 namespace tg {
 
 template <class T, int N>
@@ -22,7 +28,7 @@ struct Dual {
   T d[N];
   Dual() = default;
   __host__ __device__ Dual(T x) : v(x) {
-#pragma unroll
+TG_UNROLL
     for (int i = 0; i < N; i++) d[i] = T(0);
   }
   template <class U, class = typename std::enable_if<std::is_arithmetic<U>::value &&
@@ -44,28 +50,28 @@ template <class T, int N> struct IsDual<Dual<T, N>> : std::true_type {};
 TG_DUAL_T __host__ __device__ __forceinline__ TG_D operator-(const TG_D& a) {
   TG_D r;
   r.v = -a.v;
-#pragma unroll
+TG_UNROLL
   for (int i = 0; i < N; i++) r.d[i] = -a.d[i];
   return r;
 }
 TG_DUAL_T __host__ __device__ __forceinline__ TG_D operator+(const TG_D& a, const TG_D& b) {
   TG_D r;
   r.v = a.v + b.v;
-#pragma unroll
+TG_UNROLL
   for (int i = 0; i < N; i++) r.d[i] = a.d[i] + b.d[i];
   return r;
 }
 TG_DUAL_T __host__ __device__ __forceinline__ TG_D operator-(const TG_D& a, const TG_D& b) {
   TG_D r;
   r.v = a.v - b.v;
-#pragma unroll
+TG_UNROLL
   for (int i = 0; i < N; i++) r.d[i] = a.d[i] - b.d[i];
   return r;
 }
 TG_DUAL_T __host__ __device__ __forceinline__ TG_D operator*(const TG_D& a, const TG_D& b) {
   TG_D r;
   r.v = a.v * b.v;
-#pragma unroll
+TG_UNROLL
   for (int i = 0; i < N; i++) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
   return r;
 }
@@ -73,7 +79,7 @@ TG_DUAL_T __host__ __device__ __forceinline__ TG_D operator/(const TG_D& a, cons
   TG_D r;
   r.v = a.v / b.v;
   const T ib = T(1) / b.v;
-#pragma unroll
+TG_UNROLL
   for (int i = 0; i < N; i++) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
   return r;
 }
@@ -102,21 +108,21 @@ TG_DUAL_ARITH __host__ __device__ __forceinline__ TG_D operator-(U a, const TG_D
 TG_DUAL_ARITH __host__ __device__ __forceinline__ TG_D operator*(const TG_D& a, U b) {
   TG_D r;
   r.v = a.v * T(b);
-#pragma unroll
+TG_UNROLL
   for (int i = 0; i < N; i++) r.d[i] = a.d[i] * T(b);
   return r;
 }
 TG_DUAL_ARITH __host__ __device__ __forceinline__ TG_D operator*(U a, const TG_D& b) {
   TG_D r;
   r.v = T(a) * b.v;
-#pragma unroll
+TG_UNROLL
   for (int i = 0; i < N; i++) r.d[i] = T(a) * b.d[i];
   return r;
 }
 TG_DUAL_ARITH __host__ __device__ __forceinline__ TG_D operator/(const TG_D& a, U b) {
   TG_D r;
   r.v = a.v / T(b);
-#pragma unroll
+TG_UNROLL
   for (int i = 0; i < N; i++) r.d[i] = a.d[i] / T(b);
   return r;
 }
@@ -124,7 +130,7 @@ TG_DUAL_ARITH __host__ __device__ __forceinline__ TG_D operator/(U a, const TG_D
   TG_D r;
   r.v = T(a) / b.v;
   const T g = -r.v / b.v;
-#pragma unroll
+TG_UNROLL
   for (int i = 0; i < N; i++) r.d[i] = g * b.d[i];
   return r;
 }
@@ -160,7 +166,7 @@ TG_DUAL_CMP(!=)
 TG_DUAL_T __host__ __device__ __forceinline__ TG_D dual_chain(const TG_D& a, T fv, T dfda) {
   TG_D r;
   r.v = fv;
-#pragma unroll
+TG_UNROLL
   for (int i = 0; i < N; i++) r.d[i] = dfda * a.d[i];
   return r;
 }

@@ -7,6 +7,8 @@
 
 #include "tempo_consts.h"
 #include "tempo_dfloat.cuh"
+#include "tempo_dual.cuh"
+#include "tempo_types.h"
 
 namespace tg {
 
@@ -37,6 +39,26 @@ cudaError_t launch_points_mixed_f32_lo(int v, const StepArgs<float>& a, const Ta
 cudaError_t launch_points_mixed_f32_hi(int v, const StepArgs<float>& a, const Tables<float>& t,
                                        const TempoConsts<float>& c, const IslandConsts<df>& ci,
                                        cudaStream_t s);
+// tempo_deriv_f64.cu / tempo_deriv_f32.cu: tangent-linear and adjoint launches of the
+// step on element type T (tempo_deriv.cuh)
+template <class T>
+struct DerivOps {
+  static cudaError_t pack(Dual<T, 1>* dst, const T* v, const T* d, long n, cudaStream_t s);
+  static cudaError_t unpack(T* v, T* d, const Dual<T, 1>* src, long n, cudaStream_t s);
+  static cudaError_t tl_step(const StepArgs<Dual<T, 1>>& a, const Tables<T>& t, const TempoConsts<T>& c,
+                             const IslandConsts<Dual<T, 1>>& ci, cudaStream_t s, int part);
+  static cudaError_t colflag(uint8_t* flag, const int* act, const unsigned* nact, long ncol,
+                             cudaStream_t s);
+  static cudaError_t adj_final(const StepArgs<T>& a, const TempoConsts<T>& c,
+                               const IslandConsts<Dual<T, C_N>>& ci, const AdjArgs<T>& j, cudaStream_t s);
+  static cudaError_t adj_sedim(const StepArgs<T>& a, const AdjArgs<T>& j, T* work, const SedWork& W,
+                               cudaStream_t s);
+  static cudaError_t adj_points(const StepArgs<T>& a, const Tables<T>& t, const TempoConsts<T>& c,
+                                const IslandConsts<Dual<T, IN_N>>& ci, const AdjArgs<T>& j, cudaStream_t s);
+  static cudaError_t adj_early(const StepArgs<T>& a, const TempoConsts<T>& c,
+                               const IslandConsts<Dual<T, IN_N>>& ci, const AdjArgs<T>& j, cudaStream_t s);
+};
+
 // number of points-kernel variants of the mixed form on FP32 storage
 constexpr int kPointsVariants = 8;
 // kernels launched per step (prep, points, sedim, final)

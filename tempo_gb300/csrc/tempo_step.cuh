@@ -32,16 +32,6 @@ namespace tg {
 
 template <class I, class S> __device__ __forceinline__ I ldi(const S* p) { return I(*p); }
 
-// Inputs of a point that carry derivatives in the tangent-linear and adjoint kernels
-enum InId : int { IN_T, IN_QV, IN_QC, IN_NC, IN_QR, IN_NR, IN_QI, IN_NI, IN_QS, IN_QG, IN_NG, IN_QB, IN_N };
-// Inputs of a point of phase C (final kernel) that carry derivatives
-enum CInId : int {
-  C_T1D, C_TTEN, C_QV, C_RHO, C_QC, C_NC, C_QR, C_NR, C_QI, C_NI, C_QS, C_QG, C_NG, C_QB,
-  C_TQR, C_TNR, C_TQG, C_TNG, C_TQB, C_TQS, C_TQI, C_TNI, C_TQC, C_TNC, C_N
-};
-// Array outputs of a point
-enum ArrId : int { A_T, A_QV, A_QC, A_NC, A_QR, A_NR, A_QI, A_NI, A_QS, A_QG, A_NG, A_QB, A_NWFA, A_NIFA, A_N };
-
 // Forward I/O policy: a point reads the step's arrays and stores its outputs where the
 // step keeps them.  The derivative kernels substitute policies that seed input
 // directions and contract outputs with their adjoints.

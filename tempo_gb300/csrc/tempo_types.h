@@ -5,6 +5,12 @@
 
 #include <cstdint>
 
+#ifdef __CUDACC__
+#define TG_HD __host__ __device__
+#else
+#define TG_HD
+#endif
+
 namespace tg {
 
 // Device lookup tables.  The large collection/freezing tables are stored
@@ -95,6 +101,51 @@ struct StepArgs {
   uint8_t* pmask;     // [nz][ncol_pad]
   uint8_t* cmask;     // [ncol_pad]
   unsigned long long* stats;  // [0] early exits, [1..5] max substeps
+};
+
+// Inputs of a point that carry derivatives in the tangent-linear and adjoint kernels
+enum InId : int { IN_T, IN_QV, IN_QC, IN_NC, IN_QR, IN_NR, IN_QI, IN_NI, IN_QS, IN_QG, IN_NG, IN_QB, IN_N };
+// Inputs of a point of phase C (final kernel) that carry derivatives
+enum CInId : int {
+  C_T1D, C_TTEN, C_QV, C_RHO, C_QC, C_NC, C_QR, C_NR, C_QI, C_NI, C_QS, C_QG, C_NG, C_QB,
+  C_TQR, C_TNR, C_TQG, C_TNG, C_TQB, C_TQS, C_TQI, C_TNI, C_TQC, C_TNC, C_N
+};
+// Array outputs of a point
+enum ArrId : int { A_T, A_QV, A_QC, A_NC, A_QR, A_NR, A_QI, A_NI, A_QS, A_QG, A_NG, A_QB, A_NWFA, A_NIFA, A_N };
+
+template <class T, int N> struct Dual;
+
+// Adjoint arguments (tempo_adjoint.cuh)
+template <class T>
+struct AdjArgs {
+  T* lam[A_N];              // adjoint per ArrId (A_NWFA / A_NIFA unused), state layout
+  T* lam_th;                // theta mode: adjoint of th
+  T* lam_refl;              // tile 3-D, adjoint of refl10cm (dBZ); NULL = 0
+  T* lam_precip[4];         // tile 2-D: rain, ice, snow, graupel; NULL = 0
+  T* lam_sd;                // [SD_N][nz][ncol_pad]
+  T* lam_sr;                // [SR_N][nz][ncol_pad]
+  const Dual<T, 1>* psd;    // primal scratch (island fields) the phase reads
+  const Dual<T, 1>* psr;    // primal fall-speed candidates (sedimentation adjoint)
+  const Dual<T, 1>* psc;    // primal per-column sums
+  const uint8_t* colflag;   // [ncol]: 1 = active column
+};
+
+// Workspace rows (T, [row][slot]): working state of the 10 sedimenting fields, their
+// filled fall speeds, checkpoints every 4 substeps, the pre-substep states of one block
+// of 4 substeps, and one row of flux adjoints.
+struct SedWork {
+  int nck;      // checkpoints per field
+  long rows;    // rows in total
+  TG_HD long xw(int f, int k, int nz) const { return (long)f * nz + k; }
+  TG_HD long vf(int f, int k, int nz) const { return 10L * nz + (long)f * nz + k; }
+  TG_HD long ck(int f, int c, int k, int nz) const {
+    return 20L * nz + ((long)f * nck + c) * nz + k;
+  }
+  TG_HD long bb(int fi, int n, int k, int nz) const {
+    return 20L * nz + 10L * nck * nz + ((long)fi * 4 + n) * nz + k;
+  }
+  TG_HD long ls(int k, int nz) const { return 20L * nz + 10L * nck * nz + 12L * nz + k; }
+  TG_HD static long rows_for(int nck, int nz) { return (20L + 10L * nck + 13L) * nz; }
 };
 
 }  // namespace tg
