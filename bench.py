@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--ref-columns", type=int, default=131072,
                     help="columns per step of the reference arm's bounded sample")
     return ap.parse_args()
@@ -183,6 +184,65 @@ def mixed_vs_fp64(f32, d32, f64, d64, x0):
         e = (d32["refl10cm"].double() - d64["refl10cm"]).abs()
         out["refl10cm_dbz"] = {"max_abs": float(e.max()),
                                "rms_abs": float(torch.sqrt((e * e).mean()))}
+    return out
+
+
+def adjoint_timing(ctx, tg, W, torch, device, reps=3):
+    """Forward, tangent-linear and adjoint step on the adjoint workload: 65536 columns x
+    65 levels (256 x 256), dt = 60 s, cost J = sum of surface precipitation + 1e-3 x
+    sum of linear reflectivity x dz.  ms per call from CUDA events on the current
+    stream; FP64 (forward = the FP64 step) and FP32 (forward = the mixed-precision
+    production step; the tangent-linear and adjoint steps differentiate the all-FP32
+    step)."""
+    from tempo_gb300.autograd import cost_precip_reflectivity
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    diff = ("t", "qv", "qc", "nc", "qr", "nr", "qi", "ni", "qs", "qg")
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    base = W.config1_torch(seed=7, ni=256, nj=256, nz=65, device=device, dtype=torch.float64)
+    out = {"workload": "65536 columns x 65 levels, dt=60s, J = sum precip + 1e-3 sum Ze dz",
+           "reps": reps}
+    for name, dtype in (("fp64", torch.float64), ("fp32", torch.float32)):
+        f = {k: v.to(dtype) for k, v in base.items()}
+        nj, nk, ni = f["p"].shape
+        dg = {n: torch.zeros((nj, ni), dtype=dtype, device=device) for n in tg.DIAG2[:4]}
+        dg["refl10cm"] = torch.zeros((nj, nk, ni), dtype=dtype, device=device)
+        x = {k: v.clone() for k, v in f.items()}
+        ctx.tl_device(x, {}, 60.0, 1, diags=dg)
+        leaf = {k: v.clone().requires_grad_(True) for k, v in dg.items()}
+        J = cost_precip_reflectivity(leaf, f["dz"])
+        gl = torch.autograd.grad(J, list(leaf.values()))
+        lamd = {k: g.detach().contiguous() for k, g in zip(leaf, gl)}
+        ctx.set_precision(tg.PREC_FP64 if dtype == torch.float64 else tg.PREC_MIXED)
+        xf = {k: v.clone() for k, v in f.items()}
+        fwd_ms = timed(lambda: ctx.run_device(xf, 60.0, 2, diags=dg))
+        xt = {k: v.clone() for k, v in f.items()}
+        dx = {k: 1e-3 * f[k] for k in diff}
+        tl_ms = timed(lambda: ctx.tl_device(xt, dx, 60.0, 2, diags=dg))
+        lam0 = {k: torch.zeros_like(f[k]) for k in diff}
+        lam = {k: v.clone() for k, v in lam0.items()}
+
+        def adj():
+            for k in diff:
+                lam[k].copy_(lam0[k])
+            ctx.adjoint_device(f, lam, 60.0, 1, lam_diags=lamd)
+        ad_ms = timed(adj)
+        out[name] = {"forward_ms": fwd_ms, "tl_ms": tl_ms, "adjoint_ms": ad_ms,
+                     "adjoint_over_forward": ad_ms / fwd_ms,
+                     "grad_norm": float(sum((lam[k].double() ** 2).sum() for k in diff) ** 0.5)}
+        del f, x, xf, xt, dx, lam, lam0, dg, leaf
+        torch.cuda.empty_cache()
+    ctx.set_precision(tg.PREC_MIXED)
     return out
 
 
@@ -338,6 +398,14 @@ def main():
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
     e2e_value = world * ncol / e2e_s
 
+    adjoint = None
+    if not args.no_adjoint:
+        del host, hdiag
+        try:
+            adjoint = adjoint_timing(ctx, tg, W, torch, f"cuda:{local}")
+        except Exception as e:  # reported beside the headline, never required
+            adjoint = {"error": str(e)}
+
     pk = peaks()
     hbm = pk.get("hbm_gbs")
     peak_src = "measured" if hbm else "fallback"
@@ -367,6 +435,7 @@ def main():
                      "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src,
                      "kernel_ms": kms,
                      "kernel_share": {k: v / step_kernel_ms for k, v in kms.items()}},
+        "adjoint": adjoint,
         "gpu_launches": args.steps * stats.get("launches", 1),
         "clocks": clocks,
         "step_stats": stats,

@@ -22,7 +22,7 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["TempoError", "TempoContext", "tempo_init", "tempo_run", "default_cfgs",
+__all__ = ["TempoError", "TempoContext", "tempo_init", "tempo_run", "default_cfgs", "DIFF_FIELDS",
            "PREC_FP64", "PREC_MIXED", "DIAG2", "DIAG3", "load_library", "REPO_TABLES"]
 
 PKG = Path(__file__).resolve().parent
@@ -63,6 +63,26 @@ class TempoCfgs(ctypes.Structure):
         d = {n: bool(getattr(self, n)) for n in CFG_FLAGS + DIAG_FLAGS}
         d["single_moment_nc_opt"] = self.single_moment_nc_opt.decode()
         return d
+
+
+class TempoState(ctypes.Structure):
+    """tempo_state_t: device pointers to one state (include/tempo_gb300.h)."""
+    _fields_ = [(n, ctypes.c_void_p) for n in (
+        "t", "th", "pii", "p", "w", "dz", "qv", "qc", "qr", "qi", "qs", "qg", "ni", "nr", "nc",
+        "nwfa", "nifa", "ng", "qb", "land_input")]
+
+
+# inputs of the step that the tangent-linear and adjoint steps differentiate
+DIFF_FIELDS = ("t", "th", "qv", "qc", "nc", "qr", "nr", "qi", "ni", "qs", "qg", "ng", "qb")
+
+
+def _state_of(fields: dict) -> TempoState:
+    st = TempoState()
+    for n, _ in TempoState._fields_:
+        v = fields.get(n)
+        if v is not None:
+            setattr(st, n, v.data_ptr())
+    return st
 
 
 class TempoDiags(ctypes.Structure):
@@ -119,6 +139,13 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
                                                 ctypes.POINTER(ctypes.c_int)])
     lib.tempo_set_points_variant.argtypes = [_VP, i]
     lib.tempo_set_graphs.argtypes = [_VP, i]
+    lib.tempo_tl_dev_c.argtypes = ([_VP, ctypes.POINTER(TempoCfgs), ctypes.c_double, i, i,
+                                    ctypes.POINTER(TempoState), ctypes.POINTER(TempoState),
+                                    ctypes.POINTER(TempoDiags), ctypes.POINTER(TempoDiags)]
+                                   + [i] * 12 + [_VP])
+    lib.tempo_adjoint_dev_c.argtypes = ([_VP, ctypes.POINTER(TempoCfgs), ctypes.c_double, i, i,
+                                         ctypes.POINTER(TempoState), ctypes.POINTER(TempoState),
+                                         ctypes.POINTER(TempoDiags)] + [i] * 12 + [_VP])
     lib.tempo_kernel_times_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_float)]
     _lib = lib
     return lib
@@ -274,6 +301,52 @@ class TempoContext:
             land.data_ptr() if land is not None else None, *b[6:], ctypes.byref(d),
             ctypes.c_void_p(s.cuda_stream), int(reps), times, 8, ctypes.byref(chosen)))
         return chosen.value, [float(x) for x in times]
+
+    # ---- derivatives ----------------------------------------------------------------
+    def _dev_common(self, fields, bounds, stream):
+        import torch
+        p = fields["p"]
+        nj, nk, ni = p.shape
+        b = list(bounds) if bounds is not None else [1, ni, 1, nj, 1, nk] * 3
+        s = stream if stream is not None else torch.cuda.current_stream(p.device)
+        return b[6:], ctypes.c_void_p(s.cuda_stream), int(p.dtype == torch.float64)
+
+    def tl_device(self, fields: dict, dfields: dict, dt: float, itimestep: int,
+                  diags: Optional[dict] = None, tdiags: Optional[dict] = None, bounds=None,
+                  stream=None, cfgs: Optional[TempoCfgs] = None):
+        """Tangent-linear step (tempo_tl_dev_c) on CUDA tensors: ``fields`` advance one
+        step, ``dfields`` (tangents of DIFF_FIELDS) become the output tangents and
+        ``tdiags`` the tangents of the diagnostics.  float64 tensors: FP64 step;
+        float32: all-FP32 step."""
+        cfg = cfgs if cfgs is not None else self.cfgs
+        bb, sptr, fp64 = self._dev_common(fields, bounds, stream)
+        x, dx = _state_of(fields), _state_of({k: v for k, v in dfields.items() if k in DIFF_FIELDS})
+        d, td = TempoDiags(), TempoDiags()
+        for n in DIAG2 + DIAG3:
+            if diags and diags.get(n) is not None:
+                setattr(d, n, diags[n].data_ptr())
+            if tdiags and tdiags.get(n) is not None:
+                setattr(td, n, tdiags[n].data_ptr())
+        _check(load_library().tempo_tl_dev_c(self._h, ctypes.byref(cfg), float(dt), int(itimestep),
+                                              fp64, ctypes.byref(x), ctypes.byref(dx), ctypes.byref(d),
+                                              ctypes.byref(td), *bb, sptr))
+
+    def adjoint_device(self, fields: dict, lam: dict, dt: float, itimestep: int,
+                       lam_diags: Optional[dict] = None, bounds=None, stream=None,
+                       cfgs: Optional[TempoCfgs] = None):
+        """Adjoint step (tempo_adjoint_dev_c): ``fields`` is the state before the step
+        (unchanged); ``lam`` holds adjoints of the step's outputs on entry and of its
+        inputs on return; ``lam_diags`` the adjoints of the precipitation and refl10cm."""
+        cfg = cfgs if cfgs is not None else self.cfgs
+        bb, sptr, fp64 = self._dev_common(fields, bounds, stream)
+        x, lm = _state_of(fields), _state_of({k: v for k, v in lam.items() if k in DIFF_FIELDS})
+        ld = TempoDiags()
+        for n in DIAG2 + DIAG3:
+            if lam_diags and lam_diags.get(n) is not None:
+                setattr(ld, n, lam_diags[n].data_ptr())
+        _check(load_library().tempo_adjoint_dev_c(self._h, ctypes.byref(cfg), float(dt), int(itimestep),
+                                                   fp64, ctypes.byref(x), ctypes.byref(lm),
+                                                   ctypes.byref(ld), *bb, sptr))
 
     def set_graphs(self, on: bool = True):
         """Capture each distinct step into a CUDA graph and replay it (tempo_set_graphs)."""
