@@ -381,7 +381,7 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   const ColGeom g = col_geom(a, c);
   const long e = g.base + (long)k * a.NI;
   const uint32_t f = a.flags;
-  const bool has_nc = f & F_NC, has_nwfa = f & F_NWFA, has_nifa = f & F_NIFA, hail = f & F_HAIL;
+  const bool has_nc = f & F_NC, has_nwfa = f & F_NWFA, has_nifa = f & F_NIFA;
   const R dt = step_dt<R>(a), odt = step_odt<R>(a);
   const I dti = step_dti<R>(a);
   const R ncsave = ncsave_of<R>(a, g);

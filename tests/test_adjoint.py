@@ -85,7 +85,7 @@ def _cost_and_grad(ctx, f, dt, torch):
     new, diags = tempo_step(ctx, x, dt, 1)
     J = cost_precip_reflectivity(diags, f["dz"])
     J.backward()
-    return float(J), {k: x[k].grad for k in DIFF}
+    return float(J.detach()), {k: x[k].grad for k in DIFF}
 
 
 def test_gradient_matches_finite_differences(ctx_nohail):
@@ -102,31 +102,37 @@ def test_gradient_matches_finite_differences(ctx_nohail):
             return float(cost_precip_reflectivity(d, f["dz"]))
 
     rng = np.random.default_rng(3)
-    checked = agreed = 0
-    for _ in range(120):
+    nz_idx = {k: torch.nonzero(f[k]).cpu().numpy() for k in DIFF}
+    checked, bad = 0, []
+    for _ in range(800):
+        if checked >= 60:
+            break
         k = DIFF[rng.integers(len(DIFF))]
-        j, l, i = (int(rng.integers(s)) for s in f[k].shape)
-        x0 = float(f[k][j, l, i])
-        if x0 == 0.0:
+        nonzero = nz_idx[k]
+        if len(nonzero) == 0:
             continue
-        fd = []
-        for eps in (1e-4, 5e-5):
-            h = eps * abs(x0)
-            fp = {kk: v.clone() for kk, v in f.items()}
-            fm = {kk: v.clone() for kk, v in f.items()}
-            fp[k][j, l, i] += h
-            fm[k][j, l, i] -= h
-            fd.append((J_of(fp) - J_of(fm)) / (2 * h))
-        # a stable quotient: no threshold crossed within the perturbation
-        if abs(fd[0] - fd[1]) > 1e-3 * max(abs(fd[0]), 1e-12 * abs(J0) / abs(x0)):
+        j, l, i = (int(v) for v in nonzero[rng.integers(len(nonzero))])
+        x0 = float(f[k][j, l, i])
+        h = 1e-4 * abs(x0)
+        Jh = {}
+        for m in (1.0, -1.0, 0.5, -0.5):
+            ff = {kk: v.clone() for kk, v in f.items()}
+            ff[k][j, l, i] += m * h
+            Jh[m] = J_of(ff)
+        c1 = (Jh[1.0] - Jh[-1.0]) / (2 * h)
+        c2 = (Jh[0.5] - Jh[-0.5]) / h
+        dp, dm = (Jh[1.0] - J0) / h, (J0 - Jh[-1.0]) / h
+        floor = 1e-9 * abs(J0) / abs(x0)
+        # differentiable here: the one-sided quotients agree (no kink or clip at x0)
+        # and the centred ones converge (no threshold crossed within the perturbation)
+        if abs(dp - dm) > 1e-2 * abs(c1) + floor or abs(c1 - c2) > 1e-4 * abs(c2) + floor:
             continue
         g = float(grad[k][j, l, i])
         checked += 1
-        scale = max(abs(fd[1]), 1e-9 * abs(J0) / abs(x0))
-        if abs(g - fd[1]) <= 1e-4 * scale:
-            agreed += 1
+        if abs(g - c2) > 1e-4 * abs(c2) + floor:
+            bad.append((k, j, l, i, x0, g, c2, dp, dm))
     assert checked >= 40, checked
-    assert agreed >= 0.95 * checked, (agreed, checked)
+    assert len(bad) <= 0.05 * checked, (len(bad), checked, bad[:5])
 
 
 def test_fp32_gradient_close_to_fp64(ctx_nohail):
