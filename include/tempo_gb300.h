@@ -170,6 +170,27 @@ int tempo_run_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float 
                         int jts, int jte, int kts, int kte, tempo_diags_t *tempo_diags,
                         void *stream);
 
+/* No reference counterpart.  tempo_run_dev_f32_c (TEMPO_PREC_MIXED) that allocates no
+ * memory: for hosts that must not allocate device memory inside their time step (a
+ * model whose device memory pool is sized once at start-up with no headroom, or one
+ * that must not let a physics call synchronise the device, as cudaFree does).  The
+ * step's scratch is a fixed 64 MiB device array of the library, reserved when the
+ * library's module loads on a device; its address is looked up on the first call for
+ * each device, so make one call before any phase in which the host forbids CUDA
+ * runtime set-up.  Tiles that need more scratch (about 245 * nz + 45 bytes per column:
+ * about 4 200 columns at 65 levels) are rejected with TEMPO_ERR_ARG.  The scratch is
+ * shared by every context on a device: calls on one device must not overlap (issue
+ * them on one stream, or wait for one call's work before the next starts on another
+ * stream); overlapping calls race on the scratch.  Results equal tempo_run_dev_f32_c's. */
+int tempo_run_dev_f32_noalloc_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float dt,
+                                int itimestep, float *t, float *th, const float *pii,
+                                const float *p, const float *w, const float *dz, float *qv,
+                                float *qc, float *qr, float *qi, float *qs, float *qg, float *ni,
+                                float *nr, float *nc, float *nwfa, float *nifa, float *ng,
+                                float *qb, const int *land_input, int ims, int ime, int jms,
+                                int jme, int kms, int kme, int its, int ite, int jts, int jte,
+                                int kts, int kte, tempo_diags_t *tempo_diags, void *stream);
+
 /* tempo_aerosol_surface_emissions (src/module_mp_tempo_driver.F90:516-529) on device
  * arrays: nwfa(i,kts,j) += nwfa2d(i,j)*dt over the memory range. */
 int tempo_aerosol_surface_emissions_dev_c(tempo_ctx_t *ctx, double dt, double *nwfa,

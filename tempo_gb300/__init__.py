@@ -125,6 +125,7 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
     lib.tempo_run_dev_f32_c.argtypes = ([_VP, ctypes.POINTER(TempoCfgs), ctypes.c_float, i]
                                         + [_VP] * 19 + [_VP] + [i] * 12
                                         + [ctypes.POINTER(TempoDiags), _VP])
+    lib.tempo_run_dev_f32_noalloc_c.argtypes = lib.tempo_run_dev_f32_c.argtypes
     lib.tempo_aerosol_surface_emissions_dev_c.argtypes = [_VP, ctypes.c_double, _VP, _VP] + [i] * 7 + [_VP]
     lib.tempo_write_table_c.argtypes = [_VP, ctypes.c_char_p, ctypes.c_char_p]
     lib.tempo_get_table_c.argtypes = [_VP, ctypes.c_char_p, _DP, ctypes.c_long,
@@ -271,6 +272,36 @@ class TempoContext:
         _check(fn(self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs,
                   land.data_ptr() if land is not None else None,
                   ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte, ctypes.byref(d), sptr))
+
+    def run_device_noalloc(self, fields: dict, dt: float, itimestep: int,
+                           diags: Optional[dict] = None, bounds=None, stream=None,
+                           cfgs: Optional[TempoCfgs] = None):
+        """tempo_run_dev_f32_noalloc_c on float32 CUDA tensors (TEMPO_PREC_MIXED): the
+        step with its scratch in the library's fixed device array, allocating nothing.
+        Calls on one device must not overlap; tiles beyond the fixed scratch raise."""
+        import torch
+        lib = load_library()
+        cfg = cfgs if cfgs is not None else self.cfgs
+        p = fields["p"]
+        if p.dtype != torch.float32:
+            raise TempoError(-1, "the no-allocation step works on float32 device arrays")
+        nj, nk, ni = p.shape
+        b = list(bounds) if bounds is not None else [1, ni, 1, nj, 1, nk] * 3
+        for n, tns in fields.items():
+            if tns is not None and not (tns.is_cuda and tns.is_contiguous()):
+                raise TempoError(-1, f"{n} must be a contiguous CUDA tensor")
+        ptrs = [(fields[n].data_ptr() if fields.get(n) is not None else None) for n in FIELDS]
+        land = fields.get("land_input")
+        d = TempoDiags()
+        for n in DIAG2 + DIAG3:
+            a = (diags or {}).get(n)
+            if a is not None:
+                setattr(d, n, a.data_ptr())
+        s = stream if stream is not None else torch.cuda.current_stream(p.device)
+        _check(lib.tempo_run_dev_f32_noalloc_c(
+            self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs,
+            land.data_ptr() if land is not None else None, *b[6:], ctypes.byref(d),
+            ctypes.c_void_p(s.cuda_stream)))
 
     def autotune_device(self, fields: dict, dt: float, itimestep: int, diags: Optional[dict] = None,
                         bounds=None, stream=None, cfgs: Optional[TempoCfgs] = None,

@@ -32,6 +32,7 @@ UNITS = [
     ("tempo_tables.cu", ["-fmad=false"], "tempo_tables"),
     ("tempo_deriv_f64.cu", ["-fmad=false"], "tempo_deriv_f64"),
     ("tempo_deriv_f32.cu", [], "tempo_deriv_f32"),
+    ("tempo_noalloc.cu", [], "tempo_noalloc"),
 ]
 HOST_UNITS = ["tempo_capi.cpp", "tempo_host_init.cpp"]
 

@@ -6,6 +6,7 @@
 // arrays, stages the tile through HBM.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdint>
@@ -557,6 +558,64 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   return TEMPO_OK;
 }
 
+// The mixed step on FP32 device arrays with its scratch in the fixed device array of
+// tempo_noalloc.cu: no allocation, no graph, no timing events.  The scratch layout is
+// run_dev's.
+int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep,
+                    const RunArrays<float>& A, const Bounds& b, const tempo_diags_t* dg,
+                    cudaStream_t s) {
+  StepArgs<float> a;
+  if (int rc = build_args(c, cfg, dt, itimestep, A, b, dg, a)) return rc;
+  if (c->precision != TEMPO_PREC_MIXED)
+    return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
+  const size_t npad = (size_t)a.ncol_pad, nzs = (size_t)a.nz;
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t sd_bytes = al((size_t)SD_N * nzs * npad * 8);
+  const size_t sr_bytes = al((size_t)SR_N * nzs * npad * sizeof(float));
+  const size_t sc_bytes = al((size_t)SC_N * npad * 8);
+  const size_t act_bytes = al(npad * sizeof(int));
+  const size_t pm_bytes = al(nzs * npad);
+  const size_t cm_bytes = al(npad);
+  const size_t hg_bytes = al(nzs * npad * sizeof(float));
+  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes + 256;
+  if (total > kNoAllocScratchBytes)
+    return fail(TEMPO_ERR_ARG,
+                "%ld columns x %d levels need %zu bytes of scratch; the fixed scratch of "
+                "tempo_run_dev_f32_noalloc_c holds %zu (about %zu columns at this depth): "
+                "split the tile or call tempo_run_dev_f32_c",
+                a.ncol, a.nz, total, kNoAllocScratchBytes,
+                kNoAllocScratchBytes / (total / std::max<size_t>(npad, 1)));
+  void* base = nullptr;
+  CUDA_TRY(noalloc_scratch(c->device, &base));
+  char* sp = (char*)base;
+  a.sd = sp;
+  sp += sd_bytes;
+  a.sr = sp;
+  sp += sr_bytes;
+  a.sc = sp;
+  sp += sc_bytes;
+  a.act = (int*)sp;
+  sp += act_bytes;
+  a.pmask = (uint8_t*)sp;
+  sp += pm_bytes;
+  a.cmask = (uint8_t*)sp;
+  sp += cm_bytes;
+  a.hgt = sp;
+  sp += hg_bytes;
+  a.nact = (unsigned int*)sp;
+  a.stats = c->d_stats;
+  c->last_cols = a.ncol;
+  c->launches = kStepLaunches;
+  // the slot counter and the statistics accumulate with atomics: zero them first;
+  // every other scratch field is written before it is read
+  CUDA_TRY(cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s));
+  CUDA_TRY(cudaMemsetAsync(a.nact, 0, sizeof(unsigned int), s));
+  Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
+                  c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
+  CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->idf, s, nullptr, c->points_variant));
+  return TEMPO_OK;
+}
+
 // Stages host arrays through device mirrors (whole memory extent), runs, copies back.
 template <class S>
 int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, const RunArrays<S>& H,
@@ -814,6 +873,20 @@ int tempo_run_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, int i
   RunArrays<float> A{t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb, land_input};
   cudaStream_t s = (cudaStream_t)stream;  // NULL: the default stream
   return run_dev(c, cfg, (double)dt, itimestep, A, Bounds{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte}, diags, s);
+}
+
+int tempo_run_dev_f32_noalloc_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, int itimestep,
+                                float* t, float* th, const float* pii, const float* p,
+                                const float* w, const float* dz, float* qv, float* qc, float* qr,
+                                float* qi, float* qs, float* qg, float* ni, float* nr, float* nc,
+                                float* nwfa, float* nifa, float* ng, float* qb,
+                                const int* land_input, int ims, int ime, int jms, int jme, int kms,
+                                int kme, int its, int ite, int jts, int jte, int kts, int kte,
+                                tempo_diags_t* diags, void* stream) {
+  RunArrays<float> A{t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb, land_input};
+  cudaStream_t s = (cudaStream_t)stream;  // NULL: the default stream
+  return run_dev_noalloc(c, cfg, (double)dt, itimestep, A,
+                         Bounds{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte}, diags, s);
 }
 
 int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, int itimestep,

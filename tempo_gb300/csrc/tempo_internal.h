@@ -59,6 +59,11 @@ struct DerivOps {
                                const IslandConsts<Dual<T, IN_N>>& ci, const AdjArgs<T>& j, cudaStream_t s);
 };
 
+// tempo_noalloc.cu: the fixed scratch of tempo_run_dev_f32_noalloc_c (bytes, and its
+// address on `device`, looked up on the first call for that device)
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
+cudaError_t noalloc_scratch(int device, void** ptr);
+
 // number of points-kernel variants of the mixed form on FP32 storage
 constexpr int kPointsVariants = 8;
 // kernels launched per step (prep, points, sedim, final)
