@@ -176,8 +176,10 @@ int tempo_run_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float 
  * that must not let a physics call synchronise the device, as cudaFree does).  The
  * step's scratch is a fixed 64 MiB device array of the library, reserved when the
  * library's module loads on a device; its address is looked up on the first call for
- * each device, so make one call before any phase in which the host forbids CUDA
- * runtime set-up.  Tiles that need more scratch (about 245 * nz + 45 bytes per column:
+ * each device (with that device current), so make that first call before any stream
+ * capture and before any phase in which the host forbids CUDA runtime set-up.  Every
+ * call reuses the array and finds the previous call's contents there; the step clears
+ * what must start at zero (its active-column counter) itself.  Tiles that need more scratch (about 245 * nz + 45 bytes per column:
  * about 4 200 columns at 65 levels) are rejected with TEMPO_ERR_ARG.  The scratch is
  * shared by every context on a device: calls on one device must not overlap (issue
  * them on one stream, or wait for one call's work before the next starts on another
