@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(128) tempo_final_adjoint_kernel(
   final_point<R, T>(a, cst, ci, k, s, io);
   const ColGeom g = col_geom(a, a.act[s]);
   const long e = g.base + (long)k * a.NI;
-  const long cs = a.ncol_pad, fsd = (long)a.nz * cs, o = (long)k * cs + s;
+  const long cs = a.ncol_pad, fsd = (long)a.nz * cs, o = pt_off(s, k, a.nz);
   // state inputs: all overwritten by phase C (temperature and the checked species)
   constexpr int carr[14] = {A_T, -1, -1, -1, A_QC, A_NC, A_QR, A_NR, A_QI, A_NI, A_QS, A_QG, A_NG, A_QB};
   for (int i = 0; i < 14; i++) {
@@ -234,17 +234,17 @@ __global__ void __launch_bounds__(128) tempo_sedim_adjoint_kernel(
   const T dt = T(a.dt);
   T* w = wbase + s;
   auto WR = [&](long row) -> T& { return w[row * cs]; };
-  auto rho = [&](int k) { return j.psd[SD_RHO * fsd + (long)k * cs + s].v; };
-  auto cand = [&](int f, int k) { return j.psr[(long)f * fsd + (long)k * cs + s].v; };
-  auto lsd = [&](int f, int k) -> T& { return j.lam_sd[(long)f * fsd + (long)k * cs + s]; };
-  auto lsr = [&](int f, int k) -> T& { return j.lam_sr[(long)f * fsd + (long)k * cs + s]; };
+  auto rho = [&](int k) { return j.psd[SD_RHO * fsd + pt_off(s, k, nz)].v; };
+  auto cand = [&](int f, int k) { return j.psr[(long)f * fsd + pt_off(s, k, nz)].v; };
+  auto lsd = [&](int f, int k) -> T& { return j.lam_sd[(long)f * fsd + pt_off(s, k, nz)]; };
+  auto lsr = [&](int f, int k) -> T& { return j.lam_sr[(long)f * fsd + pt_off(s, k, nz)]; };
 
   uint8_t any = 0;
-  for (int k = 0; k < nz; k++) any |= a.pmask[(long)k * cs + s];
+  for (int k = 0; k < nz; k++) any |= a.pmask[pt_off(s, k, nz)];
   const bool any_qr = any & PM_QR, any_qg = any & PM_QG, any_qs = any & PM_QS,
              any_qi = any & PM_QI, any_qc = any & PM_QC;
   for (int f = 0; f < 10; f++)
-    for (int k = 0; k < nz; k++) WR(W.xw(f, k, nz)) = j.psd[(long)(SD_XRR + f) * fsd + (long)k * cs + s].v;
+    for (int k = 0; k < nz; k++) WR(W.xw(f, k, nz)) = j.psd[(long)(SD_XRR + f) * fsd + pt_off(s, k, nz)].v;
 
   // fill (forward): filled speeds into VF rows; steps and ktop as in the forward kernel
   auto fill = [&](int fv, int fvn, bool use_max, int& steps, int& ktop) {
@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(128) tempo_sedim_adjoint_kernel(
         if (cand(SR_VTSB, k) != T(0)) {  // v = A srr + (1 - srr) vrain, srr = rs / (rs + rr)
           const T l = lsr(SR_VTSA, k);
           const T vrain = any_qr ? WR(W.vf(SR_VTR, k, nz)) : T(0);
-          const T rsk = j.psd[(long)SD_XRS * fsd + (long)k * cs + s].v;
+          const T rsk = j.psd[(long)SD_XRS * fsd + pt_off(s, k, nz)].v;
           const T rrk = WR(W.xw(0, k, nz));  // rain after its sedimentation
           const T srr = rsk / (rsk + rrk);
           lsr(SR_VTSA, k) = l * srr;

@@ -590,6 +590,21 @@ __device__ bool thermo(Lev<R>& L) {
   return L.ssati > 0.0;
 }
 
+// The part of thermo_vars that the fall speeds read after the last stage of phase A
+// (rhof; visco for the density-dependent graupel speed), computed exactly as thermo
+// does; the other fields of the last thermo_vars call have no reader.
+template <class R>
+__device__ __forceinline__ void thermo_tail(Lev<R>& L) {
+  using I = Isl<R>;
+  I tempc = L.temp - t0;
+  L.rhof = R(Sqrt(L.ci->rho_not / L.rho));
+  R rtc = R(tempc);
+  if (tempc >= 0.0)
+    L.visco = (R(1.718) + R(0.0049) * rtc) * R(1.0e-5);
+  else
+    L.visco = (R(1.718) + R(0.0049) * rtc - R(1.2e-5) * rtc * rtc) * R(1.0e-5);
+}
+
 template <class I>
 __device__ __forceinline__ I rho_of(const IslandConsts<I>& ci, I pres, I temp, I qv) {  // main:325
   return ci.roverrv * pres / (rdry * temp * (qv + ci.roverrv));

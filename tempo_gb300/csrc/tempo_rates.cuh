@@ -749,13 +749,30 @@ __device__ void cloud_condensation(const Lev<R>& L, Tend<R>& t, const Tables<Cst
   if (Fabs(L.ssatw) < eps) return;
   using I = Isl<R>;
   R orho = R(1.0 / L.rho);
-  I lvt2 = I(L.lvt2);
-  I clap = (L.qv - L.qvs) / (1.0 + lvt2 * L.qvs);
-  for (int n = 1; n <= 3; n++) {  // Newton on qvs exp(lvt2 c) - qv + c = 0 (main:2002-2007)
-    const I ex = Exp(lvt2 * clap);
-    I fcd = L.qvs * ex - L.qv + clap;
-    I dfcd = L.qvs * lvt2 * ex + 1.0;
-    clap = clap - fcd / dfcd;
+  I clap;
+  if constexpr (std::is_same<I, df>::value) {
+    // Mixed form: the cancellation sits in qv - qvs, formed once in the island type; the
+    // three Newton iterations then solve in FP32 for the condensed amount c on
+    // qvs (exp(lvt2 c) - 1) + c - (qv - qvs), the same function as qvs exp(lvt2 c) - qv
+    // + c, with every term of the size of c (so FP32 gives c to FP32 precision).
+    const float d = float(L.qv - L.qvs), qs = float(L.qvs), lv = float(L.lvt2);
+    float c = d / (1.0f + lv * qs);
+    for (int n = 1; n <= 3; n++) {
+      const float em1 = expm1f(lv * c);
+      const float fcd = qs * em1 + (c - d);
+      const float dfcd = qs * lv * (em1 + 1.0f) + 1.0f;
+      c = c - fcd / dfcd;
+    }
+    clap = I(c);
+  } else {
+    I lvt2 = I(L.lvt2);
+    clap = (L.qv - L.qvs) / (1.0 + lvt2 * L.qvs);
+    for (int n = 1; n <= 3; n++) {  // Newton on qvs exp(lvt2 c) - qv + c = 0 (main:2002-2007)
+      const I ex = Exp(lvt2 * clap);
+      I fcd = L.qvs * ex - L.qv + clap;
+      I dfcd = L.qvs * lvt2 * ex + 1.0;
+      clap = clap - fcd / dfcd;
+    }
   }
   I xrc = I(L.rc) + clap * L.rho;
   if (xrc > r1) {

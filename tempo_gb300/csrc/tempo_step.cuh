@@ -230,11 +230,11 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
     if (!(f & F_NWFA) || !(f & F_NIFA)) {
       // heights for the aerosol initial profiles (init_*_friendly_aerosols,
       // aerosols:14-73): hgt(1) = 0, and level 1 takes hgt(2)
-      Cst<R>* hgt = reinterpret_cast<Cst<R>*>(a.hgt) + s;
+      Cst<R>* hgt = reinterpret_cast<Cst<R>*>(a.hgt) + pt_base(s, nz);
       I h = I(0.0);
       for (int k = 1; k < nz; k++) {
         h = h + ldi<I>(a.dz + g.base + (long)k * a.NI);
-        hgt[(long)k * a.ncol_pad] = Cst<R>(h);
+        hgt[(long)k * kSlotTile] = Cst<R>(h);
       }
       hgt[0] = (nz > 1) ? Cst<R>(ldi<I>(a.dz + g.base + a.NI)) : Cst<R>(0.0);
     }
@@ -366,6 +366,34 @@ __host__ __device__ constexpr int points_min_blocks(int v) {
   return ((v >> 1) & 3) == 0 ? 1 : ((v >> 1) & 3) + 2;
 }
 
+// mass- and number-weighted fall speeds of rain at a level with rain (rain_fallspeed,
+// main:1771-1774)
+template <class R>
+__device__ __forceinline__ void rain_speeds(const Lev<R>& L, const TempoConsts<Cst<R>>& cc, R& vt, R& vtn) {
+  R lamr = R(1.0) / L.ilamr;
+  vt = L.rhof * R(av_r) * cc.crg[5] * cc.org3 * Pow(lamr, cc.cre[2]) * Pow(lamr + R(fv_r), -cc.cre[5]);
+  vtn = L.rhof * R(av_r) * cc.crg[6] / cc.crg[11] * Pow(lamr, cc.cre[11]) * Pow(lamr + R(fv_r), -cc.cre[6]);
+}
+// the same for graupel (graupel_fallspeed, main:1817-1833), density-dependent with qb
+template <class R>
+__device__ __forceinline__ void graupel_speeds(const Lev<R>& L, const TempoConsts<Cst<R>>& cc, uint32_t f,
+                                               R& vt, R& vtn) {
+  R afall, bfall;
+  if (f & F_QB) {
+    R dens_g = Max(rho_g<R>(1), Min(R(meters3_to_liters) * L.rg / L.rb, rho_g<R>(nrhg)));
+    afall = R(a_coeff) * Pow((R(4.0) * dens_g * R(earth_gravity)) / (R(3.0) * R(L.rho)), R(b_coeff));
+    afall = afall * Pow(L.visco, R(1.0) - R(2.0) * R(b_coeff));
+    bfall = R(3.0) * R(b_coeff) - R(1.0);
+  } else {
+    afall = R(av_g_old);
+    bfall = R(bv_g_old);
+  }
+  const int ig = L.idx_bg;
+  R pb = Pow(L.ilamg, bfall);
+  vt = L.rhof * afall * cc.cgg[ig - 1][5] * cc.ogg3 * pb;
+  vtn = L.rhof * afall * cc.cgg[ig - 1][6] / cc.cgg[ig - 1][11] * pb;
+}
+
 // ---------------------------------------------------------------------------------
 // points: phase A at one (level, active slot)
 // ---------------------------------------------------------------------------------
@@ -387,7 +415,7 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   const R ncsave = ncsave_of<R>(a, g);
   const R ncsave_cond = has_nc ? R(nt_c_l) : ncsave;
   const bool do_ginit = a.cmask[s] & CM_GINIT;
-  const long cs = a.ncol_pad, fsd = (long)nz * cs, o = (long)k * cs + s;
+  const long cs = a.ncol_pad, fsd = (long)nz * cs, o = pt_off(s, k, nz);
   I* sd = reinterpret_cast<I*>(a.sd);
   R* sr = reinterpret_cast<R*>(a.sr);
 
@@ -417,11 +445,18 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   Tend<R> td = {};
   const bool do_cond = !(f & F_NOMICRO) && (f & F_COND);
   const bool do_evap = !(f & F_NOMICRO);
+  // Where no later reader needs them, the thermodynamic fields are not recomputed:
+  // rain evaporation reads them only where rain exists (it returns at once otherwise),
+  // and after the last stage only the fall speeds' rhof and visco are read
+  // (thermo_tail).  The values read are the same as with every call made.
   if constexpr (V & 1) {
     int stage = 0;
 #pragma unroll 1
     for (;;) {
-      thermo(L);
+      if (stage == 3 || (stage == 2 && !L.l_qr))
+        thermo_tail(L);
+      else
+        thermo(L);
       if (stage > 2) break;
       points_stage(stage, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
       stage = stage == 0 ? (do_cond ? 1 : do_evap ? 2 : 3) : stage == 1 ? (do_evap ? 2 : 3) : 3;
@@ -429,42 +464,26 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   } else {
     thermo(L);
     points_stage(0, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
-    thermo(L);
     if (do_cond) {
-      points_stage(1, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
       thermo(L);
+      points_stage(1, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
     }
     if (do_evap) {
+      if (L.l_qr)
+        thermo(L);
+      else
+        thermo_tail(L);
       points_stage(2, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
-      thermo(L);
     }
+    thermo_tail(L);
   }
 
   // fall-speed candidates (main:1770-1977), unfilled; < 0 marks "absent"
   const TempoConsts<Cst<R>>& cc = cst;
   R vtr = R(-1), vtnr = R(-1), vtg = R(-1), vtng = R(-1), vsa = R(-1), vsb = R(0);
   R vti = R(-1), vtni = R(-1), vtc = R(0), vtnc = R(0);
-  if (L.rr > R(r1)) {
-    R lamr = R(1.0) / L.ilamr;
-    vtr = L.rhof * R(av_r) * cc.crg[5] * cc.org3 * Pow(lamr, cc.cre[2]) * Pow(lamr + R(fv_r), -cc.cre[5]);
-    vtnr = L.rhof * R(av_r) * cc.crg[6] / cc.crg[11] * Pow(lamr, cc.cre[11]) * Pow(lamr + R(fv_r), -cc.cre[6]);
-  }
-  if (L.rg > R(r1)) {
-    R afall, bfall;
-    if (f & F_QB) {
-      R dens_g = Max(rho_g<R>(1), Min(R(meters3_to_liters) * L.rg / L.rb, rho_g<R>(nrhg)));
-      afall = R(a_coeff) * Pow((R(4.0) * dens_g * R(earth_gravity)) / (R(3.0) * R(L.rho)), R(b_coeff));
-      afall = afall * Pow(L.visco, R(1.0) - R(2.0) * R(b_coeff));
-      bfall = R(3.0) * R(b_coeff) - R(1.0);
-    } else {
-      afall = R(av_g_old);
-      bfall = R(bv_g_old);
-    }
-    const int ig = L.idx_bg;
-    R pb = Pow(L.ilamg, bfall);
-    vtg = L.rhof * afall * cc.cgg[ig - 1][5] * cc.ogg3 * pb;
-    vtng = L.rhof * afall * cc.cgg[ig - 1][6] / cc.cgg[ig - 1][11] * pb;
-  }
+  if (L.rr > R(r1)) rain_speeds(L, cc, vtr, vtnr);
+  if (L.rg > R(r1)) graupel_speeds(L, cc, f, vtg, vtng);
   if (L.rs > R(r1)) {
     R xds = L.smoc / L.smob;
     R mrat = R(1.0) / xds;
@@ -573,14 +592,14 @@ __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant_
   const long NI = a.NI;
   const ColGeom g = col_geom(a, a.act[s]);
   const long cs = a.ncol_pad, fsd = (long)nz * cs;
-  I* sd = reinterpret_cast<I*>(a.sd) + s;
-  R* sr = reinterpret_cast<R*>(a.sr) + s;
+  I* sd = reinterpret_cast<I*>(a.sd) + pt_base(s, nz);
+  R* sr = reinterpret_cast<R*>(a.sr) + pt_base(s, nz);
   const R dt = step_dt<R>(a);
   const I dti = step_dti<R>(a);
   const S* dzp = a.dz + g.base;
 
   uint8_t any = 0;
-  for (int k = 0; k < nz; k++) any |= a.pmask[(long)k * cs + s];
+  for (int k = 0; k < nz; k++) any |= a.pmask[pt_off(s, k, nz)];
   const bool any_qr = any & PM_QR, any_qg = any & PM_QG, any_qs = any & PM_QS,
              any_qi = any & PM_QI, any_qc = any & PM_QC;
 
@@ -592,7 +611,7 @@ __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant_
     ktop = 1;
     R vup = R(0), vnup = R(0);
     for (int k = nz - 1; k >= 0; k--) {
-      const long o = (long)k * cs;
+      const long o = (long)k * kSlotTile;
       R v, vn = R(0);
       if (snow) {
         R A = sr[SR_VTSA * fsd + o];
@@ -644,16 +663,16 @@ __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant_
       const I* ozr = sd + SD_OZR * fsd;
       const I cx = dti * osteps;
       int k = nz - 1;
-      I s_top = I(vt[k * cs]) * x[k * cs];
-      ten[k * cs] = ten[k * cs] - s_top * ozr[k * cs] * osteps;
-      x[k * cs] = Max(lim, x[k * cs] - s_top * odz[k * cs] * cx);
-      I s_up = (ktop == nz - 1) ? s_top : I(vt[ktop * cs]) * x[ktop * cs];
+      I s_top = I(vt[k * kSlotTile]) * x[k * kSlotTile];
+      ten[k * kSlotTile] = ten[k * kSlotTile] - s_top * ozr[k * kSlotTile] * osteps;
+      x[k * kSlotTile] = Max(lim, x[k * kSlotTile] - s_top * odz[k * kSlotTile] * cx);
+      I s_up = (ktop == nz - 1) ? s_top : I(vt[ktop * kSlotTile]) * x[ktop * kSlotTile];
       I s0 = (nz == 1) ? s_top : I(vt[0]) * x[0];
       for (k = ktop - 1; k >= 0; k--) {
-        const I s_k = I(vt[k * cs]) * x[k * cs];
+        const I s_k = I(vt[k * kSlotTile]) * x[k * kSlotTile];
         const I dflux = s_up - s_k;
-        ten[k * cs] = ten[k * cs] + dflux * ozr[k * cs] * osteps;
-        x[k * cs] = Max(lim, x[k * cs] + dflux * odz[k * cs] * cx);
+        ten[k * kSlotTile] = ten[k * kSlotTile] + dflux * ozr[k * kSlotTile] * osteps;
+        x[k * kSlotTile] = Max(lim, x[k * kSlotTile] + dflux * odz[k * kSlotTile] * cx);
         if (k == 0) s0 = s_k;
         s_up = s_k;
       }
@@ -661,18 +680,18 @@ __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant_
       return;
     }
     int k = nz - 1;
-    I s_top = I(vt[k * cs]) * x[k * cs];
-    I odz = 1.0 / ldi<I>(dzp + k * NI), orho = 1.0 / rho[k * cs];
-    ten[k * cs] = ten[k * cs] - s_top * odz * osteps * orho;
-    x[k * cs] = Max(lim, x[k * cs] - s_top * odz * dti * osteps);
-    I s_up = (ktop == nz - 1) ? s_top : I(vt[ktop * cs]) * x[ktop * cs];
+    I s_top = I(vt[k * kSlotTile]) * x[k * kSlotTile];
+    I odz = 1.0 / ldi<I>(dzp + k * NI), orho = 1.0 / rho[k * kSlotTile];
+    ten[k * kSlotTile] = ten[k * kSlotTile] - s_top * odz * osteps * orho;
+    x[k * kSlotTile] = Max(lim, x[k * kSlotTile] - s_top * odz * dti * osteps);
+    I s_up = (ktop == nz - 1) ? s_top : I(vt[ktop * kSlotTile]) * x[ktop * kSlotTile];
     I s0 = (nz == 1) ? s_top : I(vt[0]) * x[0];
     for (k = ktop - 1; k >= 0; k--) {
-      I s_k = I(vt[k * cs]) * x[k * cs];
+      I s_k = I(vt[k * kSlotTile]) * x[k * kSlotTile];
       odz = 1.0 / ldi<I>(dzp + k * NI);
-      orho = 1.0 / rho[k * cs];
-      ten[k * cs] = ten[k * cs] + (s_up - s_k) * odz * osteps * orho;
-      x[k * cs] = Max(lim, x[k * cs] + (s_up - s_k) * odz * dti * osteps);
+      orho = 1.0 / rho[k * kSlotTile];
+      ten[k * kSlotTile] = ten[k * kSlotTile] + (s_up - s_k) * odz * osteps * orho;
+      x[k * kSlotTile] = Max(lim, x[k * kSlotTile] + (s_up - s_k) * odz * dti * osteps);
       if (k == 0) s0 = s_k;
       s_up = s_k;
     }
@@ -712,13 +731,13 @@ __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant_
     int kt = 1;
     I hgtc = I(0.0);
     for (int k = 1; k <= nz - 1; k++) {
-      if (sd[SD_XRC * fsd + (long)(k - 1) * cs] > r2) kt = k;
+      if (sd[SD_XRC * fsd + (long)(k - 1) * kSlotTile] > r2) kt = k;
       hgtc = hgtc + ldi<I>(dzp + (long)(k - 1) * NI);
       if (hgtc > 500.0) break;
     }
     for (int k = kt; k < nz; k++) {  // vt stays zero above ktop
-      sr[SR_VTC * fsd + (long)k * cs] = R(0);
-      sr[SR_VTNC * fsd + (long)k * cs] = R(0);
+      sr[SR_VTC * fsd + (long)k * kSlotTile] = R(0);
+      sr[SR_VTNC * fsd + (long)k * kSlotTile] = R(0);
     }
     sub[4] = 1;
     sweep(SD_XRC, SD_TQC, SR_VTC, r1, 1, kt, &prec_c);
@@ -760,7 +779,7 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
   const R dt = step_dt<R>(a), odt = step_odt<R>(a);
   const I dti = step_dti<R>(a);
   const R ncsave = ncsave_of<R>(a, g);
-  const long cs = a.ncol_pad, fsd = (long)nz * cs, o = (long)k * cs + s;
+  const long cs = a.ncol_pad, fsd = (long)nz * cs, o = pt_off(s, k, nz);
 
   Lev<R> L;
   L.cs = &cst;

@@ -69,8 +69,8 @@ enum CMaskBit : uint8_t { CM_GINIT = 1 };
 // One step's arguments.  The step runs as four kernels over the tile's columns:
 // prep (per column: early-exit test, compaction of active columns into slots),
 // points (per active level: phase A), sedim (per active column: sedimentation),
-// final (per active level: phase C).  Scratch is indexed by active-column slot s,
-// [field][level][slot] with slot fastest.
+// final (per active level: phase C).  Scratch is indexed by active-column slot s: a
+// field plane per scratch field, point (level k, slot s) at pt_off(s, k, nz).
 template <class S>
 struct StepArgs {
   S *t, *th;
@@ -91,14 +91,15 @@ struct StepArgs {
   double nc_single;   // single-moment cloud number (m^-3) when nc is absent and no land
   double niccn3, niin3;  // decay rates of the aerosol initial profiles (aerosols:14-73)
   uint32_t flags;
-  void* sd;           // Isl<R>[SD_N][nz][ncol_pad]
-  void* sr;           // R[SR_N][nz][ncol_pad]
+  // scratch planes of nz * ncol_pad points in the layout of pt_off
+  void* sd;           // Isl<R>[SD_N] planes
+  void* sr;           // R[SR_N] planes
   void* sc;           // Isl<R>[SC_N][ncol_pad]
-  void* hgt;          // Cst<R>[nz][ncol_pad]: level heights for the aerosol initial profiles
+  void* hgt;          // Cst<R> plane: level heights for the aerosol initial profiles
                       // (written only when nwfa or nifa is absent)
   int* act;           // [ncol_pad] column of each active slot
   unsigned int* nact; // active-slot counter (zero before prep)
-  uint8_t* pmask;     // [nz][ncol_pad]
+  uint8_t* pmask;     // plane: species present at the point after phase A
   uint8_t* cmask;     // [ncol_pad]
   unsigned long long* stats;  // [0] early exits, [1..5] max substeps
 };
@@ -129,6 +130,17 @@ struct AdjArgs {
   const Dual<T, 1>* psc;    // primal per-column sums
   const uint8_t* colflag;   // [ncol]: 1 = active column
 };
+
+// Point layout of the scratch planes (sd, sr, pmask, hgt and the adjoint's copies):
+// each field plane holds nz * ncol_pad points; slots form tiles of kSlotTile consecutive
+// slots, a tile stores its levels one after another, its slots fastest.  A warp over 32
+// aligned slots of one level touches one contiguous segment (whole 32-byte sectors for
+// every element size); a thread walking one slot's levels stays inside nz * kSlotTile
+// entries (within one memory page), so a column's levels never spread over the whole
+// plane.
+constexpr int kSlotTile = 32;
+TG_HD inline long pt_base(long s, int nz) { return (s / kSlotTile) * (long)nz * kSlotTile + (s % kSlotTile); }
+TG_HD inline long pt_off(long s, int k, int nz) { return pt_base(s, nz) + (long)k * kSlotTile; }
 
 // Workspace rows (T, [row][slot]): working state of the 10 sedimenting fields, their
 // filled fall speeds, checkpoints every 4 substeps, the pre-substep states of one block
