@@ -1949,21 +1949,25 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
   int is_first_step = (itimestep == 1);
   long ncols = (long)(ite - its + 1) * (jte - jts + 1);
   long early = 0, maxsub[5] = {0, 0, 0, 0, 0};
-  /* driver:328-386: reset the diagnostics that tempo_run allocates */
+  /* driver:302-386: reset the diagnostics that tempo_run allocates; a diagnostic whose
+   * flag is off is neither allocated nor touched */
   for (long c = 0; c < ncols; c++) {
     double *d2[] = {dg->rain_precip, dg->ice_liquid_equiv_precip, dg->snow_liquid_equiv_precip,
                     dg->graupel_liquid_equiv_precip, dg->frozen_fraction, dg->frz_rain_precip,
                     dg->max_hail_diameter_sfc, dg->max_hail_diameter_column};
     for (int a = 0; a < 8; a++)
-      if (d2[a]) d2[a][c] = 0.0;
+      if (d2[a] && (a < 6 || cfg->max_hail_diameter_flag)) d2[a][c] = 0.0;
   }
   long n3 = ncols * tk;
   for (long c = 0; c < n3; c++) {
-    if (dg->refl10cm) dg->refl10cm[c] = -35.0;
+    if (dg->refl10cm && cfg->refl10cm_flag) dg->refl10cm[c] = -35.0;
     double *d3[] = {dg->re_cloud, dg->re_ice, dg->re_snow, dg->rain_med_vol_diam,
                     dg->graupel_med_vol_diam, dg->cloud_number_mixing_ratio};
+    const int on3[] = {cfg->re_cloud_flag, cfg->re_ice_flag, cfg->re_snow_flag,
+                       cfg->rain_med_vol_diam_flag, cfg->graupel_med_vol_diam_flag,
+                       cfg->cloud_number_mixing_ratio_flag};
     for (int a = 0; a < 6; a++)
-      if (d3[a]) d3[a][c] = 0.0;
+      if (d3[a] && on3[a]) d3[a][c] = 0.0;
   }
   if (nthreads > 0) {
 #ifdef _OPENMP

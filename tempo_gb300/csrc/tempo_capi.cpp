@@ -646,6 +646,16 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
                     dg ? dg->re_snow : nullptr, dg ? dg->rain_med_vol_diam : nullptr,
                     dg ? dg->graupel_med_vol_diam : nullptr,
                     dg ? dg->cloud_number_mixing_ratio : nullptr};
+  // diagnostics whose flag is off are not computed: the host arrays stay as they are
+  // (no mirror, no copy back), as the reference leaves them unallocated (driver:302-386)
+  const bool diag_on[15] = {true, true, true, true, true, true,
+                            cfg && cfg->max_hail_diameter_flag, cfg && cfg->max_hail_diameter_flag,
+                            cfg && cfg->refl10cm_flag, cfg && cfg->re_cloud_flag,
+                            cfg && cfg->re_ice_flag, cfg && cfg->re_snow_flag,
+                            cfg && cfg->rain_med_vol_diam_flag, cfg && cfg->graupel_med_vol_diam_flag,
+                            cfg && cfg->cloud_number_mixing_ratio_flag};
+  for (int i = 0; i < 15; i++)
+    if (!diag_on[i]) dg_h[i] = nullptr;
   const int nslots = n_in + 1 + 15;
   if (c->mirrors.size() < (size_t)nslots) c->mirrors.resize(nslots);
   void* d[nslots];

@@ -72,6 +72,9 @@ def compare(fa, da, fb, db, names3=OUT3, inputs=None):
             out[n] = (float(e.max()), float(np.sqrt(np.mean(e * e))))
     for n in tuple(DIAG2) + tuple(DIAG3):
         if n in da and n in db:
+            # a diagnostic whose flag is off stays untouched in both (driver:302-386)
+            if np.isnan(db[n]).all() and np.isnan(da[n]).all():
+                continue
             assert not np.isnan(db[n]).any(), f"oracle left {n} unset"
             assert not np.isnan(da[n]).any(), f"{n} not written"
             e = rel_err(da[n], db[n], FLOOR[n])
@@ -121,6 +124,8 @@ def compare_with_ties(fa, da, fb, db, ties, tol, names3=OUT3, inputs=None):
     items = [(n, fa, fb) for n in names3 if n in fa and n in fb]
     items += [(n, da, db) for n in tuple(DIAG2) + tuple(DIAG3) if n in da and n in db]
     for n, A, B in items:
+        if A is da and np.isnan(B[n]).all() and np.isnan(A[n]).all():
+            continue  # flag off: untouched in both
         assert not np.isnan(B[n]).any(), f"oracle left {n} unset"
         assert not np.isnan(A[n]).any(), f"{n} not written"
         sc = None if (inputs is None or A is da) else inputs.get(n)
