@@ -226,14 +226,16 @@ int tempo_last_stats_c(tempo_ctx_t *ctx, long out[8]);
 int tempo_set_kernel_timing(tempo_ctx_t *ctx, int on);
 int tempo_kernel_times_c(tempo_ctx_t *ctx, float ms[4]);
 
-/* No reference counterpart.  Autotuner of the mixed form on FP32 device storage: runs
- * the step `reps` times with every variant of its per-level kernel (thread-to-work
- * mapping and register budget) on private copies of the given state -- the caller's
- * arrays are not modified -- times the per-level kernel with CUDA events on `stream`,
- * and keeps the fastest variant for later TEMPO_PREC_MIXED runs on FP32 storage.
- * Arguments as tempo_run_dev_f32_c; times_ms (optional, `count` entries) receives each
- * variant's best time, *chosen (optional) the variant kept.  Needs device memory for a
- * copy of every array the step writes. */
+/* No reference counterpart.  Autotuner of the mixed form on FP32 device storage: for
+ * every variant of its per-level kernel (thread-to-work mapping and register budget) it
+ * copies the given state and runs `reps` consecutive steps (itimestep, itimestep + 1,
+ * ...) on the copy -- the caller's arrays are not modified -- timing the per-level
+ * kernel with CUDA events on `stream`, and keeps the variant with the smallest sum for
+ * later TEMPO_PREC_MIXED runs on FP32 storage.  Tune on a state like the ones the runs
+ * will see: the work of a step depends on the state it starts from.  Arguments as
+ * tempo_run_dev_f32_c; times_ms (optional, `count` entries) receives each variant's
+ * summed time, *chosen (optional) the variant kept.  Needs device memory for a copy of
+ * every array the step writes. */
 int tempo_autotune_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float dt,
                              int itimestep, float *t, float *th, const float *pii,
                              const float *p, const float *w, const float *dz, float *qv,

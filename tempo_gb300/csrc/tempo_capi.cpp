@@ -944,20 +944,21 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, 
   int rc = tempo_set_kernel_timing(c, 1);
   float best = 0.0f;
   int best_v = saved_variant;
+  // every variant runs the same `reps` consecutive steps from a fresh copy of the state
+  // (the work of a step depends on the state it starts from) and is scored by their sum
   for (int v = 0; v < kPointsVariants && rc == TEMPO_OK; v++) {
     c->points_variant = v;
     float vbest = 0.0f;
+    for (int i = 0; i < NIO; i++)
+      if (io[i] && cudaMemcpyAsync(cp[i], io[i], ext * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        rc = fail(TEMPO_ERR_CUDA, "autotune: state copy");
     for (int r = 0; r < reps && rc == TEMPO_OK; r++) {
-      for (int i = 0; i < NIO; i++)
-        if (io[i] && cudaMemcpyAsync(cp[i], io[i], ext * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-          rc = fail(TEMPO_ERR_CUDA, "autotune: state copy");
-      if (rc) break;
       RunArrays<float> A{cp[0], cp[1], pii, p, w, dz, cp[2], cp[3], cp[4], cp[5], cp[6],
                          cp[7], cp[8], cp[9], cp[10], cp[11], cp[12], cp[13], cp[14], land_input};
-      rc = run_dev(c, cfg, (double)dt, itimestep, A, b, diags ? &dcopy : nullptr, s);
+      rc = run_dev(c, cfg, (double)dt, itimestep + r, A, b, diags ? &dcopy : nullptr, s);
       float ms[kStepLaunches];
       if (rc == TEMPO_OK) rc = tempo_kernel_times_c(c, ms);
-      if (rc == TEMPO_OK && (r == 0 || ms[1] < vbest)) vbest = ms[1];
+      if (rc == TEMPO_OK) vbest += ms[1];
     }
     if (rc) break;
     if (times_ms && v < count) times_ms[v] = vbest;
