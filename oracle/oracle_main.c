@@ -640,12 +640,155 @@ static void sedimentation(int nz, double *xr, const double *vt, const double *dz
     if (xr[0] > low_limit_mass_for_precip) *precip = *precip + sed_r[0] * dt * (1.0 / (double)steps);
 }
 
-/* rain_fallspeed (main:1752-1790) */
+/* substep reduction of the semi-Lagrangian path (main:595, 636) */
+static const double semi_sedi_factor = 10.0;
+
+/* semilagrangian_sedimentation (main:1562-1749): the semi-Lagrangian scheme of Juang and
+ * Hong (2010), Mon. Wea. Rev. 138, 1778-1791.  vt holds nz + 1 speeds (vt[nz] = 0).
+ * Arrays below keep the reference's 1-based indices through the macros. */
+static void semilagrangian_sedimentation(int nz, const double *dz1d, const double *rho, double *xr,
+                                         double *xten, const double *vt, int steps, double limit,
+                                         double *precip, double dt, double odt) {
+  double zi_[nz + 1], wi_[nz + 1], dza_[nz + 1], za_[nz + 2], qa_[nz + 1], qmi_[nz + 1],
+      qpi_[nz + 1], rr_save_[nz];
+#define ZI(i) zi_[(i) - 1]
+#define WI(i) wi_[(i) - 1]
+#define DZA(i) dza_[(i) - 1]
+#define ZA(i) za_[(i) - 1]
+#define QA(i) qa_[(i) - 1]
+#define QMI(i) qmi_[(i) - 1]
+#define QPI(i) qpi_[(i) - 1]
+#define VT(i) vt[(i) - 1]
+#define DZ(i) dz1d[(i) - 1]
+#define XR(i) xr[(i) - 1]
+  const double osteps = 1.0 / (double)steps;
+  for (int k = 1; k <= nz + 1; k++) ZI(k) = WI(k) = DZA(k) = QA(k) = QMI(k) = QPI(k) = 0.0;
+  for (int k = 1; k <= nz + 2; k++) ZA(k) = 0.0;
+  for (int k = 0; k < nz; k++) rr_save_[k] = xr[k];
+  ZI(1) = 0.0;
+  for (int k = 1; k <= nz; k++) ZI(k + 1) = ZI(k) + DZ(k);
+  /* 3rd-order interpolation of the interface speeds (:1599-1611) */
+  const double fa1 = 9.0 / 16.0, fa2 = 1.0 / 16.0;
+  WI(1) = VT(1);
+  WI(2) = 0.5 * (VT(2) + VT(1));
+  for (int k = 3; k <= nz - 1; k++) WI(k) = fa1 * (VT(k) + VT(k - 1)) - fa2 * (VT(k + 1) + VT(k - 2));
+  WI(nz) = 0.5 * (VT(nz) + VT(nz - 1));
+  WI(nz + 1) = VT(nz + 1);
+  for (int k = 2; k <= nz; k++)
+    if (VT(k) == 0.0) WI(k) = VT(k - 1);
+  /* limit of the speed's divergence per substep (:1613-1621) */
+  const double con1 = 0.05;
+  for (int k = nz; k >= 1; k--) {
+    double decfl = (WI(k + 1) - WI(k)) * dt * osteps / DZ(k);
+    if (decfl > con1) WI(k) = WI(k + 1) - con1 * DZ(k) * odt * (double)steps;
+  }
+  /* departure heights of the interfaces and the deformed cells (:1623-1636) */
+  for (int k = 1; k <= nz + 1; k++) ZA(k) = ZI(k) - WI(k) * dt * osteps;
+  ZA(nz + 2) = ZI(nz + 1);
+  for (int k = 1; k <= nz + 1; k++) DZA(k) = ZA(k + 1) - ZA(k);
+  for (int k = 1; k <= nz; k++) QA(k) = XR(k) * DZ(k) / DZA(k);
+  QA(nz + 1) = 0.0;
+  /* interface values with the reference's monotonicity test (:1638-1659) */
+  for (int k = 2; k <= nz; k++) {
+    double dip = (QA(k + 1) - QA(k)) / (DZA(k + 1) + DZA(k));
+    double dim = (QA(k) - QA(k - 1)) / (DZA(k - 1) + DZA(k));
+    if (dip * dim <= 0.0) {
+      QMI(k) = QA(k);
+      QPI(k) = QA(k);
+    } else {
+      QPI(k) = QA(k) + 0.5 * (dip + dim) * DZA(k);
+      QMI(k) = 2.0 * QA(k) - QPI(k);
+      if (QPI(k) > 0.0 || QMI(k) < 0.0) {
+        QPI(k) = QA(k);
+        QMI(k) = QA(k);
+      }
+    }
+  }
+  QPI(1) = QA(1);
+  QMI(1) = QA(1);
+  QMI(nz + 1) = QA(nz + 1);
+  QPI(nz + 1) = QA(nz + 1);
+  /* remap onto the regular cells (:1661-1723) */
+  int kb = 1, kt = 1;
+  for (int k = 1; k <= nz; k++) {
+    kb = imax(kb - 1, 1);
+    kt = imax(kt - 1, 1);
+    if (ZI(k) >= ZA(nz + 1)) break;
+    for (int kk = kb; kk <= nz; kk++)
+      if (ZI(k) <= ZA(kk + 1)) {
+        kb = kk;
+        break;
+      }
+    for (int kk = kt; kk <= nz + 2; kk++)
+      if (ZI(k + 1) <= ZA(kk)) {
+        kt = kk;
+        break;
+      }
+    kt = kt - 1;
+    if (kt == kb) {
+      double tl = (ZI(k) - ZA(kb)) / DZA(kb);
+      double th = (ZI(k + 1) - ZA(kb)) / DZA(kb);
+      double tl2 = tl * tl, th2 = th * th;
+      double qqd = 0.5 * (QPI(kb) - QMI(kb));
+      double qqh = qqd * th2 + QMI(kb) * th;
+      double qql = qqd * tl2 + QMI(kb) * tl;
+      XR(k) = (qqh - qql) / (th - tl);
+    } else if (kt > kb) {
+      double tl = (ZI(k) - ZA(kb)) / DZA(kb);
+      double tl2 = tl * tl;
+      double qqd = 0.5 * (QPI(kb) - QMI(kb));
+      double qql = qqd * tl2 + QMI(kb) * tl;
+      double dql = QA(kb) - qql;
+      double zsum = (1.0 - tl) * DZA(kb);
+      double qsum = dql * DZA(kb);
+      if (kt - kb > 1)
+        for (int m = kb + 1; m <= kt - 1; m++) {
+          zsum = zsum + DZA(m);
+          qsum = qsum + QA(m) * DZA(m);
+        }
+      double th = (ZI(k + 1) - ZA(kt)) / DZA(kt);
+      double th2 = th * th;
+      qqd = 0.5 * (QPI(kt) - QMI(kt));
+      double dqh = qqd * th2 + QMI(kt) * th;
+      zsum = zsum + th * DZA(kt);
+      qsum = qsum + dqh * DZA(kt);
+      XR(k) = qsum / zsum;
+    }
+    double orho = 1.0 / rho[k - 1];
+    XR(k) = fmax2(XR(k), limit);
+    xten[k - 1] = xten[k - 1] + (XR(k) - rr_save_[k - 1]) * orho * odt;
+  }
+  /* mass through the surface (:1725-1739) */
+  for (int k = 1; k <= nz; k++) {
+    if (ZA(k) < 0.0 && ZA(k + 1) <= 0.0) {
+      if (precip) *precip = *precip + QA(k) * DZA(k);
+    } else if (ZA(k) < 0.0 && ZA(k + 1) > 0.0) {
+      double th = (0.0 - ZA(k)) / DZA(k);
+      double th2 = th * th;
+      double qqd = 0.5 * (QPI(k) - QMI(k));
+      double qqh = qqd * th2 + QMI(k) * th;
+      if (precip) *precip = *precip + qqh * DZA(k);
+      break;
+    }
+  }
+#undef ZI
+#undef WI
+#undef DZA
+#undef ZA
+#undef QA
+#undef QMI
+#undef QPI
+#undef VT
+#undef DZ
+#undef XR
+}
+
+/* rain_fallspeed (main:1752-1790); substeps and ktop optional (NULL = absent) */
 static void rain_fallspeed(int nz, const double *rhof, const double *rr, const double *ilamr,
                            const double *dz1d, double *vt, double *vtn, int *substeps, int *ktop,
                            double dt) {
-  *ktop = 1;
-  *substeps = 1;
+  if (ktop) *ktop = 1;
+  if (substeps) *substeps = 1;
   for (int k = nz - 1; k >= 0; k--) {
     if (rr[k] > r1) {
       double lamr = 1.0 / ilamr[k];
@@ -656,21 +799,21 @@ static void rain_fallspeed(int nz, const double *rhof, const double *rr, const d
       vtn[k] = vtn[k + 1];
     }
     if (fmax2(vt[k], vtn[k]) > 1.e-3) {
-      *ktop = imax(*ktop, k + 1);
+      if (ktop) *ktop = imax(*ktop, k + 1);
       double dz_by_vt = dz1d[k] / fmax2(vt[k], vtn[k]);
-      *substeps = imax(*substeps, int_tie(dt / dz_by_vt + 1.0, *substeps));
+      if (substeps) *substeps = imax(*substeps, int_tie(dt / dz_by_vt + 1.0, *substeps));
     }
   }
-  if (*ktop == nz) *ktop = nz - 1;
+  if (ktop && *ktop == nz) *ktop = nz - 1;
 }
 
-/* graupel_fallspeed (main:1793-1848); hail_vol = present(qb1d) */
+/* graupel_fallspeed (main:1793-1848); hail_vol = present(qb1d); substeps and ktop optional */
 static void graupel_fallspeed(int nz, const double *rhof, const double *rho, const double *visco,
                               const double *rg, const double *rb, int hail_vol, const int *idx,
                               const double *ilamg, const double *dz1d, double *vt, double *vtn,
                               int *substeps, int *ktop, double dt) {
-  *ktop = 1;
-  *substeps = 1;
+  if (ktop) *ktop = 1;
+  if (substeps) *substeps = 1;
   for (int k = nz - 1; k >= 0; k--) {
     if (rg[k] > r1) {
       double afall, bfall;
@@ -690,12 +833,12 @@ static void graupel_fallspeed(int nz, const double *rhof, const double *rho, con
       vtn[k] = vtn[k + 1];
     }
     if (vt[k] > 1.e-3) {
-      *ktop = imax(*ktop, k + 1);
+      if (ktop) *ktop = imax(*ktop, k + 1);
       double dz_by_vt = dz1d[k] / vt[k];
-      *substeps = imax(*substeps, int_tie(dt / dz_by_vt + 1.0, *substeps));
+      if (substeps) *substeps = imax(*substeps, int_tie(dt / dz_by_vt + 1.0, *substeps));
     }
   }
-  if (*ktop == nz) *ktop = nz - 1;
+  if (ktop && *ktop == nz) *ktop = nz - 1;
 }
 
 /* snow_fallspeed (main:1851-1906) */
@@ -1825,11 +1968,29 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
   for (k = 0; k < nz; k++) any |= w->l_qr[k];
   if (any) {
     rain_fallspeed(nz, w->rhof, w->rr, w->ilamr, dz1d, w->vtrr, w->vtnr, &steps, &ktop, dt);
-    md->substeps[0] = steps;
-    for (int n = 1; n <= steps; n++) {
-      sedimentation(nz, w->rr, w->vtrr, dz1d, w->rho, w->qrten, r1, steps, ktop, &md->rain_precip,
-                    dt, w->sed_r);
-      sedimentation(nz, w->nr, w->vtnr, dz1d, w->rho, w->nrten, r2, steps, ktop, NULL, dt, w->sed_r);
+    if (cfg->semi_sedi_flag) { /* :599-613 */
+      steps = imax((int)(steps / semi_sedi_factor) + 1, 1);
+      md->substeps[0] = steps;
+      for (int n = 1; n <= steps; n++) {
+        semilagrangian_sedimentation(nz, dz1d, w->rho, w->rr, w->qrten, w->vtrr, steps, r1,
+                                     &md->rain_precip, dt, odt);
+        semilagrangian_sedimentation(nz, dz1d, w->rho, w->nr, w->nrten, w->vtnr, steps, r2, NULL,
+                                     dt, odt);
+        memset(w->vtrr, 0, sizeof(double) * (nz + 1));
+        memset(w->vtnr, 0, sizeof(double) * (nz + 1));
+        memcpy(w->xrx, qr1d, sizeof(double) * nz);
+        memcpy(w->xnx, nr1d, sizeof(double) * nz);
+        rain_check_and_update(nz, w->rho, w->l_qr, w->xrx, w->xnx, w->rr, w->nr, w->qrten,
+                              w->nrten, w->ilamr, w->mvd_r, dt, odt);
+        rain_fallspeed(nz, w->rhof, w->rr, w->ilamr, dz1d, w->vtrr, w->vtnr, NULL, NULL, dt);
+      }
+    } else {
+      md->substeps[0] = steps;
+      for (int n = 1; n <= steps; n++) {
+        sedimentation(nz, w->rr, w->vtrr, dz1d, w->rho, w->qrten, r1, steps, ktop, &md->rain_precip,
+                      dt, w->sed_r);
+        sedimentation(nz, w->nr, w->vtnr, dz1d, w->rho, w->nrten, r2, steps, ktop, NULL, dt, w->sed_r);
+      }
     }
   }
   any = 0;
@@ -1837,13 +1998,40 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
   if (any) {
     graupel_fallspeed(nz, w->rhof, w->rho, w->visco, w->rg, w->rb, qb1d != NULL, w->idx_bg,
                       w->ilamg, dz1d, w->vtrg, w->vtng, &steps, &ktop, dt);
-    md->substeps[1] = steps;
-    for (int n = 1; n <= steps; n++) {
-      sedimentation(nz, w->rg, w->vtrg, dz1d, w->rho, w->qgten, r1, steps, ktop,
-                    &md->graupel_liquid_equiv_precip, dt, w->sed_r);
-      sedimentation(nz, w->ng, w->vtng, dz1d, w->rho, w->ngten, r2, steps, ktop, NULL, dt, w->sed_r);
-      sedimentation(nz, w->rb, w->vtrg, dz1d, w->rho, w->qbten, meters3_to_liters * r1 / RHO_G(nrhg),
-                    steps, ktop, NULL, dt, w->sed_r);
+    if (cfg->semi_sedi_flag) { /* :640-671 */
+      steps = imax((int)(steps / semi_sedi_factor) + 1, 1);
+      md->substeps[1] = steps;
+      for (int n = 1; n <= steps; n++) {
+        semilagrangian_sedimentation(nz, dz1d, w->rho, w->rg, w->qgten, w->vtrg, steps, r1,
+                                     &md->graupel_liquid_equiv_precip, dt, odt);
+        semilagrangian_sedimentation(nz, dz1d, w->rho, w->ng, w->ngten, w->vtng, steps, r2, NULL,
+                                     dt, odt);
+        semilagrangian_sedimentation(nz, dz1d, w->rho, w->rb, w->qbten, w->vtrg, steps,
+                                     meters3_to_liters * r1 / RHO_G(nrhg), NULL, dt, odt);
+        memset(w->vtrg, 0, sizeof(double) * (nz + 1));
+        memset(w->vtng, 0, sizeof(double) * (nz + 1));
+        memcpy(w->xrx, qg1d, sizeof(double) * nz);
+        double *xngx = NULL, *xqbx = NULL;
+        if (hail_ng_qb) {
+          memcpy(w->xngx, ng1d, sizeof(double) * nz);
+          memcpy(w->xqbx, qb1d, sizeof(double) * nz);
+          xngx = w->xngx;
+          xqbx = w->xqbx;
+        }
+        graupel_check_and_update(nz, w->rho, w->l_qg, w->xrx, xngx, xqbx, w->rg, w->ng, w->rb,
+                                 w->idx_bg, w->qgten, w->ngten, w->qbten, w->ilamg, w->mvd_g, dt, odt);
+        graupel_fallspeed(nz, w->rhof, w->rho, w->visco, w->rg, w->rb, qb1d != NULL, w->idx_bg,
+                          w->ilamg, dz1d, w->vtrg, w->vtng, NULL, NULL, dt);
+      }
+    } else {
+      md->substeps[1] = steps;
+      for (int n = 1; n <= steps; n++) {
+        sedimentation(nz, w->rg, w->vtrg, dz1d, w->rho, w->qgten, r1, steps, ktop,
+                      &md->graupel_liquid_equiv_precip, dt, w->sed_r);
+        sedimentation(nz, w->ng, w->vtng, dz1d, w->rho, w->ngten, r2, steps, ktop, NULL, dt, w->sed_r);
+        sedimentation(nz, w->rb, w->vtrg, dz1d, w->rho, w->qbten, meters3_to_liters * r1 / RHO_G(nrhg),
+                      steps, ktop, NULL, dt, w->sed_r);
+      }
     }
   }
   any = 0;
@@ -1937,7 +2125,7 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
   (void)jme;
   if (cfg->ml_for_nc_flag && !nc) return -3;
   if (qc_bl && qcfrac_bl) return -3;
-  if (cfg->semi_sedi_flag || cfg->refl10cm_from_melting_flag) return -3;
+  if (cfg->refl10cm_from_melting_flag) return -3;
   if (!t && !(th && pii)) return -2;
   int nz = kte - kts + 1;
   long ni_ = ime - ims + 1, nk_ = kme - kms + 1;

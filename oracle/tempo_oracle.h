@@ -22,7 +22,8 @@
  *                                     (without melting), max_hail_diam :398-438,
  *                                     freezing_rain :441-456
  *   src/module_mp_tempo_main.F90    : tempo_main :73-864 and every routine it calls,
- *                                     except semilagrangian_sedimentation and the ML path
+ *                                     semilagrangian_sedimentation :1562-1749 included;
+ *                                     the ML path excepted
  *   src/module_mp_tempo_driver.F90  : tempo_run :187-513, read_table_* :532-649
  *   src/module_mp_tempo_tables.F90  : qr_acr_qs :493-621, qr_acr_qg :624-714,
  *                                     freezewater :717-805, write_table_* :96-444
@@ -126,7 +127,7 @@ void oracle_snow_moments(double rs, double tc, double out[10]);
  * NULL means "optional argument not present".  bounds = ids,ide,jds,jde,kds,kde,
  * ims,ime,jms,jme,kms,kme,its,ite,jts,jte,kts,kte.  Columns run in parallel on
  * `nthreads` OpenMP threads (<=0: all).  Returns 0, or a negative code for
- * unsupported optional paths (ML, semi-Lagrangian, melting radar). */
+ * unsupported optional paths (ML, melting radar). */
 int oracle_run(const ocfg_t *cfg, double dt, int itimestep,
                double *t, double *th, const double *pii, const double *p, const double *w,
                const double *dz, double *qv, double *qc, double *qr, double *qi, double *qs,

@@ -371,8 +371,6 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
     return fail(TEMPO_ERR_ARG, "a required array (p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr) is NULL");
   if (!A.t && !(A.th && A.pii))
     return fail(TEMPO_ERR_ARG, "tempo_run requires either t or th and pii");
-  if (cfg->semi_sedi_flag)
-    return fail(TEMPO_ERR_UNSUPPORTED, "semi-Lagrangian sedimentation is not part of this build");
   if (cfg->refl10cm_from_melting_flag)
     return fail(TEMPO_ERR_UNSUPPORTED, "melting-layer reflectivity is not part of this build");
   if (cfg->ml_for_nc_flag && !A.nc)
@@ -395,6 +393,7 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
   if (cfg->cloud_number_mixing_ratio_flag) f |= F_NCMR;
   if (A.t) f |= F_USE_T;
   if (dt > timestep_conversion_rime_to_rain) f |= F_DT_RIME;
+  if (cfg->semi_sedi_flag) f |= F_SEMI;
 
   a = StepArgs<S>{};
   a.t = A.t;
@@ -478,7 +477,10 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   const size_t pm_bytes = al(nzs * npad);
   const size_t cm_bytes = al(npad);
   const size_t hg_bytes = al(nzs * npad * rsz);
-  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes + 256;
+  // semi-Lagrangian work rows (island type, 8 bytes) only on that path
+  const size_t sl_bytes = (a.flags & F_SEMI) ? al((size_t)kSlRows * (nzs + 2) * npad * 8) : 0;
+  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes +
+                       sl_bytes + 256;
   if (int rc = ensure_scratch(c, total)) return rc;
   char* sp = (char*)c->scratch;
   a.sd = sp;
@@ -495,6 +497,8 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   sp += cm_bytes;
   a.hgt = sp;
   sp += hg_bytes;
+  a.slw = sl_bytes ? sp : nullptr;
+  sp += sl_bytes;
   a.nact = (unsigned int*)sp;
   a.stats = c->d_stats;
   c->last_cols = a.ncol;
@@ -566,6 +570,9 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
                     cudaStream_t s) {
   StepArgs<float> a;
   if (int rc = build_args(c, cfg, dt, itimestep, A, b, dg, a)) return rc;
+  if (a.flags & F_SEMI)
+    return fail(TEMPO_ERR_UNSUPPORTED, "semi-Lagrangian sedimentation needs work space beyond the fixed "
+                "scratch of tempo_run_dev_f32_noalloc_c: call tempo_run_dev_f32_c");
   if (c->precision != TEMPO_PREC_MIXED)
     return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
   const size_t npad = (size_t)a.ncol_pad, nzs = (size_t)a.nz;
@@ -1104,6 +1111,8 @@ int tl_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, temp
   const RunArrays<T> X = arrays_of<T>(x);
   StepArgs<T> ap;
   if (int rc = build_args(c, cfg, dt, itimestep, X, b, dgs, ap)) return rc;
+  if (ap.flags & F_SEMI)
+    return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation are not part of this build");
   if (cfg->max_hail_diameter_flag) ap.mhd_sfc = ap.mhd_col = nullptr;  // not differentiable
   CUDA_TRY(cudaSetDevice(c->device));
   DevBufs B;
@@ -1141,6 +1150,8 @@ int adjoint_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep,
   const RunArrays<T> X = arrays_of<T>(x);
   StepArgs<T> ap;
   if (int rc = build_args(c, cfg, dt, itimestep, X, b, nullptr, ap)) return rc;
+  if (ap.flags & F_SEMI)
+    return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation are not part of this build");
   CUDA_TRY(cudaSetDevice(c->device));
   DevBufs B;
   using D1 = Dual<T, 1>;

@@ -49,7 +49,10 @@ cudaError_t launch_step(const StepArgs<S>& a, const TempoConsts<Cst<R>>& c, cons
   cudaError_t e = points();
   if (e != cudaSuccess) return e;
   if (ev) record_event(ev[2], s);
-  tempo_sedim_kernel<R, S><<<gcol, kBlock, 0, s>>>(a);
+  if (a.flags & F_SEMI)
+    tempo_sedim_semi_kernel<R, S><<<gcol, kBlock, 0, s>>>(a, c, ci);
+  else
+    tempo_sedim_kernel<R, S><<<gcol, kBlock, 0, s>>>(a);
   if (ev) record_event(ev[3], s);
   tempo_final_kernel<R, S><<<gpts, kBlock, 0, s>>>(a, c, ci);
   if (ev) record_event(ev[4], s);

@@ -583,11 +583,143 @@ __global__ void __launch_bounds__(128, points_min_blocks(V)) tempo_points_kernel
 // ---------------------------------------------------------------------------------
 // sedim: phase B for one active column
 // ---------------------------------------------------------------------------------
-template <class R, class S>
-__global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant__ StepArgs<S> a) {
+// semilagrangian_sedimentation (main:1562-1749), the scheme of Juang and Hong (2010),
+// Mon. Wea. Rev. 138, 1778-1791, on one column: x and ten are level planes (stride ls),
+// vt the filled speeds (vt(nz + 1) = 0), w the column's work rows (row stride wr, level
+// stride wl).  Indices below are the reference's, 1-based.
+template <class R, class I, class S>
+__device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dzp, long NI,
+                         const I* rho, I* w, long wr, long wl, int steps, double limit, I* precip,
+                         I dt, I odt) {
+  auto row = [&](int r, int i) -> I& { return w[(long)r * wr + (long)(i - 1) * wl]; };
+  auto ZI = [&](int i) -> I& { return row(0, i); };
+  auto WI = [&](int i) -> I& { return row(1, i); };
+  auto ZA = [&](int i) -> I& { return row(2, i); };
+  auto DZA = [&](int i) -> I& { return row(3, i); };
+  auto QA = [&](int i) -> I& { return row(4, i); };
+  auto QMI = [&](int i) -> I& { return row(5, i); };
+  auto QPI = [&](int i) -> I& { return row(6, i); };
+  auto X0 = [&](int i) -> I& { return row(7, i); };
+  auto VT = [&](int i) -> I { return i <= nz ? I(vt[(long)(i - 1) * ls]) : I(0.0); };
+  auto DZ = [&](int i) -> I { return ldi<I>(dzp + (long)(i - 1) * NI); };
+  auto XR = [&](int i) -> I& { return x[(long)(i - 1) * ls]; };
+  const I osteps = 1.0 / I(steps), fsteps = I(steps);
+  for (int k = 1; k <= nz; k++) X0(k) = XR(k);
+  ZI(1) = I(0.0);
+  for (int k = 1; k <= nz; k++) ZI(k + 1) = ZI(k) + DZ(k);
+  // 3rd-order interpolation of the interface speeds (:1599-1611)
+  const I fa1 = I(9.0 / 16.0), fa2 = I(1.0 / 16.0);
+  WI(1) = VT(1);
+  WI(2) = 0.5 * (VT(2) + VT(1));
+  for (int k = 3; k <= nz - 1; k++) WI(k) = fa1 * (VT(k) + VT(k - 1)) - fa2 * (VT(k + 1) + VT(k - 2));
+  WI(nz) = 0.5 * (VT(nz) + VT(nz - 1));
+  WI(nz + 1) = VT(nz + 1);
+  for (int k = 2; k <= nz; k++)
+    if (VT(k) == 0.0) WI(k) = VT(k - 1);
+  // limit of the speed's divergence per substep (:1613-1621)
+  const I con1 = I(0.05);
+  for (int k = nz; k >= 1; k--) {
+    const I decfl = (WI(k + 1) - WI(k)) * dt * osteps / DZ(k);
+    if (decfl > con1) WI(k) = WI(k + 1) - con1 * DZ(k) * odt * fsteps;
+  }
+  // departure heights of the interfaces and the deformed cells (:1623-1636)
+  for (int k = 1; k <= nz + 1; k++) ZA(k) = ZI(k) - WI(k) * dt * osteps;
+  ZA(nz + 2) = ZI(nz + 1);
+  for (int k = 1; k <= nz + 1; k++) DZA(k) = ZA(k + 1) - ZA(k);
+  for (int k = 1; k <= nz; k++) QA(k) = XR(k) * DZ(k) / DZA(k);
+  QA(nz + 1) = I(0.0);
+  // interface values with the reference's monotonicity test (:1638-1659)
+  for (int k = 2; k <= nz; k++) {
+    const I dip = (QA(k + 1) - QA(k)) / (DZA(k + 1) + DZA(k));
+    const I dim = (QA(k) - QA(k - 1)) / (DZA(k - 1) + DZA(k));
+    if (dip * dim <= 0.0) {
+      QMI(k) = QA(k);
+      QPI(k) = QA(k);
+    } else {
+      QPI(k) = QA(k) + 0.5 * (dip + dim) * DZA(k);
+      QMI(k) = 2.0 * QA(k) - QPI(k);
+      if (QPI(k) > 0.0 || QMI(k) < 0.0) {
+        QPI(k) = QA(k);
+        QMI(k) = QA(k);
+      }
+    }
+  }
+  QPI(1) = QA(1);
+  QMI(1) = QA(1);
+  QMI(nz + 1) = QA(nz + 1);
+  QPI(nz + 1) = QA(nz + 1);
+  // remap onto the regular cells (:1661-1723)
+  int kb = 1, kt = 1;
+  for (int k = 1; k <= nz; k++) {
+    kb = max(kb - 1, 1);
+    kt = max(kt - 1, 1);
+    if (ZI(k) >= ZA(nz + 1)) break;
+    for (int kk = kb; kk <= nz; kk++)
+      if (ZI(k) <= ZA(kk + 1)) {
+        kb = kk;
+        break;
+      }
+    for (int kk = kt; kk <= nz + 2; kk++)
+      if (ZI(k + 1) <= ZA(kk)) {
+        kt = kk;
+        break;
+      }
+    kt = kt - 1;
+    if (kt == kb) {
+      const I tl = (ZI(k) - ZA(kb)) / DZA(kb);
+      const I th = (ZI(k + 1) - ZA(kb)) / DZA(kb);
+      const I tl2 = tl * tl, th2 = th * th;
+      const I qqd = 0.5 * (QPI(kb) - QMI(kb));
+      const I qqh = qqd * th2 + QMI(kb) * th;
+      const I qql = qqd * tl2 + QMI(kb) * tl;
+      XR(k) = (qqh - qql) / (th - tl);
+    } else if (kt > kb) {
+      const I tl = (ZI(k) - ZA(kb)) / DZA(kb);
+      const I tl2 = tl * tl;
+      I qqd = 0.5 * (QPI(kb) - QMI(kb));
+      const I qql = qqd * tl2 + QMI(kb) * tl;
+      const I dql = QA(kb) - qql;
+      I zsum = (1.0 - tl) * DZA(kb);
+      I qsum = dql * DZA(kb);
+      if (kt - kb > 1)
+        for (int m = kb + 1; m <= kt - 1; m++) {
+          zsum = zsum + DZA(m);
+          qsum = qsum + QA(m) * DZA(m);
+        }
+      const I th = (ZI(k + 1) - ZA(kt)) / DZA(kt);
+      const I th2 = th * th;
+      qqd = 0.5 * (QPI(kt) - QMI(kt));
+      const I dqh = qqd * th2 + QMI(kt) * th;
+      zsum = zsum + th * DZA(kt);
+      qsum = qsum + dqh * DZA(kt);
+      XR(k) = qsum / zsum;
+    }
+    const I orho = 1.0 / rho[(long)(k - 1) * ls];
+    XR(k) = XR(k) > limit ? XR(k) : I(limit);
+    ten[(long)(k - 1) * ls] = ten[(long)(k - 1) * ls] + (XR(k) - X0(k)) * orho * odt;
+  }
+  // mass through the surface (:1725-1739)
+  for (int k = 1; k <= nz; k++) {
+    if (ZA(k) < 0.0 && ZA(k + 1) <= 0.0) {
+      if (precip) *precip = *precip + QA(k) * DZA(k);
+    } else if (ZA(k) < 0.0 && ZA(k + 1) > 0.0) {
+      const I th = (0.0 - ZA(k)) / DZA(k);
+      const I th2 = th * th;
+      const I qqd = 0.5 * (QPI(k) - QMI(k));
+      const I qqh = qqd * th2 + QMI(k) * th;
+      if (precip) *precip = *precip + qqh * DZA(k);
+      break;
+    }
+  }
+}
+
+// Phase B on the column of active slot s.  SEMI: rain and graupel by the
+// semi-Lagrangian scheme (semi_sedi_flag, main:599-613, 640-671), which rechecks the
+// species and recomputes their fall speeds after every substep (needs cst and ci).
+template <class R, class S, bool SEMI>
+__device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoConsts<Cst<R>>* cst,
+                                             const IslandConsts<Isl<R>>* ci, long s) {
   using I = Isl<R>;
-  const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= (long)*a.nact) return;
   const int nz = a.nz;
   const long NI = a.NI;
   const ColGeom g = col_geom(a, a.act[s]);
@@ -699,21 +831,110 @@ __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant_
   };
   int steps, ktop;
   unsigned sub[5] = {0, 0, 0, 0, 0};
+  // semi-Lagrangian path: one sweep on this column's work rows, and the level's state
+  // for the species checks (rhof and visco as after the last stage of phase A)
+  [[maybe_unused]] auto sl = [&](int fx, int ften, int fv, double limit, int st, I* precip) {
+    if constexpr (SEMI) {
+      const long cs2 = a.ncol_pad;
+      sl_sweep<R, I, S>(nz, sd + fx * fsd, sd + ften * fsd, sr + fv * fsd, kSlotTile, dzp, NI, rho,
+                        reinterpret_cast<I*>(a.slw) + s, (long)(nz + 2) * cs2, cs2, st, limit,
+                        precip, dti, I(a.odt));
+    }
+  };
+  [[maybe_unused]] auto level_state = [&](int k, Lev<R>& L) {
+    const long o = (long)k * kSlotTile, e = g.base + (long)k * NI;
+    L.cs = cst;
+    L.ci = ci;
+    L.rho = sd[SD_RHO * fsd + o];
+    const I t1d = (a.flags & F_USE_T) ? ldi<I>(a.t + e) : ldi<I>(a.th + e) * ldi<I>(a.pii + e);
+    L.temp = t1d + sd[SD_TTEN * fsd + o] * dti;
+    thermo_tail(L);
+  };
+  [[maybe_unused]] const R odt_r = step_odt<R>(a);
   if (any_qr) {
     fill(SR_VTR, SR_VTNR, true, false, steps, ktop);
-    sub[0] = steps;
-    for (int n = 0; n < steps; n++) {
-      sweep(SD_XRR, SD_TQR, SR_VTR, r1, steps, ktop, &prec_r);
-      sweep(SD_XNR, SD_TNR, SR_VTNR, r2, steps, ktop, nullptr);
+    if constexpr (SEMI) {
+      steps = max((int)(steps / 10.0) + 1, 1);  // semi_sedi_factor (main:595, 599)
+      sub[0] = steps;
+      for (int n = 0; n < steps; n++) {
+        sl(SD_XRR, SD_TQR, SR_VTR, r1, steps, &prec_r);
+        sl(SD_XNR, SD_TNR, SR_VTNR, r2, steps, nullptr);
+        // rain_check_and_update from qr1d, then rain_fallspeed without substeps
+        // (main:604-613), top down
+        R vup = R(0), vnup = R(0);
+        for (int k = nz - 1; k >= 0; k--) {
+          Lev<R> L;
+          level_state(k, L);
+          const long o = (long)k * kSlotTile, e = g.base + (long)k * NI;
+          const R tq = R(sd[SD_TQR * fsd + o]), tn = R(sd[SD_TNR * fsd + o]);
+          L.qrten = tq;
+          L.nrten = tn;
+          R q = R(a.qr[e]), nn = R(a.nr[e]);
+          rain_check(L, q, nn, dt, odt_r);
+          sd[SD_XRR * fsd + o] = I(L.rr);
+          sd[SD_XNR * fsd + o] = I(L.nr);
+          if (!(L.qrten == tq)) sd[SD_TQR * fsd + o] = I(L.qrten);
+          if (!(L.nrten == tn)) sd[SD_TNR * fsd + o] = I(L.nrten);
+          R v = vup, vn = vnup;
+          if (L.rr > R(r1)) rain_speeds(L, *cst, v, vn);
+          sr[SR_VTR * fsd + o] = v;
+          sr[SR_VTNR * fsd + o] = vn;
+          vup = v;
+          vnup = vn;
+        }
+      }
+    } else {
+      sub[0] = steps;
+      for (int n = 0; n < steps; n++) {
+        sweep(SD_XRR, SD_TQR, SR_VTR, r1, steps, ktop, &prec_r);
+        sweep(SD_XNR, SD_TNR, SR_VTNR, r2, steps, ktop, nullptr);
+      }
     }
   }
   if (any_qg) {
     fill(SR_VTG, SR_VTNG, false, false, steps, ktop);
-    sub[1] = steps;
-    for (int n = 0; n < steps; n++) {
-      sweep(SD_XRG, SD_TQG, SR_VTG, r1, steps, ktop, &prec_g);
-      sweep(SD_XNG, SD_TNG, SR_VTNG, r2, steps, ktop, nullptr);
-      sweep(SD_XRB, SD_TQB, SR_VTG, meters3_to_liters * r1 / rho_gd(nrhg), steps, ktop, nullptr);
+    if constexpr (SEMI) {
+      const bool hail = a.flags & F_HAIL;
+      steps = max((int)(steps / 10.0) + 1, 1);  // main:636, 640
+      sub[1] = steps;
+      for (int n = 0; n < steps; n++) {
+        sl(SD_XRG, SD_TQG, SR_VTG, r1, steps, &prec_g);
+        sl(SD_XNG, SD_TNG, SR_VTNG, r2, steps, nullptr);
+        sl(SD_XRB, SD_TQB, SR_VTG, meters3_to_liters * r1 / rho_gd(nrhg), steps, nullptr);
+        // graupel_check_and_update from qg1d (ng1d, qb1d), then graupel_fallspeed
+        // without substeps (main:651-667), top down
+        R vup = R(0), vnup = R(0);
+        for (int k = nz - 1; k >= 0; k--) {
+          Lev<R> L;
+          level_state(k, L);
+          const long o = (long)k * kSlotTile, e = g.base + (long)k * NI;
+          const R tq = R(sd[SD_TQG * fsd + o]), tn = R(sd[SD_TNG * fsd + o]), tb = R(sd[SD_TQB * fsd + o]);
+          L.qgten = tq;
+          L.ngten = tn;
+          L.qbten = tb;
+          R q = R(a.qg[e]), nn = hail ? R(a.ng[e]) : R(0), b = hail ? R(a.qb[e]) : R(0);
+          graupel_check(L, q, nn, b, hail, dt, odt_r);
+          sd[SD_XRG * fsd + o] = I(L.rg);
+          sd[SD_XNG * fsd + o] = I(L.ng);
+          sd[SD_XRB * fsd + o] = I(L.rb);
+          if (!(L.qgten == tq)) sd[SD_TQG * fsd + o] = I(L.qgten);
+          if (!(L.ngten == tn)) sd[SD_TNG * fsd + o] = I(L.ngten);
+          if (!(L.qbten == tb)) sd[SD_TQB * fsd + o] = I(L.qbten);
+          R v = vup, vn = vnup;
+          if (L.rg > R(r1)) graupel_speeds(L, *cst, a.flags, v, vn);
+          sr[SR_VTG * fsd + o] = v;
+          sr[SR_VTNG * fsd + o] = vn;
+          vup = v;
+          vnup = vn;
+        }
+      }
+    } else {
+      sub[1] = steps;
+      for (int n = 0; n < steps; n++) {
+        sweep(SD_XRG, SD_TQG, SR_VTG, r1, steps, ktop, &prec_g);
+        sweep(SD_XNG, SD_TNG, SR_VTNG, r2, steps, ktop, nullptr);
+        sweep(SD_XRB, SD_TQB, SR_VTG, meters3_to_liters * r1 / rho_gd(nrhg), steps, ktop, nullptr);
+      }
     }
   }
   if (any_qs) {
@@ -751,6 +972,22 @@ __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant_
   sc[SC_PS * cs] = prec_s;
   sc[SC_PI * cs] = prec_i;
   sc[SC_PC * cs] = prec_c;
+}
+
+template <class R, class S>
+__global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant__ StepArgs<S> a) {
+  const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= (long)*a.nact) return;
+  sedim_column<R, S, false>(a, nullptr, nullptr, s);
+}
+// phase B with semi-Lagrangian rain and graupel (F_SEMI), one thread per active column
+template <class R, class S>
+__global__ void __launch_bounds__(128) tempo_sedim_semi_kernel(const __grid_constant__ StepArgs<S> a,
+                                                               const __grid_constant__ TempoConsts<Cst<R>> cst,
+                                                               const __grid_constant__ IslandConsts<Isl<R>> ci) {
+  const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= (long)*a.nact) return;
+  sedim_column<R, S, true>(a, &cst, &ci, s);
 }
 
 // non-negative value into a running maximum (IEEE order of non-negative floats is the

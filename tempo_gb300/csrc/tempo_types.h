@@ -44,7 +44,8 @@ enum : uint32_t {
   F_COND = 1u << 8,     // cloud_condensation_flag
   F_REFL = 1u << 9, F_RE = 1u << 10, F_MHD = 1u << 11, F_MVDR = 1u << 12,
   F_MVDG = 1u << 13, F_NCMR = 1u << 14, F_USE_T = 1u << 15,
-  F_DT_RIME = 1u << 16  // dt > timestep_conversion_rime_to_rain
+  F_DT_RIME = 1u << 16,  // dt > timestep_conversion_rime_to_rain
+  F_SEMI = 1u << 17      // semi_sedi_flag: semi-Lagrangian rain and graupel sedimentation
 };
 
 // per-point scratch fields in the island type (thermodynamic and sedimentation islands)
@@ -102,6 +103,7 @@ struct StepArgs {
   uint8_t* pmask;     // plane: species present at the point after phase A
   uint8_t* cmask;     // [ncol_pad]
   unsigned long long* stats;  // [0] early exits, [1..5] max substeps
+  void* slw;          // Isl<R>[kSlRows][nz + 2][ncol_pad]: semi-Lagrangian work rows (F_SEMI)
 };
 
 // Inputs of a point that carry derivatives in the tangent-linear and adjoint kernels
@@ -139,6 +141,8 @@ struct AdjArgs {
 // entries (within one memory page), so a column's levels never spread over the whole
 // plane.
 constexpr int kSlotTile = 32;
+// work rows of the semi-Lagrangian sweep per column (zi, wi, za, dza, qa, qmi, qpi, x0)
+constexpr int kSlRows = 8;
 TG_HD inline long pt_base(long s, int nz) { return (s / kSlotTile) * (long)nz * kSlotTile + (s % kSlotTile); }
 TG_HD inline long pt_off(long s, int k, int nz) { return pt_base(s, nz) + (long)k * kSlotTile; }
 

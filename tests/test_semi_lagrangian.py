@@ -1,0 +1,122 @@
+"""Semi-Lagrangian sedimentation of rain and graupel (semi_sedi_flag,
+src/module_mp_tempo_main.F90:595-671, scheme :1562-1749).
+
+The reference's tests run this path without assertions, so parity rests on the oracle's
+restatement: the GPU FP64 step against the oracle to 1e-12 (with the hail-aware
+density-class ties handled as in the explicit-path tests), and on the CPU the property
+that the flag changes only columns where rain or graupel sediment."""
+import numpy as np
+import pytest
+
+from parity_util import compare, compare_with_ties, run_gpu, run_oracle, worst
+
+TOL64 = 1e-12
+SEMI = dict(hailaware_flag=0, semi_sedi_flag=1)
+
+
+def test_oracle_semi_changes_only_rain_and_graupel_columns(oracle_mod):
+    from tempo_gb300 import workloads as W
+    oracle_mod.init(False)
+    wl = W.config1(ni=32, nj=8, steps=1, dt=60.0)
+    fe, de = run_oracle(oracle_mod, dict(hailaware_flag=0), wl)
+    fs, ds = run_oracle(oracle_mod, SEMI, wl)
+    moving = np.zeros(wl.fields["p"].shape[::2], bool)
+    for k in ("qr", "qg"):
+        moving |= (fe[k] > 1e-12).any(axis=1) | (wl.fields[k] > 1e-12).any(axis=1)
+    assert moving.any() and (~moving).any()
+    for k in ("t", "qv", "qc", "qr", "nr", "qi", "ni", "qs", "qg"):
+        a, b = fe[k].transpose(0, 2, 1)[~moving], fs[k].transpose(0, 2, 1)[~moving]
+        assert np.array_equal(a, b), k
+        assert np.isfinite(fs[k]).all(), k
+    # the scheme moves rain: the two paths differ where rain falls
+    assert not np.array_equal(fe["qr"], fs["qr"])
+    assert (ds["rain_precip"] >= 0).all()
+    oracle_mod.init(True)
+
+
+@pytest.mark.gpu
+def test_semi_fp64_matches_oracle(ctx_nohail, oracle_mod):
+    from tempo_gb300 import workloads as W
+    oracle_mod.init(False)
+    wl = W.config1(ni=64, nj=8, steps=2, dt=60.0)
+    state = {k: v.copy() for k, v in wl.fields.items()}
+    for step in (1, 2):
+        fo, do = run_oracle(oracle_mod, SEMI, wl, fields=state, itimestep=step)
+        fg, dg = run_gpu(ctx_nohail, SEMI, wl, fields=state, itimestep=step)
+        name, e = worst(compare(fg, dg, fo, do))
+        assert e < TOL64, (step, name, e)
+        state = fo
+    oracle_mod.init(True)
+
+
+@pytest.mark.gpu
+def test_semi_hail_fp64_matches_oracle(ctx_hail, oracle_mod):
+    from tempo_gb300 import workloads as W
+    oracle_mod.init(True)
+    wl = W.config2(ni=32, nj=16, dt=60.0)
+    over = dict(hailaware_flag=1, semi_sedi_flag=1, rain_med_vol_diam_flag=1,
+                graupel_med_vol_diam_flag=1)
+    ties = np.zeros(wl.fields["p"].shape[::2], np.int32)
+    fo, do = run_oracle(oracle_mod, over, wl, ties=ties)
+    fg, dg = run_gpu(ctx_hail, over, wl)
+    # same criteria as the explicit hail-aware parity test (test_gpu_parity.py)
+    clean, b2, moved, which, frac = compare_with_ties(fg, dg, fo, do, ties, TOL64,
+                                                      inputs=wl.fields)
+    assert clean < 1e-10, (which, clean)
+    assert frac <= 1e-3, (frac, which, clean)
+    assert b2 < 1e-10, b2
+    assert moved <= max(1, ties.size // 100), moved
+
+
+@pytest.mark.gpu
+def test_semi_mixed_close_to_fp64(tg, ctx_nohail):
+    """The mixed form against the FP64 step on the same (FP32-representable) inputs: the
+    semi-Lagrangian remap switches between reconstructions at thresholds (its
+    monotonicity tests), so its pointwise error fractions may exceed the explicit
+    path's, but by a bounded factor; column precipitation agrees to 1e-4."""
+    from copy import copy
+    from tempo_gb300 import workloads as W
+    wl = copy(W.config1(ni=64, nj=8, steps=1, dt=60.0))
+    wl.fields = {k: v.astype(np.float32).astype(np.float64) for k, v in wl.fields.items()}
+
+    def fractions(over):
+        f64, d64 = run_gpu(ctx_nohail, over, wl)
+        ctx_nohail.set_precision(tg.PREC_MIXED)
+        try:
+            f32, d32 = run_gpu(ctx_nohail, over, wl, dtype=np.float32)
+        finally:
+            ctx_nohail.set_precision(tg.PREC_FP64)
+        out = {}
+        for k in ("t", "qv", "qr", "nr"):
+            floor = 1e-6 if k == "nr" else 1e-12
+            scale = np.maximum(np.abs(f64[k]), np.maximum(np.abs(wl.fields[k]), floor))
+            out[k] = float(np.mean(np.abs(f32[k].astype(np.float64) - f64[k]) / scale > 1e-5))
+        p32, p64 = d32["rain_precip"].astype(np.float64), d64["rain_precip"]
+        out["precip"] = float(np.max(np.abs(p32 - p64) / np.maximum(p64, 1e-3 * p64.max() + 1e-30)))
+        return out
+
+    explicit = fractions(dict(hailaware_flag=0))
+    semi = fractions(SEMI)
+    for k in ("t", "qv", "qr", "nr"):
+        assert semi[k] <= max(5 * explicit[k], 0.05), (k, semi, explicit)
+    assert semi["precip"] < 1e-4, (semi, explicit)
+
+
+@pytest.mark.gpu
+def test_semi_rejected_where_unsupported(tg, ctx_nohail):
+    torch = pytest.importorskip("torch")
+    from tempo_gb300 import workloads as W
+    wl = W.config1(ni=8, nj=4, steps=1, dt=60.0)
+    f = {k: torch.tensor(v, device="cuda") for k, v in wl.fields.items()}
+    cfg = tg.default_cfgs(hailaware_flag=0, semi_sedi_flag=1)
+    with pytest.raises(tg.TempoError) as e:
+        ctx_nohail.tl_device(f, {}, wl.dt, 1, cfgs=cfg)
+    assert e.value.code == -2
+    f32 = {k: v.float() for k, v in f.items()}
+    ctx_nohail.set_precision(tg.PREC_MIXED)
+    try:
+        with pytest.raises(tg.TempoError) as e:
+            ctx_nohail.run_device_noalloc(f32, wl.dt, 1, cfgs=cfg)
+        assert e.value.code == -2
+    finally:
+        ctx_nohail.set_precision(tg.PREC_FP64)
