@@ -332,7 +332,7 @@ def main():
     for _ in range(max(args.warmup - 1, 1)):
         ctx.run_device(f32, args.dt, it, diags=diag)
         it += 1
-    variant, variant_ms = ctx.autotune_device(f32, args.dt, it, diags=diag, reps=3)
+    variant, variant_ms = ctx.autotune_device(f32, args.dt, it, diags=diag, reps=6)
     ctx.set_kernel_timing(True)
     ctx.set_graphs(True)
     ctx.run_device(f32, args.dt, it, diags=diag)
