@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-multi", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--ref-columns", type=int, default=131072,
                     help="columns per step of the reference arm's bounded sample")
@@ -246,6 +247,46 @@ def adjoint_timing(ctx, tg, W, torch, device, reps=3):
     return out
 
 
+def multi_domain(ctx, tg, W, torch, device, steps=2):
+    """The uneven multi-domain batch: 24 domains with log-uniform column counts
+    (1e3 .. 5e5), 50 to 128 levels and dt of 10 to 60 s (seeded descriptors), the large
+    tables rebuilt on the GPU first.  One batch step runs every domain's step on the
+    same stream; ms from CUDA events, value = all domains' columns x steps / time."""
+    doms = W.config4_domains(seed=0)
+    table_ms = ctx.build_tables()
+    data = []
+    for d, (ncol, nz, dt, seed) in enumerate(doms):
+        f = W.config1_torch(seed=100 + d, ni=ncol, nj=1, nz=nz, device=device, dtype=torch.float32)
+        dg = {n: torch.zeros((1, ncol), device=device) for n in tg.DIAG2}
+        dg.update({n: torch.zeros((1, nz, ncol), device=device)
+                   for n in ("refl10cm", "re_cloud", "re_ice", "re_snow")})
+        data.append((f, dg, dt))
+    ncols = sum(d[0] for d in doms)
+    ctx.set_graphs(False)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def batch(it):
+        for f, dg, dt in data:
+            ctx.run_device(f, dt, it, diags=dg)
+
+    batch(1)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for it in range(2, 2 + steps):
+        batch(it)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    del data
+    torch.cuda.empty_cache()
+    return {"workload": "24 domains, columns log-uniform in [1e3, 5e5], nz in {50, 65, 90, 128}, "
+                        "dt in {10, 20, 30, 60} s, mixed precision, tables rebuilt first",
+            "domains": [{"columns": n, "levels": z, "dt": t} for n, z, t, _ in doms],
+            "columns": ncols, "table_build_ms": table_ms, "steps": steps,
+            "ms_per_batch_step": ms, "value": ncols / (ms / 1e3), "unit": "column-steps/s"}
+
+
 def run_reference(args, rank, world):
     """The reference arm: the FP64 CPU restatement on all host cores (the Fortran
     reference has no compiler on either machine), W untimed and K timed steps, each
@@ -412,6 +453,14 @@ def main():
         except Exception as e:  # reported beside the headline, never required
             adjoint = {"error": str(e)}
 
+    multi = None
+    if not args.no_multi:
+        try:
+            ctx.set_precision(tg.PREC_MIXED)
+            multi = multi_domain(ctx, tg, W, torch, f"cuda:{local}")
+        except Exception as e:  # reported beside the headline, never required
+            multi = {"error": str(e)}
+
     pk = peaks()
     hbm = pk.get("hbm_gbs")
     peak_src = "measured" if hbm else "fallback"
@@ -442,6 +491,7 @@ def main():
                      "kernel_ms": kms,
                      "kernel_share": {k: v / step_kernel_ms for k, v in kms.items()}},
         "adjoint": adjoint,
+        "multi_domain": multi,
         "gpu_launches": args.steps * stats.get("launches", 1),
         "clocks": clocks,
         "step_stats": stats,
