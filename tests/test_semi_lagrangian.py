@@ -48,12 +48,29 @@ def _fractions_over(fa, da, fb, db, tol, inputs):
 
 
 # The remap decides by comparisons of departure heights with cell edges and by the
-# sign tests of its monotonicity limiter; where the interpolated interface speed is a
-# cancellation near zero (the top of a rain layer), a last-bit difference between the
-# device's and glibc's pow in the fall speeds can flip such a decision, which moves
-# that level's value by O(1).  FP64 parity is therefore stated as: all but a small
-# fraction of points within 1e-12 of the oracle.
-SEMI_FRACTION = 2e-3
+# sign tests of its monotonicity limiter, so last-bit differences (the device's and
+# glibc's pow in the fall speeds) flip some decisions and move those levels' values by
+# O(1).  The oracle shows the same behaviour against itself: perturbing its inputs in
+# the last bit changes a fraction of its semi-Lagrangian outputs beyond 1e-12 (and none
+# of the explicit path's rain).  FP64 parity is stated against that calibration: per
+# field, the fraction of points beyond 1e-12 from the oracle is at most three times the
+# oracle's own last-bit fraction, or 1e-3.
+def _self_fraction(oracle_mod, over, wl, state=None, itimestep=1):
+    from copy import copy
+    base = state if state is not None else wl.fields
+    rng = np.random.default_rng(17)
+    w2 = copy(wl)
+    w2.fields = {k: (v * (1 + 2e-16 * rng.standard_normal(v.shape))
+                     if k in ("t", "qv", "qc", "qr", "nr", "qg", "qs") else v.copy())
+                 for k, v in base.items()}
+    fa, da = run_oracle(oracle_mod, over, wl, fields=base, itimestep=itimestep)
+    fb, db = run_oracle(oracle_mod, over, w2, itimestep=itimestep)
+    return _fractions_over(fb, db, fa, da, TOL64, base)
+
+
+def _check_calibrated(frac, calib):
+    bad = {k: (v, calib.get(k, 0.0)) for k, v in frac.items() if v > max(3 * calib.get(k, 0.0), 1e-3)}
+    assert not bad, bad
 
 
 @pytest.mark.gpu
@@ -63,11 +80,10 @@ def test_semi_fp64_matches_oracle(ctx_nohail, oracle_mod):
     wl = W.config1(ni=64, nj=8, steps=2, dt=60.0)
     state = {k: v.copy() for k, v in wl.fields.items()}
     for step in (1, 2):
+        calib = _self_fraction(oracle_mod, SEMI, wl, state, step)
         fo, do = run_oracle(oracle_mod, SEMI, wl, fields=state, itimestep=step)
         fg, dg = run_gpu(ctx_nohail, SEMI, wl, fields=state, itimestep=step)
-        frac = _fractions_over(fg, dg, fo, do, TOL64, state)
-        bad = {k: v for k, v in frac.items() if v > SEMI_FRACTION}
-        assert not bad, (step, bad)
+        _check_calibrated(_fractions_over(fg, dg, fo, do, TOL64, state), calib)
         state = fo
     oracle_mod.init(True)
 
@@ -79,16 +95,14 @@ def test_semi_hail_fp64_matches_oracle(ctx_hail, oracle_mod):
     wl = W.config2(ni=32, nj=16, dt=60.0)
     over = dict(hailaware_flag=1, semi_sedi_flag=1, rain_med_vol_diam_flag=1,
                 graupel_med_vol_diam_flag=1)
+    calib = _self_fraction(oracle_mod, over, wl)
     ties = np.zeros(wl.fields["p"].shape[::2], np.int32)
     fo, do = run_oracle(oracle_mod, over, wl, ties=ties)
     fg, dg = run_gpu(ctx_hail, over, wl)
-    # columns with a density-class rounding tie (as in the explicit hail-aware test)
-    # aside, the fraction criterion of the semi-Lagrangian path
+    # columns with a density-class rounding tie (as in the explicit hail-aware test) aside
     keep = (ties & 3) == 0
     sub = lambda d: {k: (v.transpose(0, 2, 1)[keep] if v.ndim == 3 else v[keep]) for k, v in d.items()}
-    frac = _fractions_over(sub(fg), sub(dg), sub(fo), sub(do), TOL64, sub(wl.fields))
-    bad = {k: v for k, v in frac.items() if v > SEMI_FRACTION}
-    assert not bad, bad
+    _check_calibrated(_fractions_over(sub(fg), sub(dg), sub(fo), sub(do), TOL64, sub(wl.fields)), calib)
     assert keep.mean() > 0.9
 
 
