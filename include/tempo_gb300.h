@@ -230,11 +230,11 @@ int tempo_kernel_times_c(tempo_ctx_t *ctx, float ms[4]);
  * every variant of its per-level kernel (thread-to-work mapping and register budget) it
  * copies the given state and runs `reps` consecutive steps (itimestep, itimestep + 1,
  * ...) on the copy -- the caller's arrays are not modified -- timing the per-level
- * kernel with CUDA events on `stream`, and keeps the variant with the smallest sum for
- * later TEMPO_PREC_MIXED runs on FP32 storage.  Tune on a state like the ones the runs
- * will see: the work of a step depends on the state it starts from.  Arguments as
- * tempo_run_dev_f32_c; times_ms (optional, `count` entries) receives each variant's
- * summed time, *chosen (optional) the variant kept.  Needs device memory for a copy of
+ * kernel with CUDA events on `stream`, and keeps the variant with the smallest median
+ * step time for later TEMPO_PREC_MIXED runs on FP32 storage.  Tune on a state like the
+ * ones the runs will see: the work of a step depends on the state it starts from.
+ * Arguments as tempo_run_dev_f32_c; times_ms (optional, `count` entries) receives each
+ * variant's median time, *chosen (optional) the variant kept.  Needs device memory for a copy of
  * every array the step writes. */
 int tempo_autotune_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float dt,
                              int itimestep, float *t, float *th, const float *pii,

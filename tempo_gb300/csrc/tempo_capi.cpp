@@ -952,7 +952,10 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, 
   float best = 0.0f;
   int best_v = saved_variant;
   // every variant runs the same `reps` consecutive steps from a fresh copy of the state
-  // (the work of a step depends on the state it starts from) and is scored by their sum
+  // (the work of a step depends on the state it starts from) and is scored by the
+  // median of its per-step times (single steps of a workload can cost far more than
+  // the others, and by amounts that vary from run to run)
+  std::vector<float> per_step((size_t)reps);
   for (int v = 0; v < kPointsVariants && rc == TEMPO_OK; v++) {
     c->points_variant = v;
     float vbest = 0.0f;
@@ -965,7 +968,12 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, 
       rc = run_dev(c, cfg, (double)dt, itimestep + r, A, b, diags ? &dcopy : nullptr, s);
       float ms[kStepLaunches];
       if (rc == TEMPO_OK) rc = tempo_kernel_times_c(c, ms);
-      if (rc == TEMPO_OK) vbest += ms[1];
+      if (rc == TEMPO_OK) per_step[(size_t)r] = ms[1];
+    }
+    if (rc == TEMPO_OK) {
+      std::sort(per_step.begin(), per_step.end());
+      vbest = (reps % 2) ? per_step[(size_t)reps / 2]
+                         : 0.5f * (per_step[(size_t)reps / 2 - 1] + per_step[(size_t)reps / 2]);
     }
     if (rc) break;
     if (times_ms && v < count) times_ms[v] = vbest;
