@@ -93,6 +93,10 @@ extern double nic1;
 extern double dc[nbc], dtc[nbc], di[nbi], dti[nbi], dr[nbr], dtr[nbr], ds[nbs], dts[nbs],
     dg[nbg], dtg[nbg], t_nc[nbc];
 extern double hbins[nhbins], dhbins[nhbins];
+/* radar bins of melting snow and graupel (initialize_bins_for_radar, params:674-692) */
+#define radar_bins 50
+extern double sbins_radar[radar_bins], dsbins_radar[radar_bins], gbins_radar[radar_bins],
+    dgbins_radar[radar_bins];
 
 /* Fortran-order tables (column-major, 1-based accessors below) */
 extern double *t_efrw, *t_efsw;             /* (nbr|nbs, nbc) */

@@ -68,6 +68,8 @@ double nic1;
 double dc[nbc], dtc[nbc], di[nbi], dti[nbi], dr[nbr], dtr[nbr], ds[nbs], dts[nbs], dg[nbg],
     dtg[nbg], t_nc[nbc];
 double hbins[nhbins], dhbins[nhbins];
+double sbins_radar[radar_bins], dsbins_radar[radar_bins], gbins_radar[radar_bins],
+    dgbins_radar[radar_bins];
 
 double *t_efrw, *t_efsw, *tpc_wev, *tnc_wev;
 float *tnccn_act;
@@ -566,6 +568,9 @@ int oracle_init(int hailaware_flag) {
   compute_drop_evap();
   qi_aut_qs();
   create_bins(nhbins, 500.e-6, 0.075, hbins, dhbins); /* initialize_bins_for_hail_size */
+  /* initialize_bins_for_radar (params:674-692): snow 100 um to 2 cm, graupel to 5 cm */
+  create_bins(radar_bins, 100.e-6, 0.02, sbins_radar, dsbins_radar);
+  create_bins(radar_bins, 100.e-6, 0.05, gbins_radar, dgbins_radar);
   g_initialized = 1;
   return 0;
 }

@@ -5,6 +5,7 @@
  * module_mp_tempo_driver.F90 tempo_run (:187-513).  Levels are 0-based here
  * (k0 = k-1); every comment cites the Fortran line it restates.
  */
+#include <complex.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -1688,28 +1689,199 @@ static void effective_radius(ws_t *w, double *re_qc, double *re_qi, double *re_q
   }
 }
 
-/* reflectivity_10cm without melting (diags:59-121) */
-static void reflectivity_10cm(ws_t *w, double *dbz) {
+/* complex_water_ray (diags:144-173): refractive index of water after Ray (1972), Appl.
+ * Opt. 11, 1836, for temperature t (Celsius) and wavelength lambda (m) */
+static double complex complex_water_ray(double lambda, double t) {
+  double epsinf = 5.27137 + 0.02164740 * t - 0.00131198 * t * t;
+  double epss = 78.54 * (1.0 - 4.579e-3 * (t - 25.0) + 1.190e-5 * (t - 25.0) * (t - 25.0) -
+                         2.800e-8 * (t - 25.0) * (t - 25.0) * (t - 25.0));
+  double alpha = -16.8129 / (t + 273.16) + 0.0609265;
+  double lambdas = 0.00033836 * exp(2513.98 / (t + 273.16)) * 1e-2;
+  double nenner = 1.0 + 2.0 * pow(lambdas / lambda, 1.0 - alpha) * sin(alpha * pi * 0.5) +
+                  pow(lambdas / lambda, 2.0 - 2.0 * alpha);
+  double epsr = epsinf + ((epss - epsinf) * (pow(lambdas / lambda, 1.0 - alpha) *
+                                                 sin(alpha * pi * 0.5) + 1.0)) / nenner;
+  double epsi = ((epss - epsinf) * (pow(lambdas / lambda, 1.0 - alpha) * cos(alpha * pi * 0.5) +
+                                    0.0)) / nenner + lambda * 1.25664 / 1.88496;
+  return csqrt(CMPLX(epsr, -epsi));
+}
+
+/* complex_ice_maetzler (diags:176-203): refractive index of ice after Maetzler (1998) */
+static double complex complex_ice_maetzler(double lambda, double t) {
+  double c = 2.99e8, tk = t + 273.16, f = c / lambda * 1e-9;
+  double b1 = 0.0207, b2 = 1.16e-11, b = 335.0;
+  double deltabeta = exp(-10.02 + 0.0364 * (tk - 273.16));
+  double e = exp(b / tk) - 1.0;
+  double betam = (b1 / tk) * (exp(b / tk) / (e * e)) + b2 * f * f;
+  double beta = betam + deltabeta;
+  double theta = 300.0 / tk - 1.0;
+  double alfa = (0.00504 + 0.0062 * theta) * exp(-22.1 * theta);
+  double complex ri = 3.1884 + 9.1e-4 * (tk - 273.16);
+  ri = ri + CMPLX(0.0, (alfa / f + beta * f));
+  return csqrt(conj(ri));
+}
+
+/* rayleigh_soak_wetgraupel (diags:311-394): backscatter cross section of a wet snow or
+ * graupel particle of mass x_g, Maxwell-Garnett mixing and the Rayleigh approximation */
+static double rayleigh_soak_wetgraupel(double x_g, double a_geo, double b_geo, double fmelt,
+                                       double lambda_radar, double meltratio_outside,
+                                       double complex m_w, double complex m_i) {
+  double complex m_air = CMPLX(1.0, 0.0);
+  double fm = fmax2(fmin2(fmelt, 1.0), 0.0);
+  double mra = fmax2(fmin2(meltratio_outside, 1.0), 0.0);
+  mra = mra + (1.0 - mra) * fm;
+  double x_w = x_g * fm;
+  double d_g = a_geo * pow(x_g, b_geo);
+  if (!(d_g >= r1)) return 0.0;
+  double vg = pi / 6.0 * d_g * d_g * d_g;
+  double rhog = fmax2(fmin2(x_g / vg, 900.0), 10.0);
+  vg = x_g / rhog;
+  double meltratio_outside_grenz = 1.0 - rhog / 1000.0;
+  double volg;
+  if (mra <= meltratio_outside_grenz) {
+    volg = vg * (1.0 - mra * fm);
+  } else {
+    double fmgrenz = (900.0 - rhog) / (mra * 900.0 - rhog + 900.0 * rhog / 1000.0);
+    if (fm <= fmgrenz)
+      volg = (1.0 - mra * fm) * vg;
+    else
+      volg = (x_g - x_w) / 900.0 + x_w / 1000.0;
+  }
+  double d_large = pow(6.0 / pi * volg, 1.0 / 3.0);
+  double volice = (x_g - x_w) / (volg * 900.0);
+  double volwater = x_w / (1000.0 * volg);
+  double volair = 1.0 - volice - volwater;
+  double volmix1 = volice / fmax2(volice + volwater, 1e-10);
+  double volmix2 = 1.0 - volmix1;
+  (void)volmix2;
+  /* ice in water */
+  double complex m1t = m_w * m_w, m2t = m_air * m_air, m3t = m_i * m_i;
+  double vol2 = 0.0, vol3 = volmix1;
+  double complex beta2 = 2.0 * m1t / (m2t - m1t) * (m2t / (m2t - m1t) * clog(m2t / m1t) - 1.0);
+  double complex beta3 = 2.0 * m1t / (m3t - m1t) * (m3t / (m3t - m1t) * clog(m3t / m1t) - 1.0);
+  double complex m_tmp = csqrt(((1.0 - vol2 - vol3) * m1t + vol2 * beta2 * m2t + vol3 * beta3 * m3t) /
+                               (1.0 - vol2 - vol3 + vol2 * beta2 + vol3 * beta3));
+  /* air in the mixture */
+  m1t = m_tmp * m_tmp;
+  m2t = m_air * m_air;
+  m3t = (2.0 * m_air) * (2.0 * m_air);
+  vol2 = volair;
+  vol3 = 0.0;
+  beta2 = 2.0 * m1t / (m2t - m1t) * (m2t / (m2t - m1t) * clog(m2t / m1t) - 1.0);
+  beta3 = 2.0 * m1t / (m3t - m1t) * (m3t / (m3t - m1t) * clog(m3t / m1t) - 1.0);
+  double complex m_core = csqrt(((1.0 - vol2 - vol3) * m1t + vol2 * beta2 * m2t + vol3 * beta3 * m3t) /
+                                (1.0 - vol2 - vol3 + vol2 * beta2 + vol3 * beta3));
+  double kk = cabs((m_core * m_core - 1.0) / (m_core * m_core + 2.0));
+  double d6 = ipow(d_large, 6);
+  return kk * kk * pi * pi * pi * pi * pi * d6 /
+         (lambda_radar * lambda_radar * lambda_radar * lambda_radar);
+}
+
+/* Simpson weights over the radar bins (diags:224-231) */
+static void simpson_weights(double *simpson) {
+  const double basis[3] = {1.0 / 3.0, 4.0 / 3.0, 1.0 / 3.0};
+  for (int n = 0; n < radar_bins + 1; n++) simpson[n] = 0.0;
+  for (int n = 1; n <= radar_bins - 1; n += 2) {
+    simpson[n - 1] += basis[0];
+    simpson[n] += basis[1];
+    simpson[n + 1] += basis[2];
+  }
+}
+
+/* reflectivity_from_melting_graupel (diags:206-248) */
+static double reflectivity_from_melting_graupel(double rg, double ng, double ilamg, int idx,
+                                                double rr) {
+  const double melt_outside = 0.9, lambda_radar = 0.10;
+  double simpson[radar_bins + 1];
+  simpson_weights(simpson);
+  double complex m_w_0 = complex_water_ray(lambda_radar, 0.0);
+  double complex m_i_0 = complex_ice_maetzler(lambda_radar, 0.0);
+  double kw1 = cabs((m_w_0 * m_w_0 - 1.0) / (m_w_0 * m_w_0 + 2.0));
+  double k_w = kw1 * kw1;
+  double sr = fmax2(0.01, fmin2(1.0 - rg / fmax2(rg + rr, r1), 0.99));
+  double fmelt = sr * sr;
+  double eta = 0.0;
+  double lamg = 1.0 / ilamg;
+  double n0_g = ng * ogg2 * pow(lamg, CGE(2, 1));
+  for (int n = 0; n < radar_bins; n++) {
+    double mass = AM_G(idx) * pow(gbins_radar[n], bm_g);
+    double backscatter = rayleigh_soak_wetgraupel(mass, OCMG(idx), obmg, fmelt, lambda_radar,
+                                                  melt_outside, m_w_0, m_i_0);
+    double f_d = n0_g * pow(gbins_radar[n], mu_g) * exp(-lamg * gbins_radar[n]);
+    eta = eta + f_d * backscatter * simpson[n] * dgbins_radar[n];
+  }
+  return lambda_radar * lambda_radar * lambda_radar * lambda_radar / (pi * pi * pi * pi * pi * k_w) * eta;
+}
+
+/* reflectivity_from_melting_snow (diags:251-308) */
+static double reflectivity_from_melting_snow(double rs, double smob, double smoc, double rr) {
+  const double melt_outside = 0.9, lambda_radar = 0.10;
+  double simpson[radar_bins + 1];
+  simpson_weights(simpson);
+  double complex m_w_0 = complex_water_ray(lambda_radar, 0.0);
+  double complex m_i_0 = complex_ice_maetzler(lambda_radar, 0.0);
+  double kw1 = cabs((m_w_0 * m_w_0 - 1.0) / (m_w_0 * m_w_0 + 2.0));
+  double k_w = kw1 * kw1;
+  double sr = fmax2(0.01, fmin2(1.0 - rs / (rs + rr), 0.99));
+  double fmelt = sr * sr;
+  double eta = 0.0;
+  double om3 = 1.0 / smoc;
+  double m0 = smob * om3;
+  double mrat = smob * m0 * m0 * m0;
+  double slam1 = m0 * lam0, slam2 = m0 * lam1;
+  for (int n = 0; n < radar_bins; n++) {
+    double mass = am_s * pow(sbins_radar[n], bm_s);
+    double backscatter = rayleigh_soak_wetgraupel(mass, ocms, obms, fmelt, lambda_radar,
+                                                  melt_outside, m_w_0, m_i_0);
+    double f_d = mrat * (kap0 * exp(-slam1 * sbins_radar[n]) +
+                         kap1 * pow(m0 * sbins_radar[n], mu_s) * exp(-slam2 * sbins_radar[n]));
+    eta = eta + f_d * backscatter * simpson[n] * dsbins_radar[n];
+  }
+  return lambda_radar * lambda_radar * lambda_radar * lambda_radar / (pi * pi * pi * pi * pi * k_w) * eta;
+}
+
+/* find_melting_level (diags:124-141); 1-based level, 1 = none found */
+static int find_melting_level(const ws_t *w) {
+  int nz = w->nz, k_melt = 1;
+  for (int k = nz - 1; k >= 1; k--) /* reference k = nz-1 .. 1 */
+    if (w->temp[k - 1] > t0 && w->l_qr[k - 1] && (w->l_qs[k] || w->l_qg[k])) {
+      k_melt = imax(k + 1, k_melt);
+      break;
+    }
+  return k_melt;
+}
+
+/* reflectivity_10cm (diags:59-121), with the melting contributions of snow and graupel
+ * below the melting level when `melting` */
+static void reflectivity_10cm(ws_t *w, double *dbz, int melting) {
   int nz = w->nz;
+  int k_melt = melting ? find_melting_level(w) : 1;
   for (int k = 0; k < nz; k++) {
     w->ze_r[k] = 1.e-22;
     w->ze_s[k] = 1.e-22;
     w->ze_g[k] = 1.e-22;
   }
   for (int k = nz - 1; k >= 0; k--) {
+    const int kf = k + 1; /* the reference's level index */
+    const int melt_here = melting && k_melt > 2 && kf < k_melt - 1;
     dbz[k] = -35.0;
     if (w->l_qr[k]) {
       double lamr = 1.0 / w->ilamr[k];
       double n0_r = w->nr[k] * org2 * pow(lamr, CRE(2));
       w->ze_r[k] = n0_r * CRG(4) * pow(w->ilamr[k], CRE(4));
     }
-    if (w->l_qs[k])
+    if (w->l_qs[k]) {
       w->ze_s[k] = (0.176 / 0.93) * (6.0 / pi) * (6.0 / pi) * (am_s / 900.0) * (am_s / 900.0) * w->smoz[k];
+      if (melt_here)
+        w->ze_s[k] = reflectivity_from_melting_snow(w->rs[k], w->smob[k], w->smoc[k], w->rr[k]);
+    }
     if (w->l_qg[k]) {
       int ig = w->idx_bg[k];
       double n0_g = w->ng[k] * ogg2 * pow(1.0 / w->ilamg[k], CGE(2, 1));
       w->ze_g[k] = (0.176 / 0.93) * (6.0 / pi) * (6.0 / pi) * (AM_G(ig) / 900.0) * (AM_G(ig) / 900.0) *
                    n0_g * CGG(4, 1) * pow(w->ilamg[k], CGE(4, 1));
+      if (melt_here)
+        w->ze_g[k] = reflectivity_from_melting_graupel(w->rg[k], w->ng[k], w->ilamg[k], ig, w->rr[k]);
     }
     dbz[k] = fmax2(-35.0, 10.0 * log10((w->ze_r[k] + w->ze_s[k] + w->ze_g[k]) * 1.e18));
   }
@@ -2103,7 +2275,7 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
   if (co->mvd_g)
     for (k = 0; k < nz; k++) co->mvd_g[k] = w->mvd_g[k];
   if (co->mhd) max_hail_diam(w, co->mhd);
-  if (co->refl) reflectivity_10cm(w, co->refl);
+  if (co->refl) reflectivity_10cm(w, co->refl, cfg->refl10cm_from_melting_flag);
   if (co->re_c) effective_radius(w, co->re_c, co->re_i, co->re_s);
 }
 
@@ -2125,7 +2297,6 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
   (void)jme;
   if (cfg->ml_for_nc_flag && !nc) return -3;
   if (qc_bl && qcfrac_bl) return -3;
-  if (cfg->refl10cm_from_melting_flag) return -3;
   if (!t && !(th && pii)) return -2;
   int nz = kte - kts + 1;
   long ni_ = ime - ims + 1, nk_ = kme - kms + 1;
