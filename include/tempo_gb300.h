@@ -27,7 +27,8 @@ extern "C" {
 typedef enum {
   TEMPO_OK = 0,
   TEMPO_ERR_ARG = -1,         /* NULL required pointer, bad bounds, dt <= 0, ... */
-  TEMPO_ERR_UNSUPPORTED = -2, /* optional path outside this build (ML, melting radar; semi-Lagrangian derivatives) */
+  TEMPO_ERR_UNSUPPORTED = -2, /* optional path outside this build (ML; derivatives of the
+                                 semi-Lagrangian and melting-layer paths) */
   TEMPO_ERR_TABLE = -3,       /* missing, truncated or malformed lookup table */
   TEMPO_ERR_CUDA = -4,        /* CUDA runtime failure (message has the CUDA error string) */
   TEMPO_ERR_NOMEM = -5,       /* host or device allocation failed */

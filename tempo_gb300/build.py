@@ -33,6 +33,7 @@ UNITS = [
     ("tempo_deriv_f64.cu", ["-fmad=false"], "tempo_deriv_f64"),
     ("tempo_deriv_f32.cu", [], "tempo_deriv_f32"),
     ("tempo_noalloc.cu", [], "tempo_noalloc"),
+    ("tempo_melt.cu", ["-fmad=false"], "tempo_melt"),
 ]
 HOST_UNITS = ["tempo_capi.cpp", "tempo_host_init.cpp"]
 

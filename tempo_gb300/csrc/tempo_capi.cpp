@@ -98,6 +98,7 @@ struct tempo_ctx {
   bool kernel_timing = false;
   cudaEvent_t kev[kStepLaunches + 1] = {};
   int points_variant = 0;  // mixed form on FP32 storage (tempo_autotune_dev_f32_c)
+  RadarConsts radar{};     // melting-layer reflectivity (FP64)
   bool use_graphs = false;
   std::vector<GraphEntry> graphs;  // captured steps, oldest first
 };
@@ -371,8 +372,6 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
     return fail(TEMPO_ERR_ARG, "a required array (p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr) is NULL");
   if (!A.t && !(A.th && A.pii))
     return fail(TEMPO_ERR_ARG, "tempo_run requires either t or th and pii");
-  if (cfg->refl10cm_from_melting_flag)
-    return fail(TEMPO_ERR_UNSUPPORTED, "melting-layer reflectivity is not part of this build");
   if (cfg->ml_for_nc_flag && !A.nc)
     return fail(TEMPO_ERR_UNSUPPORTED, "ML cloud-number prediction is not part of this build");
   uint32_t f = 0;
@@ -394,6 +393,7 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
   if (A.t) f |= F_USE_T;
   if (dt > timestep_conversion_rime_to_rain) f |= F_DT_RIME;
   if (cfg->semi_sedi_flag) f |= F_SEMI;
+  if (cfg->refl10cm_from_melting_flag && cfg->refl10cm_flag && dg && dg->refl10cm) f |= F_MELT;
 
   a = StepArgs<S>{};
   a.t = A.t;
@@ -479,8 +479,10 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   const size_t hg_bytes = al(nzs * npad * rsz);
   // semi-Lagrangian work rows (island type, 8 bytes) only on that path
   const size_t sl_bytes = (a.flags & F_SEMI) ? al((size_t)kSlRows * (nzs + 2) * npad * 8) : 0;
+  // melting-reflectivity record of phase C only on that path
+  const size_t ml_bytes = (a.flags & F_MELT) ? al((size_t)kMeltN * nzs * npad * 8 + nzs * npad) : 0;
   const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes +
-                       sl_bytes + 256;
+                       sl_bytes + ml_bytes + 256;
   if (int rc = ensure_scratch(c, total)) return rc;
   char* sp = (char*)c->scratch;
   a.sd = sp;
@@ -499,6 +501,8 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   sp += hg_bytes;
   a.slw = sl_bytes ? sp : nullptr;
   sp += sl_bytes;
+  a.mlw = ml_bytes ? sp : nullptr;
+  sp += ml_bytes;
   a.nact = (unsigned int*)sp;
   a.stats = c->d_stats;
   c->last_cols = a.ncol;
@@ -516,16 +520,19 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
       if constexpr (sizeof(S) == sizeof(double)) {
         Tables<double> T{c->t64.t_efrw, c->t64.t_efsw, c->t64.tnc_wev, c->t64.tps_iaus, c->t64.tni_iaus,
                          c->t64.tpi_ide, c->t64.tnccn, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
-        return launch_step_f64(a, T, c->c64, c->i64, st, ev);
+        e = launch_step_f64(a, T, c->c64, c->i64, st, ev);
+        return e == cudaSuccess ? launch_melt_refl(a, c->c64, c->radar, st) : e;
       }
       return cudaErrorInvalidValue;
     }
     Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
                     c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
     if constexpr (sizeof(S) == sizeof(double))
-      return launch_step_mixed_f64(a, T, c->c32, c->idf, st, ev);
+      e = launch_step_mixed_f64(a, T, c->c32, c->idf, st, ev);
     else
-      return launch_step_mixed_f32(a, T, c->c32, c->idf, st, ev, c->points_variant);
+      e = launch_step_mixed_f32(a, T, c->c32, c->idf, st, ev, c->points_variant);
+    // the melting-layer reflectivity pass (F_MELT) after phase C, outside the timed kernels
+    return e == cudaSuccess ? launch_melt_refl(a, c->c64, c->radar, st) : e;
   };
   if (!c->use_graphs) {
     CUDA_TRY(enqueue(s));
@@ -570,9 +577,10 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
                     cudaStream_t s) {
   StepArgs<float> a;
   if (int rc = build_args(c, cfg, dt, itimestep, A, b, dg, a)) return rc;
-  if (a.flags & F_SEMI)
-    return fail(TEMPO_ERR_UNSUPPORTED, "semi-Lagrangian sedimentation needs work space beyond the fixed "
-                "scratch of tempo_run_dev_f32_noalloc_c: call tempo_run_dev_f32_c");
+  if (a.flags & (F_SEMI | F_MELT))
+    return fail(TEMPO_ERR_UNSUPPORTED, "semi-Lagrangian sedimentation and the melting-layer reflectivity "
+                "need work space beyond the fixed scratch of tempo_run_dev_f32_noalloc_c: call "
+                "tempo_run_dev_f32_c");
   if (c->precision != TEMPO_PREC_MIXED)
     return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
   const size_t npad = (size_t)a.ncol_pad, nzs = (size_t)a.nz;
@@ -774,6 +782,7 @@ int tempo_init_c(const int* aerosolaware_flag, const int* hailaware_flag, const 
   narrow_consts(c->c64, &c->c32);
   make_island_consts(c->c64, &c->i64);
   make_island_consts(c->c64, &c->idf);
+  make_radar_consts(&c->radar);
   make_bins(&c->bins);
   int rc;
   if ((rc = alloc_tables(c))) return bail(rc);
@@ -1119,8 +1128,9 @@ int tl_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, temp
   const RunArrays<T> X = arrays_of<T>(x);
   StepArgs<T> ap;
   if (int rc = build_args(c, cfg, dt, itimestep, X, b, dgs, ap)) return rc;
-  if (ap.flags & F_SEMI)
-    return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation are not part of this build");
+  if (ap.flags & (F_SEMI | F_MELT))
+    return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation and of the "
+                "melting-layer reflectivity are not part of this build");
   if (cfg->max_hail_diameter_flag) ap.mhd_sfc = ap.mhd_col = nullptr;  // not differentiable
   CUDA_TRY(cudaSetDevice(c->device));
   DevBufs B;
@@ -1158,8 +1168,9 @@ int adjoint_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep,
   const RunArrays<T> X = arrays_of<T>(x);
   StepArgs<T> ap;
   if (int rc = build_args(c, cfg, dt, itimestep, X, b, nullptr, ap)) return rc;
-  if (ap.flags & F_SEMI)
-    return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation are not part of this build");
+  if (ap.flags & (F_SEMI | F_MELT))
+    return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation and of the "
+                "melting-layer reflectivity are not part of this build");
   CUDA_TRY(cudaSetDevice(c->device));
   DevBufs B;
   using D1 = Dual<T, 1>;

@@ -78,6 +78,17 @@ struct TempoConsts {
 // Fills a double-precision constant set exactly as tempo_init does for the given
 // hail-aware flag (graupel vars, initialize_parameters, bins).  Host only.
 void make_consts(TempoConsts<double>* c, bool hailaware);
+// Melting-layer 10-cm reflectivity (diags:124-395), always evaluated in FP64: the
+// radar bins of snow and graupel (initialize_bins_for_radar, params:674-692) and the
+// refractive indices of water and ice at 0 C for a 10-cm wavelength with the
+// dielectric factor |K_w|^2 (complex_water_ray, complex_ice_maetzler).  Host only.
+constexpr int radar_bins = 50;
+struct RadarConsts {
+  double sbins[radar_bins], dsbins[radar_bins], gbins[radar_bins], dgbins[radar_bins];
+  double mw_re, mw_im, mi_re, mi_im, k_w;
+};
+void make_radar_consts(RadarConsts* r);
+
 // Narrows every member to float for the mixed-precision kernels.
 void narrow_consts(const TempoConsts<double>& d, TempoConsts<float>* f);
 

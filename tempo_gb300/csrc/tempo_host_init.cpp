@@ -6,6 +6,7 @@
 // and create_bins (:695-722).  Gamma values use the C library tgamma, the same
 // routine the Fortran GAMMA intrinsic calls under gfortran.
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -273,6 +274,49 @@ void narrow_consts(const TempoConsts<double>& d, TempoConsts<float>* f) {
   f->nic2 = d.nic2; f->nii2 = d.nii2; f->nii3 = d.nii3; f->nir2 = d.nir2; f->nir3 = d.nir3;
   f->nis2 = d.nis2; f->nig2 = d.nig2; f->nig3 = d.nig3; f->niin2 = d.niin2;
   f->dim_nrhg = d.dim_nrhg;
+}
+
+// refractive index of water after Ray (1972), Appl. Opt. 11, 1836 (diags:144-173)
+static std::complex<double> water_ray(double lambda, double t) {
+  const double pi_ = 3.1415926535897932384626434;
+  double epsinf = 5.27137 + 0.02164740 * t - 0.00131198 * t * t;
+  double epss = 78.54 * (1.0 - 4.579e-3 * (t - 25.0) + 1.190e-5 * (t - 25.0) * (t - 25.0) -
+                         2.800e-8 * (t - 25.0) * (t - 25.0) * (t - 25.0));
+  double alpha = -16.8129 / (t + 273.16) + 0.0609265;
+  double lambdas = 0.00033836 * std::exp(2513.98 / (t + 273.16)) * 1e-2;
+  double nenner = 1.0 + 2.0 * std::pow(lambdas / lambda, 1.0 - alpha) * std::sin(alpha * pi_ * 0.5) +
+                  std::pow(lambdas / lambda, 2.0 - 2.0 * alpha);
+  double epsr = epsinf + ((epss - epsinf) * (std::pow(lambdas / lambda, 1.0 - alpha) *
+                                                 std::sin(alpha * pi_ * 0.5) + 1.0)) / nenner;
+  double epsi = ((epss - epsinf) * (std::pow(lambdas / lambda, 1.0 - alpha) * std::cos(alpha * pi_ * 0.5) +
+                                    0.0)) / nenner + lambda * 1.25664 / 1.88496;
+  return std::sqrt(std::complex<double>(epsr, -epsi));
+}
+// refractive index of ice after Maetzler (1998) (diags:176-203)
+static std::complex<double> ice_maetzler(double lambda, double t) {
+  double c = 2.99e8, tk = t + 273.16, f = c / lambda * 1e-9;
+  double b1 = 0.0207, b2 = 1.16e-11, b = 335.0;
+  double deltabeta = std::exp(-10.02 + 0.0364 * (tk - 273.16));
+  double e = std::exp(b / tk) - 1.0;
+  double betam = (b1 / tk) * (std::exp(b / tk) / (e * e)) + b2 * f * f;
+  double beta = betam + deltabeta;
+  double theta = 300.0 / tk - 1.0;
+  double alfa = (0.00504 + 0.0062 * theta) * std::exp(-22.1 * theta);
+  std::complex<double> ri = 3.1884 + 9.1e-4 * (tk - 273.16);
+  ri = ri + std::complex<double>(0.0, (alfa / f + beta * f));
+  return std::sqrt(std::conj(ri));
+}
+
+void make_radar_consts(RadarConsts* r) {
+  create_bins(radar_bins, 100.e-6, 0.02, r->sbins, r->dsbins);
+  create_bins(radar_bins, 100.e-6, 0.05, r->gbins, r->dgbins);
+  const std::complex<double> mw = water_ray(0.10, 0.0), mi = ice_maetzler(0.10, 0.0);
+  r->mw_re = mw.real();
+  r->mw_im = mw.imag();
+  r->mi_re = mi.real();
+  r->mi_im = mi.imag();
+  const double kw1 = std::abs((mw * mw - 1.0) / (mw * mw + 2.0));
+  r->k_w = kw1 * kw1;
 }
 
 }  // namespace tg

@@ -64,6 +64,11 @@ struct DerivOps {
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
 cudaError_t noalloc_scratch(int device, void** ptr);
 
+// tempo_melt.cu: melting-layer reflectivity pass after phase C (F_MELT), FP64
+template <class S>
+cudaError_t launch_melt_refl(const StepArgs<S>& a, const TempoConsts<double>& c, const RadarConsts& rc,
+                             cudaStream_t s);
+
 // number of points-kernel variants of the mixed form on FP32 storage
 constexpr int kPointsVariants = 8;
 // kernels launched per step (prep, points, sedim, final)

@@ -855,10 +855,13 @@ __device__ void rain_evaporation(const Lev<R>& L, Tend<R>& t, R odt) {
 // ---------------------------------------------------------------------------------
 // diagnostics (diags.F90), one level
 // ---------------------------------------------------------------------------------
+// the three contributions to Ze without melting (diags:80-111)
 template <class R>
-__device__ R reflectivity_10cm(const Lev<R>& L) {  // diags:59-121 without melting
+__device__ void reflectivity_parts(const Lev<R>& L, R& ze_r, R& ze_s, R& ze_g) {
   const TempoConsts<Cst<R>>& c = *L.cs;
-  R ze_r = R(1.e-22), ze_s = R(1.e-22), ze_g = R(1.e-22);
+  ze_r = R(1.e-22);
+  ze_s = R(1.e-22);
+  ze_g = R(1.e-22);
   if (L.l_qr) {
     R lamr = R(1.0) / L.ilamr;
     R n0_r = L.nr * c.org2 * Pow(lamr, c.cre[1]);
@@ -873,6 +876,11 @@ __device__ R reflectivity_10cm(const Lev<R>& L) {  // diags:59-121 without melti
     ze_g = R(0.176 / 0.93) * (R(6.0) / R(pi)) * (R(6.0) / R(pi)) * (c.am_g[ig - 1] / R(900.0)) *
            (c.am_g[ig - 1] / R(900.0)) * n0_g * c.cgg[0][3] * Pow(L.ilamg, c.cge[0][3]);
   }
+}
+template <class R>
+__device__ R reflectivity_10cm(const Lev<R>& L) {  // diags:59-121 without melting
+  R ze_r, ze_s, ze_g;
+  reflectivity_parts(L, ze_r, ze_s, ze_g);
   return Max(R(-35.0), R(10.0) * Log10((ze_r + ze_s + ze_g) * R(1.e18)));
 }
 

