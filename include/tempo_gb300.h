@@ -27,8 +27,9 @@ extern "C" {
 typedef enum {
   TEMPO_OK = 0,
   TEMPO_ERR_ARG = -1,         /* NULL required pointer, bad bounds, dt <= 0, ... */
-  TEMPO_ERR_UNSUPPORTED = -2, /* optional path outside this build (ML; derivatives of the
-                                 semi-Lagrangian and melting-layer paths) */
+  TEMPO_ERR_UNSUPPORTED = -2, /* optional path outside this build (the ML boundary-layer
+                                 cloud path; derivatives of the semi-Lagrangian, melting-layer
+                                 and ML cloud-number paths) */
   TEMPO_ERR_TABLE = -3,       /* missing, truncated or malformed lookup table */
   TEMPO_ERR_CUDA = -4,        /* CUDA runtime failure (message has the CUDA error string) */
   TEMPO_ERR_NOMEM = -5,       /* host or device allocation failed */
@@ -270,6 +271,17 @@ int tempo_adjoint_dev_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double
                         const tempo_diags_t *lam_diags, int ims, int ime, int jms, int jme,
                         int kms, int kme, int its, int ite, int jts, int jte, int kts, int kte,
                         void *stream);
+
+/* The cloud-number network of the ML path, as init_ml_data stores it for the reference
+ * (src/module_mp_tempo_driver.F90:703-735, src/module_mp_tempo_ml.F90:33-98): input
+ * scaler means and variances (7 each; inputs qc, qr, qi, qs, p, T, w), weights00 (24 x 7,
+ * column-major as reshape(nc_ml_w00, [24, 7])), bias00 (24), weights01 (24), bias01 (1).
+ * Needed by runs with ml_for_nc_flag and no nc array: the single-moment cloud number of
+ * each level is then the network's prediction (main:364-371) instead of a constant.  The
+ * weights are the host's data (the library ships none); they are copied to the device. */
+int tempo_set_ml_cloud_number_c(tempo_ctx_t *ctx, const double *mean, const double *var,
+                                const double *weights00, const double *bias00,
+                                const double *weights01, const double *bias01);
 
 /* No reference counterpart.  Selects the per-level kernel variant directly (0..7). */
 int tempo_set_points_variant(tempo_ctx_t *ctx, int variant);

@@ -89,6 +89,7 @@ def load() -> ctypes.CDLL:
         lib.oracle_ccn_ptr.argtypes = [ctypes.POINTER(ctypes.c_long)]
         lib.oracle_ccn_ptr.restype = ctypes.POINTER(ctypes.c_float)
         lib.oracle_set_tie_sink.argtypes = [_IP]
+        lib.oracle_set_ml.argtypes = [_DP] * 6
         lib.oracle_param.argtypes = [ctypes.c_char_p, ctypes.c_int]
         lib.oracle_param.restype = ctypes.c_double
         lib.oracle_calc_gamma_p.argtypes = [ctypes.c_double, ctypes.c_double]
@@ -132,6 +133,14 @@ def init(hailaware: bool = True, ccn_path: str | os.PathLike | None = None) -> N
         rc = lib.oracle_read_ccn(str(ccn_path).encode())
         if rc:
             raise IOError(f"oracle: cannot read CCN table {ccn_path} (code {rc})")
+
+
+def set_ml(weights: dict) -> None:
+    """Weights of the cloud-number network (keys of tests/golden/ml_cloud_number.npz)."""
+    arrs = [np.ascontiguousarray(np.asarray(weights[k], dtype=np.float64))
+            for k in ("nc_ml_trans_mean", "nc_ml_trans_var", "nc_ml_w00", "nc_ml_b00",
+                      "nc_ml_w01", "nc_ml_b01")]
+    load().oracle_set_ml(*[a.ctypes.data_as(_DP) for a in arrs])
 
 
 def param(name: str, idx: int = 0) -> float:

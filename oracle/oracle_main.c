@@ -1923,6 +1923,46 @@ typedef struct {
   double *refl, *re_c, *re_i, *re_s, *mvd_r, *mvd_g, *mhd, *ncmr; /* nz each, NULL if off */
 } colout_t;
 
+/* cloud-number network of the ML path (ml:104-176): input scaler, two dense layers
+ * with ReLU, clamp to [-6, log10(2e9)], bias correction, 10**x.  The weights come from
+ * the host (oracle_set_ml), as the reference's come from its ML module. */
+static double ml_mean[7], ml_var[7], ml_w00[168], ml_b00[24], ml_w01[24], ml_b01[1];
+static int ml_loaded = 0;
+
+int oracle_set_ml(const double *mean, const double *var, const double *w00, const double *b00,
+                  const double *w01, const double *b01) {
+  memcpy(ml_mean, mean, sizeof ml_mean);
+  memcpy(ml_var, var, sizeof ml_var);
+  memcpy(ml_w00, w00, sizeof ml_w00);
+  memcpy(ml_b00, b00, sizeof ml_b00);
+  memcpy(ml_w01, w01, sizeof ml_w01);
+  memcpy(ml_b01, b01, sizeof ml_b01);
+  ml_loaded = 1;
+  return 0;
+}
+
+static double ml_predict_nc(double qc, double qr, double qi, double qs, double pres, double temp,
+                            double w) {
+  const double logmin = -6.0, logmax = 9.3010299957;
+  const double in[7] = {qc, qr, qi, qs, pres, temp, w};
+  double x[7], h[24];
+  for (int j = 0; j < 7; j++) x[j] = (in[j] - ml_mean[j]) / sqrt(ml_var[j]);
+  for (int i = 0; i < 24; i++) { /* weights00 = reshape(w00, [24, 7]) */
+    double acc = 0.0;
+    for (int j = 0; j < 7; j++) acc = acc + ml_w00[j * 24 + i] * x[j];
+    h[i] = fmax2(acc + ml_b00[i], 0.0);
+  }
+  double acc = 0.0;
+  for (int i = 0; i < 24; i++) acc = acc + ml_w01[i] * h[i];
+  double out = fmax2(acc + ml_b01[0], 0.0);
+  double pe = fmin2(logmax, fmax2(logmin, out));
+  double corr = 1.0;
+  if (pe >= 0.0 && pe < 3.0)
+    corr = -0.2704 * ipow(pe, 5) + 1.838 * ipow(pe, 4) - 5.127 * ipow(pe, 3) + 8.547 * ipow(pe, 2) -
+           8.439 * pe + 4.297;
+  return corr * pow(10.0, pe);
+}
+
 static double resolve_nc_value(const ocfg_t *cfg) {
   const char *s = cfg->single_moment_nc_opt;
   while (*s == ' ') s++;
@@ -1997,13 +2037,20 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
   snow_check_and_update(nz, w->rho, w->l_qs, qs1d, w->rs, w->qsten, dt, odt);
   for (k = 0; k < nz; k++) /* :353-361 */
     if (w->l_qs[k]) snow_moments_all(w, k, 1);
-  if (!nc1d) { /* :364-380 (ML path rejected before the call) */
-    double v;
-    if (land1d)
-      v = (*land1d != 1) ? nt_c_o : nt_c_l;
-    else
-      v = resolve_nc_value(cfg);
-    for (k = 0; k < nz; k++) w->nc[k] = v;
+  if (!nc1d) { /* :364-380 */
+    if (cfg->ml_for_nc_flag) {
+      for (k = 0; k < nz; k++) {
+        const double xq = qc1d[k] <= 1.e-12 ? 0.0 : qc1d[k];
+        w->nc[k] = ml_predict_nc(xq, qr1d[k], qi1d[k], qs1d[k], w->pres[k], w->temp[k], w1d[k]) * w->rho[k];
+      }
+    } else {
+      double v;
+      if (land1d)
+        v = (*land1d != 1) ? nt_c_o : nt_c_l;
+      else
+        v = resolve_nc_value(cfg);
+      for (k = 0; k < nz; k++) w->nc[k] = v;
+    }
     for (k = 0; k < nz; k++) w->ncsave[k] = w->nc[k];
     have_ncsave = 1;
   }
@@ -2295,7 +2342,7 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
   int ims = b[6], ime = b[7], jms = b[8], jme = b[9], kms = b[10], kme = b[11];
   int its = b[12], ite = b[13], jts = b[14], jte = b[15], kts = b[16], kte = b[17];
   (void)jme;
-  if (cfg->ml_for_nc_flag && !nc) return -3;
+  if (cfg->ml_for_nc_flag && !nc && !ml_loaded) return -3;
   if (qc_bl && qcfrac_bl) return -3;
   if (!t && !(th && pii)) return -2;
   int nz = kte - kts + 1;

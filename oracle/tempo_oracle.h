@@ -123,6 +123,12 @@ double oracle_calc_rslf(double p, double t);
 double oracle_calc_rsif(double p, double t);
 void oracle_snow_moments(double rs, double tc, double out[10]);
 
+/* Weights of the cloud-number network of the ML path (ml:33-98 layout: scaler means
+ * and variances [7], weights00 [24 x 7 column-major], bias00 [24], weights01 [24],
+ * bias01 [1]). */
+int oracle_set_ml(const double *mean, const double *var, const double *w00, const double *b00,
+                  const double *w01, const double *b01);
+
 /* tempo_run (driver:187-513).  Arrays are (ims:ime, kms:kme, jms:jme), i fastest.
  * NULL means "optional argument not present".  bounds = ids,ide,jds,jde,kds,kde,
  * ims,ime,jms,jme,kms,kme,its,ite,jts,jte,kts,kte.  Columns run in parallel on

@@ -383,6 +383,15 @@ class TempoContext:
         """Capture each distinct step into a CUDA graph and replay it (tempo_set_graphs)."""
         _check(load_library().tempo_set_graphs(self._h, int(bool(on))))
 
+    def set_ml_cloud_number(self, weights: dict):
+        """The cloud-number network of the ML path (tempo_set_ml_cloud_number_c); keys
+        nc_ml_trans_mean, nc_ml_trans_var, nc_ml_w00, nc_ml_b00, nc_ml_w01, nc_ml_b01
+        (the reference's names, src/module_mp_tempo_ml.F90:33-98)."""
+        arrs = [np.ascontiguousarray(np.asarray(weights[k], dtype=np.float64))
+                for k in ("nc_ml_trans_mean", "nc_ml_trans_var", "nc_ml_w00", "nc_ml_b00",
+                          "nc_ml_w01", "nc_ml_b01")]
+        _check(load_library().tempo_set_ml_cloud_number_c(self._h, *[_np_ptr(a, ctypes.c_double) for a in arrs]))
+
     def set_points_variant(self, v: int):
         _check(load_library().tempo_set_points_variant(self._h, int(v)))
 

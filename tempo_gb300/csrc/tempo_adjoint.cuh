@@ -160,7 +160,8 @@ __global__ void __launch_bounds__(128) tempo_early_adjoint_kernel(
   L.cs = &cst;
   L.ci = &ci;
   load_level(a, e, L, io);
-  initial_checks(L, a.flags, ncsave_of<R>(a, g), do_ginit, step_dt<R>(a), step_odt<R>(a));
+  R ncsave = ncsave_of<R>(a, g);
+  initial_checks(L, a.flags, ncsave, do_ginit, step_dt<R>(a), step_odt<R>(a));
   store_checked(a, e, L, io);
   // the checks overwrite the hydrometeor inputs; temperature and qv pass through
   for (int i = 0; i < IN_N; i++) {

@@ -99,6 +99,7 @@ struct tempo_ctx {
   cudaEvent_t kev[kStepLaunches + 1] = {};
   int points_variant = 0;  // mixed form on FP32 storage (tempo_autotune_dev_f32_c)
   RadarConsts radar{};     // melting-layer reflectivity (FP64)
+  double* d_mlnet = nullptr;  // cloud-number network (tempo_set_ml_cloud_number_c)
   bool use_graphs = false;
   std::vector<GraphEntry> graphs;  // captured steps, oldest first
 };
@@ -372,8 +373,9 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
     return fail(TEMPO_ERR_ARG, "a required array (p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr) is NULL");
   if (!A.t && !(A.th && A.pii))
     return fail(TEMPO_ERR_ARG, "tempo_run requires either t or th and pii");
-  if (cfg->ml_for_nc_flag && !A.nc)
-    return fail(TEMPO_ERR_UNSUPPORTED, "ML cloud-number prediction is not part of this build");
+  if (cfg->ml_for_nc_flag && !A.nc && !c->d_mlnet)
+    return fail(TEMPO_ERR_STATE, "ml_for_nc_flag without nc needs the cloud-number network "
+                "(tempo_set_ml_cloud_number_c)");
   uint32_t f = 0;
   if (A.nc) f |= F_NC;
   if (A.nwfa) f |= F_NWFA;
@@ -394,6 +396,7 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
   if (dt > timestep_conversion_rime_to_rain) f |= F_DT_RIME;
   if (cfg->semi_sedi_flag) f |= F_SEMI;
   if (cfg->refl10cm_from_melting_flag && cfg->refl10cm_flag && dg && dg->refl10cm) f |= F_MELT;
+  if (cfg->ml_for_nc_flag && !A.nc) f |= F_MLNC;
 
   a = StepArgs<S>{};
   a.t = A.t;
@@ -452,6 +455,7 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
   a.odt_f = (float)a.odt;
   a.nc_single = resolve_nc_value(cfg);
   a.flags = f;
+  a.mlnet = (f & F_MLNC) ? c->d_mlnet : nullptr;
   // decay rates of the aerosol initial profiles (init_*_friendly_aerosols,
   // aerosols:14-73; h_01 = 0.8 km), host libm as in the reference
   a.niccn3 = -1.0 * std::log(naccn1 / naccn0) / 0.8;
@@ -481,8 +485,10 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   const size_t sl_bytes = (a.flags & F_SEMI) ? al((size_t)kSlRows * (nzs + 2) * npad * 8) : 0;
   // melting-reflectivity record of phase C only on that path
   const size_t ml_bytes = (a.flags & F_MELT) ? al((size_t)kMeltN * nzs * npad * 8 + nzs * npad) : 0;
+  // per-point cloud number of the network only on that path
+  const size_t nc_bytes = (a.flags & F_MLNC) ? al(nzs * npad * rsz) : 0;
   const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes +
-                       sl_bytes + ml_bytes + 256;
+                       sl_bytes + ml_bytes + nc_bytes + 256;
   if (int rc = ensure_scratch(c, total)) return rc;
   char* sp = (char*)c->scratch;
   a.sd = sp;
@@ -503,6 +509,8 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   sp += sl_bytes;
   a.mlw = ml_bytes ? sp : nullptr;
   sp += ml_bytes;
+  a.ncw = nc_bytes ? sp : nullptr;
+  sp += nc_bytes;
   a.nact = (unsigned int*)sp;
   a.stats = c->d_stats;
   c->last_cols = a.ncol;
@@ -577,10 +585,10 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
                     cudaStream_t s) {
   StepArgs<float> a;
   if (int rc = build_args(c, cfg, dt, itimestep, A, b, dg, a)) return rc;
-  if (a.flags & (F_SEMI | F_MELT))
-    return fail(TEMPO_ERR_UNSUPPORTED, "semi-Lagrangian sedimentation and the melting-layer reflectivity "
-                "need work space beyond the fixed scratch of tempo_run_dev_f32_noalloc_c: call "
-                "tempo_run_dev_f32_c");
+  if (a.flags & (F_SEMI | F_MELT | F_MLNC))
+    return fail(TEMPO_ERR_UNSUPPORTED, "semi-Lagrangian sedimentation, the melting-layer reflectivity "
+                "and the ML cloud number need work space beyond the fixed scratch of "
+                "tempo_run_dev_f32_noalloc_c: call tempo_run_dev_f32_c");
   if (c->precision != TEMPO_PREC_MIXED)
     return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
   const size_t npad = (size_t)a.ncol_pad, nzs = (size_t)a.nz;
@@ -810,6 +818,7 @@ int tempo_ctx_destroy(tempo_ctx_t* c) {
   free_tables(c);
   cudaFree(c->scratch);
   cudaFree(c->d_stats);
+  cudaFree(c->d_mlnet);
   for (auto& m : c->mirrors) cudaFree(m.d);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -1009,6 +1018,33 @@ int tempo_set_graphs(tempo_ctx_t* c, int on) {
   return TEMPO_OK;
 }
 
+int tempo_set_ml_cloud_number_c(tempo_ctx_t* c, const double* mean, const double* var,
+                                const double* weights00, const double* bias00,
+                                const double* weights01, const double* bias01) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (!mean || !var || !weights00 || !bias00 || !weights01 || !bias01)
+    return fail(TEMPO_ERR_ARG, "a network array is NULL");
+  double h[kMlNet];
+  std::memcpy(h, mean, 7 * sizeof(double));
+  std::memcpy(h + 7, var, 7 * sizeof(double));
+  std::memcpy(h + 14, weights00, 168 * sizeof(double));
+  std::memcpy(h + 182, bias00, 24 * sizeof(double));
+  std::memcpy(h + 206, weights01, 24 * sizeof(double));
+  h[230] = bias01[0];
+  for (int i = 7; i < 14; i++)
+    if (!(h[i] > 0.0)) return fail(TEMPO_ERR_ARG, "scaler variance %d is not positive", i - 7);
+  CUDA_TRY(cudaSetDevice(c->device));
+  if (!c->d_mlnet) {
+    cudaError_t e = cudaMalloc(&c->d_mlnet, sizeof h);
+    if (e != cudaSuccess) {
+      c->d_mlnet = nullptr;
+      return fail(TEMPO_ERR_NOMEM, "network weights: %s", cudaGetErrorString(e));
+    }
+  }
+  CUDA_TRY(cudaMemcpy(c->d_mlnet, h, sizeof h, cudaMemcpyHostToDevice));
+  return TEMPO_OK;
+}
+
 int tempo_set_points_variant(tempo_ctx_t* c, int variant) {
   if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
   if (variant < 0 || variant >= kPointsVariants) return fail(TEMPO_ERR_ARG, "variant %d outside [0, %d)", variant, kPointsVariants);
@@ -1128,9 +1164,9 @@ int tl_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, temp
   const RunArrays<T> X = arrays_of<T>(x);
   StepArgs<T> ap;
   if (int rc = build_args(c, cfg, dt, itimestep, X, b, dgs, ap)) return rc;
-  if (ap.flags & (F_SEMI | F_MELT))
-    return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation and of the "
-                "melting-layer reflectivity are not part of this build");
+  if (ap.flags & (F_SEMI | F_MELT | F_MLNC))
+    return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation, the "
+                "melting-layer reflectivity and the ML cloud number are not part of this build");
   if (cfg->max_hail_diameter_flag) ap.mhd_sfc = ap.mhd_col = nullptr;  // not differentiable
   CUDA_TRY(cudaSetDevice(c->device));
   DevBufs B;
@@ -1168,9 +1204,9 @@ int adjoint_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep,
   const RunArrays<T> X = arrays_of<T>(x);
   StepArgs<T> ap;
   if (int rc = build_args(c, cfg, dt, itimestep, X, b, nullptr, ap)) return rc;
-  if (ap.flags & (F_SEMI | F_MELT))
-    return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation and of the "
-                "melting-layer reflectivity are not part of this build");
+  if (ap.flags & (F_SEMI | F_MELT | F_MLNC))
+    return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation, the "
+                "melting-layer reflectivity and the ML cloud number are not part of this build");
   CUDA_TRY(cudaSetDevice(c->device));
   DevBufs B;
   using D1 = Dual<T, 1>;

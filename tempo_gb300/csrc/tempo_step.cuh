@@ -139,14 +139,50 @@ __device__ __forceinline__ void load_level(const StepArgs<S>& a, long e, Lev<R>&
 }
 
 // initial checks (main:347-396)
+// cloud number (kg^-1) of the ML path (ml:104-176): input scaler, two dense layers with
+// ReLU, the exponent clamped to [-6, log10(2e9)], the reference's bias correction and
+// 10**x; weights from the host (kMlNet values)
 template <class R>
-__device__ __forceinline__ void initial_checks(Lev<R>& L, uint32_t f, R ncsave, bool do_ginit, R dt,
-                                               R odt) {
+__device__ R ml_cloud_number(const double* net, R qc, R qr, R qi, R qs, R pres, R temp, R w) {
+  const double *mean = net, *var = net + 7, *w00 = net + 14, *b00 = net + 182, *w01 = net + 206,
+               *b01 = net + 230;
+  const R in[7] = {qc, qr, qi, qs, pres, temp, w};
+  R x[7];
+TG_UNROLL
+  for (int j = 0; j < 7; j++) x[j] = (in[j] - R(mean[j])) / Sqrt(R(var[j]));
+  R acc1 = R(0.0);
+  for (int i = 0; i < 24; i++) {
+    R acc = R(0.0);
+TG_UNROLL
+    for (int j = 0; j < 7; j++) acc = acc + R(w00[j * 24 + i]) * x[j];
+    acc = Max(acc + R(b00[i]), R(0.0));
+    acc1 = acc1 + R(w01[i]) * acc;
+  }
+  const R out = Max(acc1 + R(b01[0]), R(0.0));
+  const R pe = Min(R(9.3010299957), Max(R(-6.0), out));
+  R corr = R(1.0);
+  if (pe >= R(0.0) && pe < R(3.0)) {
+    const R p2 = pe * pe, p4 = p2 * p2;  // integer powers by binary powering
+    corr = R(-0.2704) * (pe * p4) + R(1.838) * p4 - R(5.127) * (pe * p2) + R(8.547) * p2 -
+           R(8.439) * pe + R(4.297);
+  }
+  return corr * Pow(R(10.0), pe);
+}
+
+// The initial checks of the level (main:346-396).  With F_MLNC the single-moment cloud
+// number comes from the network (main:364-371) and is returned in ncsave.
+template <class R>
+__device__ __forceinline__ void initial_checks(Lev<R>& L, uint32_t f, R& ncsave, bool do_ginit, R dt,
+                                               R odt, const double* mlnet = nullptr, R w = R(0)) {
   using I = Isl<R>;
   rain_check(L, L.qr1d, L.nr1d, dt, odt);
   ice_check(L, L.qi1d, L.ni1d, dt, odt);
   snow_check(L, L.qs1d, dt, odt);
   if (L.l_qs) snow_moments(L, R(Min(I(-0.1), L.temp - t0)), 1);
+  if ((f & F_MLNC) && mlnet) {
+    const R xq = L.qc1d <= R(1.e-12) ? R(0.0) : L.qc1d;
+    ncsave = ml_cloud_number(mlnet, xq, L.qr1d, L.qi1d, L.qs1d, R(L.pres), R(L.temp), w) * R(L.rho);
+  }
   if (!(f & F_NC)) L.nc = ncsave;
   cloud_check(L, L.qc1d, L.nc1d, (f & F_NC) != 0, ncsave, dt, odt);
   if (do_ginit) graupel_init(L);
@@ -242,7 +278,6 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
   }
 
   // early exit: initial checks only, default diagnostics
-  const R ncsave = ncsave_of<R>(a, g);
   for (int k = 0; k < nz; k++) {
     const long e = g.base + (long)k * a.NI;
     Lev<R> L;
@@ -250,7 +285,8 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
     L.ci = &ci;
     const FwdIO<S> io{a};
     load_level(a, e, L, io);
-    initial_checks(L, f, ncsave, do_ginit, dt, odt);
+    R ncsave = ncsave_of<R>(a, g);
+    initial_checks(L, f, ncsave, do_ginit, dt, odt, a.mlnet, R(a.w[e]));
     store_checked(a, e, L, io);
   }
   const long t2 = g.tile2;
@@ -412,8 +448,7 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   const bool has_nc = f & F_NC, has_nwfa = f & F_NWFA, has_nifa = f & F_NIFA;
   const R dt = step_dt<R>(a), odt = step_odt<R>(a);
   const I dti = step_dti<R>(a);
-  const R ncsave = ncsave_of<R>(a, g);
-  const R ncsave_cond = has_nc ? R(nt_c_l) : ncsave;
+  R ncsave = ncsave_of<R>(a, g);  // per level with F_MLNC, set by the initial checks
   const bool do_ginit = a.cmask[s] & CM_GINIT;
   const long cs = a.ncol_pad, fsd = (long)nz * cs, o = pt_off(s, k, nz);
   I* sd = reinterpret_cast<I*>(a.sd);
@@ -436,7 +471,10 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   L.nwfa = nwfa_in;
   L.nifa = nifa_in;
   aerosol_check(L, f, dt);
-  initial_checks(L, f, ncsave, do_ginit, dt, odt);
+  initial_checks(L, f, ncsave, do_ginit, dt, odt, a.mlnet, w);
+  if constexpr (IO::forward && !IsDual<S>::value)
+    if (f & F_MLNC) reinterpret_cast<R*>(a.ncw)[o] = ncsave;  // for phase C
+  const R ncsave_cond = has_nc ? R(nt_c_l) : ncsave;
   L.qcten = L.qiten = L.qrten = L.qsten = L.qgten = L.ngten = L.qbten = L.niten = L.nrten =
       L.ncten = R(0);
 
@@ -1015,8 +1053,9 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
   const bool has_nc = f & F_NC, hail = f & F_HAIL;
   const R dt = step_dt<R>(a), odt = step_odt<R>(a);
   const I dti = step_dti<R>(a);
-  const R ncsave = ncsave_of<R>(a, g);
   const long cs = a.ncol_pad, fsd = (long)nz * cs, o = pt_off(s, k, nz);
+  // the cloud number of phase A's initial checks (per level from the network with F_MLNC)
+  const R ncsave = (f & F_MLNC) ? reinterpret_cast<const R*>(a.ncw)[o] : ncsave_of<R>(a, g);
 
   Lev<R> L;
   L.cs = &cst;

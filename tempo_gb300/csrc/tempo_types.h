@@ -46,7 +46,8 @@ enum : uint32_t {
   F_MVDG = 1u << 13, F_NCMR = 1u << 14, F_USE_T = 1u << 15,
   F_DT_RIME = 1u << 16,  // dt > timestep_conversion_rime_to_rain
   F_SEMI = 1u << 17,     // semi_sedi_flag: semi-Lagrangian rain and graupel sedimentation
-  F_MELT = 1u << 18      // refl10cm_from_melting_flag (with refl10cm requested)
+  F_MELT = 1u << 18,     // refl10cm_from_melting_flag (with refl10cm requested)
+  F_MLNC = 1u << 19      // ml_for_nc_flag without nc: cloud number from the network
 };
 
 // per-point scratch fields in the island type (thermodynamic and sedimentation islands)
@@ -107,7 +108,13 @@ struct StepArgs {
   void* slw;          // Isl<R>[kSlRows][nz + 2][ncol_pad]: semi-Lagrangian work rows (F_SEMI)
   void* mlw;          // melting-reflectivity record (F_MELT): double[kMeltN] planes, then
                       // a byte plane of MeltBit flags
+  const double* mlnet;  // cloud-number network (F_MLNC), kMlNet values in the layout of
+                        // tempo_set_ml_cloud_number_c
+  void* ncw;          // R plane: the network's cloud number per point (F_MLNC)
 };
+// size of the cloud-number network: scaler means and variances (7 + 7), weights00
+// (24 x 7, column-major), bias00 (24), weights01 (24), bias01 (1)
+constexpr int kMlNet = 7 + 7 + 168 + 24 + 24 + 1;
 
 // Inputs of a point that carry derivatives in the tangent-linear and adjoint kernels
 enum InId : int { IN_T, IN_QV, IN_QC, IN_NC, IN_QR, IN_NR, IN_QI, IN_NI, IN_QS, IN_QG, IN_NG, IN_QB, IN_N };
