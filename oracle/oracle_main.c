@@ -1921,6 +1921,7 @@ static void max_hail_diam(ws_t *w, double *mhd) {
 /* ------------------------------------------------------------------------------ */
 typedef struct {
   double *refl, *re_c, *re_i, *re_s, *mvd_r, *mvd_g, *mhd, *ncmr; /* nz each, NULL if off */
+  const double *qc_bl, *qcfrac_bl; /* the boundary-layer cloud of the column, or NULL */
 } colout_t;
 
 /* cloud-number network of the ML path (ml:104-176): input scaler, two dense layers
@@ -2323,7 +2324,25 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
     for (k = 0; k < nz; k++) co->mvd_g[k] = w->mvd_g[k];
   if (co->mhd) max_hail_diam(w, co->mhd);
   if (co->refl) reflectivity_10cm(w, co->refl, cfg->refl10cm_from_melting_flag);
-  if (co->re_c) effective_radius(w, co->re_c, co->re_i, co->re_s);
+  if (co->re_c) {
+    if (co->qc_bl && co->qcfrac_bl) {
+      /* :832-857: the in-cloud boundary-layer water joins the resolved cloud, the network
+       * predicts its number, and the cloud check recomputes rc, nc and ilamc for the
+       * effective radius (the state of the step is not touched) */
+      for (k = 0; k < nz; k++) {
+        double xq = qc1d[k];
+        if (xq <= r1 && co->qc_bl[k] > 1.e-9 && co->qcfrac_bl[k] > 0.0) xq = xq + co->qc_bl[k] / co->qcfrac_bl[k];
+        if (xq <= 1.e-12) xq = 0.0;
+        w->xrx[k] = xq;
+        w->xncx[k] = ml_predict_nc(xq, qr1d[k], qi1d[k], qs1d[k], w->pres[k], w->temp[k], w1d[k]);
+        w->qcten[k] = 0.0;
+        w->ncten[k] = 0.0;
+      }
+      cloud_check_and_update(nz, w->rho, w->l_qc, w->xrx, w->xncx, NULL, w->rc, w->nc, w->qcten,
+                             w->ncten, w->ilamc, w->mvd_c, dt, odt);
+    }
+    effective_radius(w, co->re_c, co->re_i, co->re_s);
+  }
 }
 
 /* ------------------------------------------------------------------------------ */
@@ -2343,7 +2362,7 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
   int its = b[12], ite = b[13], jts = b[14], jte = b[15], kts = b[16], kte = b[17];
   (void)jme;
   if (cfg->ml_for_nc_flag && !nc && !ml_loaded) return -3;
-  if (qc_bl && qcfrac_bl) return -3;
+  if (qc_bl && qcfrac_bl && !ml_loaded) return -3;
   if (!t && !(th && pii)) return -2;
   int nz = kte - kts + 1;
   long ni_ = ime - ims + 1, nk_ = kme - kms + 1;
@@ -2383,7 +2402,8 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
 #pragma omp parallel reduction(+ : early)
   {
     ws_t *w = ws_new(nz);
-    double *buf = (double *)calloc((size_t)nz * 30, sizeof(double));
+    double *buf = (double *)calloc((size_t)nz * 32, sizeof(double));
+    double *qcbl1d = buf + 30 * nz, *qcfbl1d = buf + 31 * nz;
     double *t1d = buf, *p1d = buf + nz, *w1d = buf + 2 * nz, *dz1d = buf + 3 * nz,
            *qv1d = buf + 4 * nz, *qc1d = buf + 5 * nz, *qi1d = buf + 6 * nz, *qr1d = buf + 7 * nz,
            *qs1d = buf + 8 * nz, *qg1d = buf + 9 * nz, *ni1d = buf + 10 * nz, *nr1d = buf + 11 * nz,
@@ -2419,6 +2439,10 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
           ng1d[k0] = ng[a];
           qb1d[k0] = qb[a];
         }
+        if (qc_bl && qcfrac_bl) {
+          qcbl1d[k0] = qc_bl[a];
+          qcfbl1d[k0] = qcfrac_bl[a];
+        }
       }
       int land1d = 0;
       if (land_input) land1d = land_input[((long)i - ims) + ((long)j - jms) * ni_];
@@ -2432,6 +2456,8 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
       co.mvd_g = cfg->graupel_med_vol_diam_flag ? o_mvg : NULL;
       co.mhd = cfg->max_hail_diameter_flag ? o_mhd : NULL;
       co.ncmr = cfg->cloud_number_mixing_ratio_flag ? o_ncm : NULL;
+      co.qc_bl = (qc_bl && qcfrac_bl) ? qcbl1d : NULL;
+      co.qcfrac_bl = (qc_bl && qcfrac_bl) ? qcfbl1d : NULL;
       mdiag_t md;
       t_tie = 0;
       t_tie_bit = 1;

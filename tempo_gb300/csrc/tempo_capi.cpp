@@ -358,6 +358,7 @@ struct RunArrays {
   const S *pii, *p, *w, *dz;
   S *qv, *qc, *qr, *qi, *qs, *qg, *ni, *nr, *nc, *nwfa, *nifa, *ng, *qb;
   const int* land;
+  const S *qc_bl = nullptr, *qcfrac_bl = nullptr;  // host path only
 };
 
 // Validates the argument list and launches the step on device arrays.
@@ -373,6 +374,9 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
     return fail(TEMPO_ERR_ARG, "a required array (p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr) is NULL");
   if (!A.t && !(A.th && A.pii))
     return fail(TEMPO_ERR_ARG, "tempo_run requires either t or th and pii");
+  if (A.qc_bl && A.qcfrac_bl && !c->d_mlnet)
+    return fail(TEMPO_ERR_STATE, "the boundary-layer cloud path (qc_bl, qcfrac_bl) needs the "
+                "cloud-number network (tempo_set_ml_cloud_number_c)");
   if (cfg->ml_for_nc_flag && !A.nc && !c->d_mlnet)
     return fail(TEMPO_ERR_STATE, "ml_for_nc_flag without nc needs the cloud-number network "
                 "(tempo_set_ml_cloud_number_c)");
@@ -397,6 +401,7 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
   if (cfg->semi_sedi_flag) f |= F_SEMI;
   if (cfg->refl10cm_from_melting_flag && cfg->refl10cm_flag && dg && dg->refl10cm) f |= F_MELT;
   if (cfg->ml_for_nc_flag && !A.nc) f |= F_MLNC;
+  if (A.qc_bl && A.qcfrac_bl) f |= F_BLRE;
 
   a = StepArgs<S>{};
   a.t = A.t;
@@ -419,6 +424,8 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
   a.ng = A.ng;
   a.qb = A.qb;
   a.land = A.land;
+  a.qc_bl = A.qc_bl;
+  a.qcfrac_bl = A.qcfrac_bl;
   if (dg) {
     a.rain_precip = (S*)dg->rain_precip;
     a.ice_precip = (S*)dg->ice_liquid_equiv_precip;
@@ -455,7 +462,7 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
   a.odt_f = (float)a.odt;
   a.nc_single = resolve_nc_value(cfg);
   a.flags = f;
-  a.mlnet = (f & F_MLNC) ? c->d_mlnet : nullptr;
+  a.mlnet = (f & (F_MLNC | F_BLRE)) ? c->d_mlnet : nullptr;
   // decay rates of the aerosol initial profiles (init_*_friendly_aerosols,
   // aerosols:14-73; h_01 = 0.8 km), host libm as in the reference
   a.niccn3 = -1.0 * std::log(naccn1 / naccn0) / 0.8;
@@ -654,11 +661,13 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
     size_t bytes;
     bool out;
   };
+  const bool bl = H.qc_bl && H.qcfrac_bl;
   const S* in3[] = {H.t, H.th, H.pii, H.p, H.w, H.dz, H.qv, H.qc, H.qr, H.qi, H.qs, H.qg,
-                    H.ni, H.nr, H.nc, H.nwfa, H.nifa, H.ng, H.qb};
+                    H.ni, H.nr, H.nc, H.nwfa, H.nifa, H.ng, H.qb,
+                    bl ? H.qc_bl : nullptr, bl ? H.qcfrac_bl : nullptr};
   const bool out3[] = {true, true, false, false, false, false, true, true, true, true, true,
-                       true, true, true, true, true, true, true, true};
-  const int n_in = 19;
+                       true, true, true, true, true, true, true, true, false, false};
+  const int n_in = 21;
   void* dg_h[15] = {dg ? dg->rain_precip : nullptr, dg ? dg->ice_liquid_equiv_precip : nullptr,
                     dg ? dg->snow_liquid_equiv_precip : nullptr,
                     dg ? dg->graupel_liquid_equiv_precip : nullptr,
@@ -713,7 +722,8 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
   RunArrays<S> D{(S*)d[0],  (S*)d[1],  (const S*)d[2], (const S*)d[3], (const S*)d[4],
                  (const S*)d[5], (S*)d[6],  (S*)d[7],  (S*)d[8],  (S*)d[9],
                  (S*)d[10], (S*)d[11], (S*)d[12], (S*)d[13], (S*)d[14],
-                 (S*)d[15], (S*)d[16], (S*)d[17], (S*)d[18], (const int*)d[n_in]};
+                 (S*)d[15], (S*)d[16], (S*)d[17], (S*)d[18], (const int*)d[n_in],
+                 (const S*)d[19], (const S*)d[20]};
   tempo_diags_t ddg{};
   void** ddp[15] = {&ddg.rain_precip, &ddg.ice_liquid_equiv_precip, &ddg.snow_liquid_equiv_precip,
                     &ddg.graupel_liquid_equiv_precip, &ddg.frozen_fraction, &ddg.frz_rain_precip,
@@ -868,11 +878,11 @@ int tempo_run_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, double dt, int itimeste
                 int kts, int kte, tempo_diags_t* diags) {
   (void)qcfrac; (void)qifrac; (void)thten_bl; (void)qvten_bl; (void)qcten_bl; (void)qiten_bl;
   (void)thten_lwrad; (void)thten_swrad; (void)ids; (void)ide; (void)jds; (void)jde; (void)kds; (void)kde;
-  if (qc_bl && qcfrac_bl)
-    return fail(TEMPO_ERR_UNSUPPORTED, "the ML boundary-layer cloud path (qc_bl, qcfrac_bl) is not part of this build");
   if (c && c->precision != TEMPO_PREC_FP64 && c->precision != TEMPO_PREC_MIXED)
     return fail(TEMPO_ERR_STATE, "bad precision");
   RunArrays<double> H{t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb, land_input};
+  H.qc_bl = qc_bl;  // with qcfrac_bl: the boundary-layer cloud in re_cloud (main:832-857)
+  H.qcfrac_bl = qcfrac_bl;
   return run_host(c, cfg, dt, itimestep, H, Bounds{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte}, diags);
 }
 

@@ -1156,6 +1156,21 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
     }
   }
   if (f & F_RE) {  // effective_radius (diags:13-56)
+    if constexpr (IO::forward && !IsDual<S>::value) {
+      if (f & F_BLRE) {
+        // main:832-857: the in-cloud boundary-layer water joins the resolved cloud, the
+        // network predicts its number, and the cloud check recomputes rc, nc and ilamc
+        // for the effective radius (the step's outputs are already stored)
+        R xq = L.qc1d;
+        const R qbl = R(a.qc_bl[e]), fbl = R(a.qcfrac_bl[e]);
+        if (xq <= R(r1) && qbl > R(1.e-9) && fbl > R(0.0)) xq = xq + qbl / fbl;
+        if (xq <= R(1.e-12)) xq = R(0.0);
+        R xn = ml_cloud_number(a.mlnet, xq, L.qr1d, L.qi1d, L.qs1d, R(L.pres), R(L.temp), R(a.w[e]));
+        L.qcten = R(0.0);
+        L.ncten = R(0.0);
+        cloud_check(L, xq, xn, true, ncsave, dt, odt);
+      }
+    }
     R rec = R(0), rei = R(0), res = R(0);
     if (L.l_qc) {
       int nu_c = get_nuc(L.nc);

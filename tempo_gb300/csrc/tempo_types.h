@@ -47,7 +47,8 @@ enum : uint32_t {
   F_DT_RIME = 1u << 16,  // dt > timestep_conversion_rime_to_rain
   F_SEMI = 1u << 17,     // semi_sedi_flag: semi-Lagrangian rain and graupel sedimentation
   F_MELT = 1u << 18,     // refl10cm_from_melting_flag (with refl10cm requested)
-  F_MLNC = 1u << 19      // ml_for_nc_flag without nc: cloud number from the network
+  F_MLNC = 1u << 19,     // ml_for_nc_flag without nc: cloud number from the network
+  F_BLRE = 1u << 20      // qc_bl and qcfrac_bl given: boundary-layer cloud in re_cloud
 };
 
 // per-point scratch fields in the island type (thermodynamic and sedimentation islands)
@@ -111,6 +112,7 @@ struct StepArgs {
   const double* mlnet;  // cloud-number network (F_MLNC), kMlNet values in the layout of
                         // tempo_set_ml_cloud_number_c
   void* ncw;          // R plane: the network's cloud number per point (F_MLNC)
+  const S *qc_bl, *qcfrac_bl;  // boundary-layer cloud water and fraction (F_BLRE)
 };
 // size of the cloud-number network: scaler means and variances (7 + 7), weights00
 // (24 x 7, column-major), bias00 (24), weights01 (24), bias01 (1)

@@ -90,3 +90,54 @@ def test_ml_mixed_close_to_fp64(tg, oracle_tables):
             assert frac <= 1e-2, (k, frac)
     finally:
         ctx.close()
+
+
+def _with_bl(wl):
+    """Boundary-layer cloud water and fraction in the lowest 12 levels (seeded)."""
+    rng = np.random.default_rng(41)
+    shape = wl.fields["p"].shape
+    qbl = np.zeros(shape)
+    fbl = np.zeros(shape)
+    qbl[:, :12, :] = rng.uniform(0.0, 5e-4, (shape[0], 12, shape[2]))
+    fbl[:, :12, :] = rng.uniform(0.05, 1.0, (shape[0], 12, shape[2]))
+    w2 = copy(wl)
+    w2.fields = dict(wl.fields, qc_bl=qbl, qcfrac_bl=fbl)
+    return w2
+
+
+def test_oracle_bl_changes_only_re_cloud(oracle_mod):
+    oracle_mod.init(False)
+    oracle_mod.set_ml(dict(np.load(WEIGHTS)))
+    from tempo_gb300 import workloads as W
+    wl = W.config1(ni=32, nj=8, steps=1)
+    fa, da = run_oracle(oracle_mod, dict(hailaware_flag=0), wl)
+    fb, db = run_oracle(oracle_mod, dict(hailaware_flag=0), _with_bl(wl))
+    for k in fa:
+        if k in ("qc_bl", "qcfrac_bl"):
+            continue
+        assert np.array_equal(fa[k], fb[k]), k
+    for k in da:
+        if k != "re_cloud":
+            assert np.array_equal(da[k], db[k], equal_nan=True), k
+    assert not np.array_equal(da["re_cloud"], db["re_cloud"])
+    oracle_mod.init(True)
+
+
+@pytest.mark.gpu
+def test_bl_fp64_matches_oracle(tg, oracle_mod, oracle_tables):
+    from tempo_gb300 import workloads as W
+    oracle_mod.init(False)
+    weights = dict(np.load(WEIGHTS))
+    oracle_mod.set_ml(weights)
+    ctx = tg.TempoContext(table_dir=oracle_tables, build_tables=False,
+                          cfgs=tg.default_cfgs(hailaware_flag=0))
+    try:
+        ctx.set_ml_cloud_number(weights)
+        wl = _with_bl(W.config1(ni=32, nj=8, steps=1))
+        fo, do = run_oracle(oracle_mod, dict(hailaware_flag=0), wl)
+        fg, dg = run_gpu(ctx, dict(hailaware_flag=0), wl)
+        name, e = worst(compare(fg, dg, fo, do, inputs=wl.fields))
+        assert e < TOL64, (name, e)
+    finally:
+        ctx.close()
+        oracle_mod.init(True)
