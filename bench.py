@@ -364,16 +364,17 @@ def main():
     stream = torch.cuda.current_stream()
     # warm-up: the first steps move the generated state towards the ones the timed steps
     # see (condensation, evaporation and sedimentation change where the work is); the
-    # autotuner then scores every per-level kernel variant over the next steps on a
-    # private copy of that state, and the last warm-up step captures the CUDA graph of
-    # the chosen variant (the timed steps replay it, with per-kernel timing events in the
-    # graph): W warm-up steps in all
+    # autotuner then scores every per-level kernel variant in both point orders
+    # (level-major, regime) over the next steps on a private copy of that state, and the
+    # last warm-up step captures the CUDA graph of the chosen candidate (the timed steps
+    # replay it, with per-kernel timing events in the graph): W warm-up steps in all
     ctx.set_points_variant(4)
     it = 1
     for _ in range(max(args.warmup - 1, 1)):
         ctx.run_device(f32, args.dt, it, diags=diag)
         it += 1
     variant, variant_ms = ctx.autotune_device(f32, args.dt, it, diags=diag, reps=6)
+    tuning = ctx.tuning()
     ctx.set_kernel_timing(True)
     ctx.set_graphs(True)
     ctx.run_device(f32, args.dt, it, diags=diag)
@@ -481,12 +482,13 @@ def main():
         "fp64_value": world * ncol / (ms64 / 1e3), "fp64_ms_per_step": ms64,
         "fp32_over_fp64": ms64 / ms_step,
         "mixed_error_vs_fp64": mixed_error,
-        "autotune": {"points_variant": variant, "points_ms_per_variant": variant_ms},
+        "autotune": {**tuning, "points_order": ("level-major", "regime")[tuning["points_order"]],
+                     "points_ms_per_candidate": variant_ms[:16], "sedim_ms_per_variant": variant_ms[16:]},
         "e2e": {"value": e2e_value, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "path": "tempo_run_f32_c (host arrays)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic_from_profiles(),
-                     "kernel": "column step = tempo_{prep,points,sedim,final}_kernel<float,float>",
+                     "kernel": "column step = tempo_{prep,regime_count,regime_scatter,points,sedim,final}_kernel",
                      "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src,
                      "kernel_ms": kms,
                      "kernel_share": {k: v / step_kernel_ms for k, v in kms.items()}},

@@ -222,22 +222,27 @@ int tempo_build_tables_c(tempo_ctx_t *ctx, float *elapsed_ms);
 int tempo_last_stats_c(tempo_ctx_t *ctx, long out[8]);
 
 /* No reference counterpart.  With on != 0, each later run records CUDA events on its
- * stream around its four kernels (prep, points, sedim, final);
- * tempo_kernel_times_c waits for the last run's events and returns the four kernel
- * durations in milliseconds. */
+ * stream around its kernels; tempo_kernel_times_c waits for the last run's events and
+ * returns five durations in milliseconds: prep, the regime-order kernels (0 in
+ * level-major order), points, sedim, final. */
 int tempo_set_kernel_timing(tempo_ctx_t *ctx, int on);
-int tempo_kernel_times_c(tempo_ctx_t *ctx, float ms[4]);
+int tempo_kernel_times_c(tempo_ctx_t *ctx, float ms[5]);
 
-/* No reference counterpart.  Autotuner of the mixed form on FP32 device storage: for
- * every variant of its per-level kernel (thread-to-work mapping and register budget) it
- * copies the given state and runs `reps` consecutive steps (itimestep, itimestep + 1,
- * ...) on the copy -- the caller's arrays are not modified -- timing the per-level
- * kernel with CUDA events on `stream`, and keeps the variant with the smallest median
- * step time for later TEMPO_PREC_MIXED runs on FP32 storage.  Tune on a state like the
- * ones the runs will see: the work of a step depends on the state it starts from.
- * Arguments as tempo_run_dev_f32_c; times_ms (optional, `count` entries) receives each
- * variant's median time, *chosen (optional) the variant kept.  Needs device memory for a copy of
- * every array the step writes. */
+/* No reference counterpart.  Autotuner of the mixed form on FP32 device storage.  For
+ * each of 19 candidates it copies the given state and runs `reps` consecutive steps
+ * (itimestep, itimestep + 1, ...) on the copy -- the caller's arrays are not modified
+ * -- timing kernels with CUDA events on `stream`, and scores the candidate by its
+ * median step time.  Candidates 0-15: every variant of the per-level kernel (block
+ * shape, barriers, register budget) in each order of the points (candidate v: variant
+ * v % 8, order v / 8, as tempo_set_points_variant and tempo_set_points_order take
+ * them), timed over the regime-order and per-level kernels; candidates 16-18: the
+ * sedimentation variants 0-2 (tempo_set_sedim_variant) with the best of 0-15, timed
+ * over the sedimentation kernel.  The best of each group is kept for later runs (all
+ * precisions).  Tune on a state like the ones the runs will see: the work of a step
+ * depends on the state it starts from.  Arguments as tempo_run_dev_f32_c; times_ms
+ * (optional, `count` entries) receives each candidate's median time, *chosen
+ * (optional) the per-level candidate kept.  Needs device memory for a copy of every
+ * array the step writes. */
 int tempo_autotune_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float dt,
                              int itimestep, float *t, float *th, const float *pii,
                              const float *p, const float *w, const float *dz, float *qv,
@@ -285,6 +290,23 @@ int tempo_set_ml_cloud_number_c(tempo_ctx_t *ctx, const double *mean, const doub
 
 /* No reference counterpart.  Selects the per-level kernel variant directly (0..7). */
 int tempo_set_points_variant(tempo_ctx_t *ctx, int variant);
+
+/* No reference counterpart.  Order in which the per-level kernel's threads take the
+ * active points: 0 (the default) = level-major; 1 = grouped by regime (species present
+ * in the input state and the side of 0 C) inside windows of 8192 consecutive
+ * level-major points, one extra kernel per step, so that a warp's points take the same
+ * branches.  The order never changes a result, only which thread computes a point.
+ * tempo_run_dev_f32_noalloc_c always runs level-major. */
+int tempo_set_points_order(tempo_ctx_t *ctx, int order);
+
+/* No reference counterpart.  Selects the sedimentation kernel variant directly: the
+ * number of levels whose loads a sweep issues together, 1 (variant 0, the default),
+ * 2 (1) or 3 (2).  Every variant computes the same values. */
+int tempo_set_sedim_variant(tempo_ctx_t *ctx, int variant);
+
+/* No reference counterpart.  The context's kernel choices: out[0] the per-level kernel
+ * variant, out[1] the point order, out[2] the sedimentation variant. */
+int tempo_tuning_c(tempo_ctx_t *ctx, int out[3]);
 
 /* No reference counterpart.  With on != 0, a run captures its work (counter resets and
  * the four kernels) into a CUDA graph the first time it sees a given argument set

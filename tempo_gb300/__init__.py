@@ -139,6 +139,9 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
                                                 ctypes.POINTER(ctypes.c_float), i,
                                                 ctypes.POINTER(ctypes.c_int)])
     lib.tempo_set_points_variant.argtypes = [_VP, i]
+    lib.tempo_set_points_order.argtypes = [_VP, i]
+    lib.tempo_set_sedim_variant.argtypes = [_VP, i]
+    lib.tempo_tuning_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_int)]
     lib.tempo_set_graphs.argtypes = [_VP, i]
     lib.tempo_tl_dev_c.argtypes = ([_VP, ctypes.POINTER(TempoCfgs), ctypes.c_double, i, i,
                                     ctypes.POINTER(TempoState), ctypes.POINTER(TempoState),
@@ -306,9 +309,11 @@ class TempoContext:
     def autotune_device(self, fields: dict, dt: float, itimestep: int, diags: Optional[dict] = None,
                         bounds=None, stream=None, cfgs: Optional[TempoCfgs] = None,
                         reps: int = 2):
-        """Picks the fastest per-level kernel variant of the mixed form for this
-        workload (tempo_autotune_dev_f32_c) on private copies of the float32 CUDA
-        tensors; returns (chosen variant, per-variant time in ms)."""
+        """Picks the fastest per-level kernel variant, point order and sedimentation
+        variant of the mixed form for this workload (tempo_autotune_dev_f32_c) on
+        private copies of the float32 CUDA tensors; returns (chosen per-level
+        candidate, per-candidate time in ms): candidates 0-15 are variant v % 8 in
+        order v // 8, candidates 16-18 the sedimentation variants."""
         import torch
         lib = load_library()
         cfg = cfgs if cfgs is not None else self.cfgs
@@ -325,12 +330,12 @@ class TempoContext:
             if a is not None:
                 setattr(d, n, a.data_ptr())
         s = stream if stream is not None else torch.cuda.current_stream(p.device)
-        times = (ctypes.c_float * 8)()
+        times = (ctypes.c_float * 19)()
         chosen = ctypes.c_int(-1)
         _check(lib.tempo_autotune_dev_f32_c(
             self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs,
             land.data_ptr() if land is not None else None, *b[6:], ctypes.byref(d),
-            ctypes.c_void_p(s.cuda_stream), int(reps), times, 8, ctypes.byref(chosen)))
+            ctypes.c_void_p(s.cuda_stream), int(reps), times, 19, ctypes.byref(chosen)))
         return chosen.value, [float(x) for x in times]
 
     # ---- derivatives ----------------------------------------------------------------
@@ -395,6 +400,20 @@ class TempoContext:
     def set_points_variant(self, v: int):
         _check(load_library().tempo_set_points_variant(self._h, int(v)))
 
+    def set_points_order(self, order: int):
+        """0: phase A's points level-major (default); 1: grouped by regime."""
+        _check(load_library().tempo_set_points_order(self._h, int(order)))
+
+    def set_sedim_variant(self, v: int):
+        """Levels loaded together by a sedimentation sweep: 0 -> 1, 1 -> 2, 2 -> 3."""
+        _check(load_library().tempo_set_sedim_variant(self._h, int(v)))
+
+    def tuning(self) -> dict:
+        """The context's kernel choices (tempo_tuning_c)."""
+        out = (ctypes.c_int * 3)()
+        _check(load_library().tempo_tuning_c(self._h, out))
+        return dict(points_variant=out[0], points_order=out[1], sedim_variant=out[2])
+
     def aerosol_surface_emissions(self, dt: float, nwfa, nwfa2d, kts: int = 1, stream=None):
         """tempo_aerosol_surface_emissions (driver:516-529) on CUDA tensors."""
         import torch
@@ -422,15 +441,16 @@ class TempoContext:
         _check(load_library().tempo_build_tables_c(self._h, ctypes.byref(ms)))
         return ms.value
 
-    KERNELS = ("prep", "points", "sedim", "final")
+    KERNELS = ("prep", "order", "points", "sedim", "final")
 
     def set_kernel_timing(self, on: bool = True):
-        """Record CUDA events around the four kernels of each later run."""
+        """Record CUDA events around the kernels of each later run."""
         _check(load_library().tempo_set_kernel_timing(self._h, int(bool(on))))
 
     def kernel_times(self) -> dict:
-        """Durations (ms) of the four kernels of the last run; waits for it."""
-        ms = (ctypes.c_float * 4)()
+        """Durations (ms) of the kernels of the last run (the regime-order pair as one
+        entry); waits for it."""
+        ms = (ctypes.c_float * 5)()
         _check(load_library().tempo_kernel_times_c(self._h, ms))
         return dict(zip(self.KERNELS, (float(x) for x in ms)))
 

@@ -95,8 +95,8 @@ __device__ __forceinline__ bool input_present(const StepArgs<T>& a, int i) {
 }
 
 // ---------------------------------------------------------------------------------
-// phase A adjoint: one thread per (level, active slot); primal arrays = the state
-// before the step
+// phase A adjoint: one thread per (level, active slot), in the trajectory's point
+// order; primal arrays = the state before the step
 // ---------------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(128) tempo_points_adjoint_kernel(
@@ -105,7 +105,9 @@ __global__ void __launch_bounds__(128) tempo_points_adjoint_kernel(
     const __grid_constant__ AdjArgs<T> j) {
   using R = Dual<T, IN_N>;
   const long nact = (long)*a.nact;
-  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nact * a.nz) return;
+  const long p = a.ord ? (long)a.ord[q] : q;  // level-major index (regime order of the trajectory)
   if (p >= nact * a.nz) return;
   const int k = (int)(p / nact);
   const long s = p - (long)k * nact;

@@ -96,8 +96,10 @@ struct tempo_ctx {
   std::vector<Mirror> mirrors;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool kernel_timing = false;
-  cudaEvent_t kev[kStepLaunches + 1] = {};
+  cudaEvent_t kev[kStepPhases + 1] = {};
   int points_variant = 0;  // mixed form on FP32 storage (tempo_autotune_dev_f32_c)
+  int points_order = 0;    // phase A's points level-major (0) or in regime order (1)
+  int sedim_variant = 0;   // levels loaded together by a sedimentation sweep: 1, 2, 3
   RadarConsts radar{};     // melting-layer reflectivity (FP64)
   double* d_mlnet = nullptr;  // cloud-number network (tempo_set_ml_cloud_number_c)
   bool use_graphs = false;
@@ -494,8 +496,11 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   const size_t ml_bytes = (a.flags & F_MELT) ? al((size_t)kMeltN * nzs * npad * 8 + nzs * npad) : 0;
   // per-point cloud number of the network only on that path
   const size_t nc_bytes = (a.flags & F_MLNC) ? al(nzs * npad * rsz) : 0;
+  // regime order: a point index per point
+  const bool order = c->points_order != 0;
+  const size_t od_bytes = order ? al(nzs * npad * sizeof(unsigned)) : 0;
   const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes +
-                       sl_bytes + ml_bytes + nc_bytes + 256;
+                       sl_bytes + ml_bytes + nc_bytes + od_bytes + 256;
   if (int rc = ensure_scratch(c, total)) return rc;
   char* sp = (char*)c->scratch;
   a.sd = sp;
@@ -518,10 +523,12 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   sp += ml_bytes;
   a.ncw = nc_bytes ? sp : nullptr;
   sp += nc_bytes;
+  a.ord = order ? (unsigned*)sp : nullptr;
+  sp += od_bytes;
   a.nact = (unsigned int*)sp;
   a.stats = c->d_stats;
   c->last_cols = a.ncol;
-  c->launches = kStepLaunches;
+  c->launches = kStepLaunches + (order ? kOrderLaunches : 0);
   if (!mixed && sizeof(S) != sizeof(double))
     return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
   const bool timed = c->kernel_timing;
@@ -535,7 +542,7 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
       if constexpr (sizeof(S) == sizeof(double)) {
         Tables<double> T{c->t64.t_efrw, c->t64.t_efsw, c->t64.tnc_wev, c->t64.tps_iaus, c->t64.tni_iaus,
                          c->t64.tpi_ide, c->t64.tnccn, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
-        e = launch_step_f64(a, T, c->c64, c->i64, st, ev);
+        e = launch_step_f64(a, T, c->c64, c->i64, st, ev, c->sedim_variant);
         return e == cudaSuccess ? launch_melt_refl(a, c->c64, c->radar, st) : e;
       }
       return cudaErrorInvalidValue;
@@ -543,9 +550,9 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
     Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
                     c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
     if constexpr (sizeof(S) == sizeof(double))
-      e = launch_step_mixed_f64(a, T, c->c32, c->idf, st, ev);
+      e = launch_step_mixed_f64(a, T, c->c32, c->idf, st, ev, c->sedim_variant);
     else
-      e = launch_step_mixed_f32(a, T, c->c32, c->idf, st, ev, c->points_variant);
+      e = launch_step_mixed_f32(a, T, c->c32, c->idf, st, ev, c->points_variant, c->sedim_variant);
     // the melting-layer reflectivity pass (F_MELT) after phase C, outside the timed kernels
     return e == cudaSuccess ? launch_melt_refl(a, c->c64, c->radar, st) : e;
   };
@@ -556,7 +563,8 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   // CUDA graph: captured once per distinct argument set, replayed on the caller's stream
   std::string key((const char*)&a, sizeof a);
   key.push_back((char)c->precision);
-  key.push_back((char)c->points_variant);
+  key.push_back((char)c->points_variant);  // (the regime order changes a.ord)
+  key.push_back((char)c->sedim_variant);
   key.push_back((char)sizeof(S));
   key.push_back((char)timed);  // event-record nodes around the kernels
   cudaGraphExec_t exec = nullptr;
@@ -642,7 +650,7 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
   CUDA_TRY(cudaMemsetAsync(a.nact, 0, sizeof(unsigned int), s));
   Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
                   c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
-  CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->idf, s, nullptr, c->points_variant));
+  CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->idf, s, nullptr, c->points_variant, c->sedim_variant));
   return TEMPO_OK;
 }
 
@@ -857,12 +865,12 @@ int tempo_set_kernel_timing(tempo_ctx_t* c, int on) {
   return TEMPO_OK;
 }
 
-int tempo_kernel_times_c(tempo_ctx_t* c, float ms[4]) {
+int tempo_kernel_times_c(tempo_ctx_t* c, float ms[5]) {
   if (!c || !ms) return fail(TEMPO_ERR_ARG, "NULL argument");
   if (!c->kernel_timing) return fail(TEMPO_ERR_STATE, "kernel timing is off (tempo_set_kernel_timing)");
   CUDA_TRY(cudaSetDevice(c->device));
-  CUDA_TRY(cudaEventSynchronize(c->kev[kStepLaunches]));
-  for (int i = 0; i < kStepLaunches; i++) CUDA_TRY(cudaEventElapsedTime(&ms[i], c->kev[i], c->kev[i + 1]));
+  CUDA_TRY(cudaEventSynchronize(c->kev[kStepPhases]));
+  for (int i = 0; i < kStepPhases; i++) CUDA_TRY(cudaEventElapsedTime(&ms[i], c->kev[i], c->kev[i + 1]));
   return TEMPO_OK;
 }
 
@@ -975,17 +983,25 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, 
       return fail(TEMPO_ERR_NOMEM, "autotune: diagnostic buffers");
     }
   const bool timing = c->kernel_timing;
-  const int saved_variant = c->points_variant;
+  const int saved_variant = c->points_variant, saved_order = c->points_order,
+            saved_sedim = c->sedim_variant;
   int rc = tempo_set_kernel_timing(c, 1);
-  float best = 0.0f;
-  int best_v = saved_variant;
-  // every variant runs the same `reps` consecutive steps from a fresh copy of the state
-  // (the work of a step depends on the state it starts from) and is scored by the
-  // median of its per-step times (single steps of a workload can cost far more than
-  // the others, and by amounts that vary from run to run)
+  float best = 0.0f, best_sed = 0.0f;
+  int best_v = saved_order * kPointsVariants + saved_variant, best_s = saved_sedim;
+  // every candidate runs the same `reps` consecutive steps from a fresh copy of the
+  // state (the work of a step depends on the state it starts from) and is scored by
+  // the median of its per-step times (single steps of a workload can cost far more
+  // than the others, and by amounts that vary from run to run).  Candidates
+  // [0, kPointsCandidates): points variant v % kPointsVariants in point order
+  // v / kPointsVariants, scored by the regime kernel and the points kernel; then the
+  // sedimentation variants with the points candidate kept, scored by that kernel.
   std::vector<float> per_step((size_t)reps);
-  for (int v = 0; v < kPointsVariants && rc == TEMPO_OK; v++) {
-    c->points_variant = v;
+  for (int v = 0; v < kPointsCandidates + kSedimCandidates && rc == TEMPO_OK; v++) {
+    const bool sed = v >= kPointsCandidates;
+    const int pv = sed ? best_v : v;
+    c->points_variant = pv % kPointsVariants;
+    c->points_order = pv / kPointsVariants;
+    c->sedim_variant = sed ? v - kPointsCandidates : saved_sedim;
     float vbest = 0.0f;
     for (int i = 0; i < NIO; i++)
       if (io[i] && cudaMemcpyAsync(cp[i], io[i], ext * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
@@ -994,9 +1010,9 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, 
       RunArrays<float> A{cp[0], cp[1], pii, p, w, dz, cp[2], cp[3], cp[4], cp[5], cp[6],
                          cp[7], cp[8], cp[9], cp[10], cp[11], cp[12], cp[13], cp[14], land_input};
       rc = run_dev(c, cfg, (double)dt, itimestep + r, A, b, diags ? &dcopy : nullptr, s);
-      float ms[kStepLaunches];
+      float ms[kStepPhases];
       if (rc == TEMPO_OK) rc = tempo_kernel_times_c(c, ms);
-      if (rc == TEMPO_OK) per_step[(size_t)r] = ms[1];
+      if (rc == TEMPO_OK) per_step[(size_t)r] = sed ? ms[3] : ms[1] + ms[2];
     }
     if (rc == TEMPO_OK) {
       std::sort(per_step.begin(), per_step.end());
@@ -1005,9 +1021,13 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, 
     }
     if (rc) break;
     if (times_ms && v < count) times_ms[v] = vbest;
-    if (v == 0 || vbest < best) {
+    if (!sed && (v == 0 || vbest < best)) {
       best = vbest;
       best_v = v;
+    }
+    if (sed && (v == kPointsCandidates || vbest < best_sed)) {
+      best_sed = vbest;
+      best_s = v - kPointsCandidates;
     }
   }
   if (!timing) tempo_set_kernel_timing(c, 0);
@@ -1015,10 +1035,30 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, 
   release();
   if (rc) {
     c->points_variant = saved_variant;
+    c->points_order = saved_order;
+    c->sedim_variant = saved_sedim;
     return rc;
   }
-  c->points_variant = best_v;
+  c->points_variant = best_v % kPointsVariants;
+  c->points_order = best_v / kPointsVariants;
+  c->sedim_variant = best_s;
   if (chosen) *chosen = best_v;
+  return TEMPO_OK;
+}
+
+int tempo_tuning_c(tempo_ctx_t* c, int out[3]) {
+  if (!c || !out) return fail(TEMPO_ERR_ARG, "NULL argument");
+  out[0] = c->points_variant;
+  out[1] = c->points_order;
+  out[2] = c->sedim_variant;
+  return TEMPO_OK;
+}
+
+int tempo_set_sedim_variant(tempo_ctx_t* c, int variant) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (variant < 0 || variant >= kSedimCandidates)
+    return fail(TEMPO_ERR_ARG, "sedimentation variant %d outside [0, %d)", variant, kSedimCandidates);
+  c->sedim_variant = variant;
   return TEMPO_OK;
 }
 
@@ -1059,6 +1099,13 @@ int tempo_set_points_variant(tempo_ctx_t* c, int variant) {
   if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
   if (variant < 0 || variant >= kPointsVariants) return fail(TEMPO_ERR_ARG, "variant %d outside [0, %d)", variant, kPointsVariants);
   c->points_variant = variant;
+  return TEMPO_OK;
+}
+
+int tempo_set_points_order(tempo_ctx_t* c, int order) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (order != 0 && order != 1) return fail(TEMPO_ERR_ARG, "point order %d is neither 0 nor 1", order);
+  c->points_order = order;
   return TEMPO_OK;
 }
 
@@ -1159,6 +1206,8 @@ struct DualStep {
         !(a.pmask = B.alloc<uint8_t>(nzs * npad)) || !(a.cmask = B.alloc<uint8_t>(npad)) ||
         !(a.hgt = B.alloc<T>(nzs * npad)) || !(a.nact = B.alloc<unsigned>(1)))
       return fail(TEMPO_ERR_NOMEM, "derivative step: scratch");
+    if (c->points_order && !(a.ord = B.alloc<unsigned>(nzs * npad)))
+      return fail(TEMPO_ERR_NOMEM, "derivative step: point order");
     a.stats = c->d_stats;
     if (cudaMemsetAsync(a.nact, 0, sizeof(unsigned), s) != cudaSuccess ||
         cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s) != cudaSuccess)
@@ -1203,7 +1252,7 @@ int tl_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, temp
                                                (long)(i < 8 ? st.n2 : st.n3), s));
   CUDA_TRY(cudaStreamSynchronize(s));
   c->last_cols = ap.ncol;
-  c->launches = kStepLaunches;
+  c->launches = kStepLaunches + (c->points_order ? kOrderLaunches : 0);
   return TEMPO_OK;
 }
 
@@ -1294,7 +1343,9 @@ int adjoint_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep,
   j.lam_sd = lam_sd;
   j.lam_sr = lam_sr;
   j.colflag = colflag;
-  // shared step bookkeeping of the trajectory
+  // shared step bookkeeping of the trajectory (phase A's adjoint takes its points in
+  // the trajectory's order)
+  ap.ord = st.a.ord;
   for (StepArgs<T>* q : {&aC, &ap}) {
     q->act = st.a.act;
     q->nact = st.a.nact;

@@ -44,7 +44,7 @@ cudaError_t unpack_dual(T* v, T* d, const Dual<T, 1>* src, long n, cudaStream_t 
 }
 
 // step on packed dual state: part 0 = all four kernels, 1 = prep + points, 2 = sedim
-// only, 3 = final only
+// only, 3 = final only (with a.ord, phase A's points in regime order)
 template <class T>
 cudaError_t tl_step(const StepArgs<Dual<T, 1>>& a, const Tables<T>& t, const TempoConsts<T>& c,
                     const IslandConsts<Dual<T, 1>>& ci, cudaStream_t s, int part) {
@@ -55,6 +55,7 @@ cudaError_t tl_step(const StepArgs<Dual<T, 1>>& a, const Tables<T>& t, const Tem
   const unsigned gpts = points_grid(a.ncol, a.nz);
   if (part == 0 || part == 1) {
     tempo_prep_kernel<D1, D1><<<gcol, kBlock, 0, s>>>(a, c, ci);
+    if (cudaError_t e = launch_regime_order(a, s)) return e;
     tempo_points_kernel<D1, D1, 0><<<gpts, kBlock, 0, s>>>(a, t, c, ci);
   }
   if (part == 0 || part == 2) tempo_sedim_kernel<D1, D1><<<gcol, kBlock, 0, s>>>(a);

@@ -19,15 +19,17 @@ template <class I> struct IslandConsts;
 // tempo_step_f64.cu (FP64 drop-in, compiled without FMA contraction)
 cudaError_t launch_step_f64(const StepArgs<double>& a, const Tables<double>& t,
                             const TempoConsts<double>& c64, const IslandConsts<double>& i64,
-                            cudaStream_t s, const cudaEvent_t* ev);
+                            cudaStream_t s, const cudaEvent_t* ev, int sedim_variant);
 
-// tempo_step_f32.cu (mixed precision: FP32 bulk, double-float islands)
+// tempo_step_f32.cu (mixed precision: FP32 bulk, double-float islands); sedim_variant
+// in [0, kSedimVariants) (tempo_step.cuh: sedim_group)
 cudaError_t launch_step_mixed_f32(const StepArgs<float>& a, const Tables<float>& t,
                                   const TempoConsts<float>& c32, const IslandConsts<df>& idf,
-                                  cudaStream_t s, const cudaEvent_t* ev, int points_variant);
+                                  cudaStream_t s, const cudaEvent_t* ev, int points_variant,
+                                  int sedim_variant);
 cudaError_t launch_step_mixed_f64(const StepArgs<double>& a, const Tables<float>& t,
                                   const TempoConsts<float>& c32, const IslandConsts<df>& idf,
-                                  cudaStream_t s, const cudaEvent_t* ev);
+                                  cudaStream_t s, const cudaEvent_t* ev, int sedim_variant);
 // tempo_points_f32.cu: points kernel of the mixed form on FP32 storage, variant v in
 // [0, kPointsVariants) (tempo_step.cuh describes the variants)
 cudaError_t launch_points_mixed_f32(int v, const StepArgs<float>& a, const Tables<float>& t,
@@ -69,10 +71,18 @@ template <class S>
 cudaError_t launch_melt_refl(const StepArgs<S>& a, const TempoConsts<double>& c, const RadarConsts& rc,
                              cudaStream_t s);
 
-// number of points-kernel variants of the mixed form on FP32 storage
+// number of points-kernel variants of the mixed form on FP32 storage, and of the
+// autotuner's candidates (each variant in level-major and in regime order)
 constexpr int kPointsVariants = 8;
-// kernels launched per step (prep, points, sedim, final)
+constexpr int kPointsCandidates = 2 * kPointsVariants;
+// number of sedimentation-kernel variants (tempo_step.cuh: sedim_group)
+constexpr int kSedimCandidates = 3;
+// kernels launched per step (prep, points, sedim, final), and one more when phase A's
+// points run in regime order
 constexpr int kStepLaunches = 4;
+constexpr int kOrderLaunches = 1;
+// timed intervals of a step: prep, regime order, points, sedim, final
+constexpr int kStepPhases = 5;
 
 // tempo_tables.cu (FP64 table construction on the GPU)
 struct DevTables64 {

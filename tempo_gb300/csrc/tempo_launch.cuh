@@ -19,9 +19,9 @@ inline void record_event(cudaEvent_t ev, cudaStream_t s) {
     cudaEventRecord(ev, s);
 }
 
-inline unsigned points_grid(long ncol, int nz) {
+inline unsigned points_grid(long ncol, int nz, int block = kBlock) {
   const unsigned long long npts = (unsigned long long)ncol * (unsigned long long)nz;
-  return (unsigned)((npts + kBlock - 1) / kBlock);
+  return (unsigned)((npts + block - 1) / block);
 }
 
 // points kernel, variant V; its grid covers every column's levels and threads past the
@@ -29,16 +29,31 @@ inline unsigned points_grid(long ncol, int nz) {
 template <class R, class S, int V>
 cudaError_t launch_points(const StepArgs<S>& a, const Tables<Cst<R>>& T, const TempoConsts<Cst<R>>& c,
                           const IslandConsts<Isl<R>>& ci, cudaStream_t s) {
-  tempo_points_kernel<R, S, V><<<points_grid(a.ncol, a.nz), kBlock, 0, s>>>(a, T, c, ci);
+  constexpr int block = points_block(V);
+  tempo_points_kernel<R, S, V><<<points_grid(a.ncol, a.nz, block), block, 0, s>>>(a, T, c, ci);
   return cudaGetLastError();
 }
 
-// ev (optional, kStepLaunches + 1 events): recorded before each kernel and after the
-// last, for per-kernel durations measured on the launching stream.  points() launches
-// the points kernel (the variant is the caller's choice).
+// regime order of phase A's points into a.ord (nothing when a.ord is NULL); the grid
+// covers every column's levels, windows past the active points return at once
+template <class S>
+cudaError_t launch_regime_order(const StepArgs<S>& a, cudaStream_t s) {
+  if (!a.ord || a.ncol == 0) return cudaSuccess;
+  constexpr unsigned long long per = kRegimeWindow;
+  const unsigned greg = (unsigned)(((unsigned long long)a.ncol * (unsigned long long)a.nz + per - 1) / per);
+  tempo_regime_order_kernel<S><<<greg, kRegimeBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ev (optional, kStepPhases + 1 events): recorded before prep, before the regime
+// kernels (an empty interval when a.ord is NULL), before the points, sedimentation and
+// final kernels and after the last, for per-kernel durations measured on the launching
+// stream.  points() launches the points kernel (the variant is the caller's choice).
+// With a.ord the regime kernels order phase A's points first.
+// sedimentation variant sv (sedim_group) for the explicit path
 template <class R, class S, class Points>
 cudaError_t launch_step(const StepArgs<S>& a, const TempoConsts<Cst<R>>& c, const IslandConsts<Isl<R>>& ci,
-                        cudaStream_t s, const cudaEvent_t* ev, Points&& points) {
+                        cudaStream_t s, const cudaEvent_t* ev, Points&& points, int sv = 0) {
   const unsigned long long ncol = (unsigned long long)a.ncol;
   if (ncol == 0) return cudaSuccess;
   const unsigned gcol = (unsigned)((ncol + kBlock - 1) / kBlock);
@@ -46,16 +61,23 @@ cudaError_t launch_step(const StepArgs<S>& a, const TempoConsts<Cst<R>>& c, cons
   if (ev) record_event(ev[0], s);
   tempo_prep_kernel<R, S><<<gcol, kBlock, 0, s>>>(a, c, ci);
   if (ev) record_event(ev[1], s);
-  cudaError_t e = points();
+  cudaError_t e = launch_regime_order(a, s);
   if (e != cudaSuccess) return e;
   if (ev) record_event(ev[2], s);
+  e = points();
+  if (e != cudaSuccess) return e;
+  if (ev) record_event(ev[3], s);
   if (a.flags & F_SEMI)
     tempo_sedim_semi_kernel<R, S><<<gcol, kBlock, 0, s>>>(a, c, ci);
+  else if (sv == 1)
+    tempo_sedim_kernel<R, S, sedim_group(1)><<<gcol, kBlock, 0, s>>>(a);
+  else if (sv == 2)
+    tempo_sedim_kernel<R, S, sedim_group(2)><<<gcol, kBlock, 0, s>>>(a);
   else
-    tempo_sedim_kernel<R, S><<<gcol, kBlock, 0, s>>>(a);
-  if (ev) record_event(ev[3], s);
-  tempo_final_kernel<R, S><<<gpts, kBlock, 0, s>>>(a, c, ci);
+    tempo_sedim_kernel<R, S, sedim_group(0)><<<gcol, kBlock, 0, s>>>(a);
   if (ev) record_event(ev[4], s);
+  tempo_final_kernel<R, S><<<gpts, kBlock, 0, s>>>(a, c, ci);
+  if (ev) record_event(ev[5], s);
   return cudaGetLastError();
 }
 

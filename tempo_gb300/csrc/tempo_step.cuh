@@ -66,6 +66,14 @@ struct FwdIO {
   static constexpr bool forward = true;
 };
 
+// a barrier of the block when B (the lockstep variants of the points kernel) and go
+// (the same for every thread of the block)
+template <bool B>
+__device__ __forceinline__ void block_sync(bool go) {
+  if constexpr (B)
+    if (go) __syncthreads();
+}
+
 // the time step in the bulk type, its reciprocal, and the time step in the island type
 // (host-computed, so that no kernel of the mixed form converts or divides in FP64)
 template <class R, class S> __device__ __forceinline__ R step_dt(const StepArgs<S>& a) {
@@ -311,27 +319,132 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
   atomicAdd(a.stats, 1ull);
 }
 
+// ---------------------------------------------------------------------------------
+// regime order of phase A's points
+// ---------------------------------------------------------------------------------
+// Phase A's work at a point depends on which species are present and on the side of
+// 0 C (ice nucleation, deposition and riming below it, melting above).  In level-major
+// order a warp's 32 points mix clear air with cloud.  Inside each window of W
+// consecutive level-major points, the points are grouped by regime (the regimes with
+// more species first), so that a warp's points take the same branches.  Keeping the
+// grouping inside a window keeps the writes of phase A to a window's scratch sectors
+// close together in time (a global grouping scatters them over the whole step and
+// costs partial-sector writes).  The order decides only which thread computes a
+// point, never its value.
+constexpr int kRegimeBlock = 512, kRegimeItems = 16;
+constexpr int kRegimeWindow = kRegimeBlock * kRegimeItems;  // 8192 points
+
+// bits 1-5: cloud, rain, ice, snow, graupel present (> r1) in the input state; bit 0:
+// below 0 C.  Compared in FP32: the regime only groups points.
+template <class S>
+__device__ __forceinline__ int point_regime(const StepArgs<S>& a, long e) {
+  const float t = (a.flags & F_USE_T) ? float(a.t[e]) : float(a.th[e]) * float(a.pii[e]);
+  constexpr float q1 = float(r1);
+  return (t < float(t0) ? 1 : 0) | (float(a.qc[e]) > q1 ? 2 : 0) | (float(a.qr[e]) > q1 ? 4 : 0) |
+         (float(a.qi[e]) > q1 ? 8 : 0) | (float(a.qs[e]) > q1 ? 16 : 0) |
+         (float(a.qg[e]) > q1 ? 32 : 0);
+}
+
+// one block per window: the regime of each of its points, then their positions in the
+// window (regime by regime from regime 63 down; inside a regime, warp w's points after
+// those of the warps below w, each warp's in the order of its items and lanes)
+template <class S>
+__global__ void __launch_bounds__(kRegimeBlock) tempo_regime_order_kernel(const __grid_constant__ StepArgs<S> a) {
+  constexpr int kWarps = kRegimeBlock / 32;
+  __shared__ unsigned wcnt[kWarps][kRegimes];  // per warp: count, then offset in the window
+  __shared__ unsigned start[kRegimes];         // first position of a regime in the window
+  __shared__ unsigned wtot;
+  const long nact = (long)*a.nact, npts = nact * a.nz;
+  const long q0 = (long)blockIdx.x * kRegimeWindow;
+  if (q0 >= npts) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < kWarps * kRegimes; i += kRegimeBlock) (&wcnt[0][0])[i] = 0;
+  __syncthreads();
+  int reg[kRegimeItems];
+  unsigned rank[kRegimeItems];
+  // the regimes first (independent loads), then the ranks
+#pragma unroll
+  for (int j = 0; j < kRegimeItems; j++) {
+    const long q = q0 + (long)j * kRegimeBlock + threadIdx.x;
+    reg[j] = -1;
+    if (q < npts) {
+      const int k = (int)(q / nact);
+      const long s = q - (long)k * nact;
+      reg[j] = point_regime(a, col_geom(a, a.act[s]).base + (long)k * a.NI);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kRegimeItems; j++) {
+    const int r = reg[j];
+    const unsigned m = __match_any_sync(0xffffffffu, r);
+    const unsigned before = r >= 0 ? wcnt[wid][r] : 0u;
+    __syncwarp();
+    if (r >= 0 && lane == __ffs(m) - 1) wcnt[wid][r] = before + (unsigned)__popc(m);
+    __syncwarp();
+    rank[j] = before + (unsigned)__popc(m & ((1u << lane) - 1u));
+  }
+  __syncthreads();
+  // threads 0-63 (two warps), thread t for regime i = 63 - t: per-warp offsets, the
+  // regime's count in the window, and the sum of the counts of the regimes above i (a
+  // shuffle scan per warp; the second warp adds the first warp's total below)
+  if (threadIdx.x < kRegimes) {
+    const int t = threadIdx.x, i = kRegimes - 1 - t;
+    unsigned tot = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) {
+      const unsigned n = wcnt[w][i];
+      wcnt[w][i] = tot;
+      tot += n;
+    }
+    unsigned inc = tot;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned v = __shfl_up_sync(0xffffffffu, inc, d);
+      if (lane >= d) inc += v;
+    }
+    if (t == 31) wtot = inc;
+    start[i] = inc - tot;
+  }
+  __syncthreads();
+  if (threadIdx.x >= 32 && threadIdx.x < kRegimes) start[kRegimes - 1 - threadIdx.x] += wtot;
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kRegimeItems; j++)
+    if (reg[j] >= 0) {
+      const long pos = q0 + (long)(start[reg[j]] + wcnt[wid][reg[j]] + rank[j]);
+      if (pos < npts) a.ord[pos] = (unsigned)(q0 + (long)j * kRegimeBlock + threadIdx.x);
+    }
+}
+
 // One stage of phase A, each followed by thermo_vars in the caller: 0 = process
 // rates, limiter, tendency sums, provisional update and checks on temporaries
 // (main:420-522); 1 = saturation adjustment (main:530-560); 2 = rain evaporation
 // (main:563-588).
-template <class R>
+// With kSync and go, a block barrier follows each process group of stage 0 (all
+// threads of the block call the stage).
+template <class R, bool kSync = false>
 __device__ __forceinline__ void points_stage(int stage, Lev<R>& L, Tend<R>& td, const Tables<Cst<R>>& T,
                                              const IslandConsts<Isl<R>>& ci, uint32_t f, R w, R dt,
                                              R odt, Isl<R> dti, R ncsave, R ncsave_cond, R nwfa_in,
-                                             R nifa_in) {
+                                             R nifa_in, bool go = false) {
   using I = Isl<R>;
   const bool has_nc = f & F_NC, has_nwfa = f & F_NWFA, has_nifa = f & F_NIFA, hail = f & F_HAIL;
   if (stage == 0) {
     if (!(f & F_NOMICRO)) {
       warm_rain(L, td, T, odt);
+      block_sync<kSync>(go);
       rain_snow_rain_graupel(L, td, T, odt);
+      block_sync<kSync>(go);
       ice_nucleation(L, td, T, w, f, dt, odt);
+      block_sync<kSync>(go);
       const R t1s = t1_subl_of(L);
       ice_processes(L, td, T, w, t1s, odt);
+      block_sync<kSync>(go);
       riming(L, td, T, odt);
+      block_sync<kSync>(go);
       melting(L, td, t1s, f, dt, odt);
       if (has_nwfa || has_nifa) aerosol_scavenging(L, td, odt);
+      block_sync<kSync>(go);
     }
     check_over_depletion(L, td, odt);
     sum_tendencies(L, td);
@@ -393,13 +506,22 @@ __device__ __forceinline__ void points_stage(int stage, Lev<R>& L, Tend<R>& td, 
   }
 }
 
-// Variants of the points kernel (picked per context by tempo_autotune_c): bit 0 drives
-// the stages from one loop with a single copy of thermo_vars (smaller code, more live
-// registers) instead of inlining each stage; bits 1-2 select the minimum resident
-// blocks per SM asked of the register allocator (1, 3, 4 or 5 blocks of 128 threads:
-// no cap, 170, 128 or 102 registers per thread).
+// Variants of the points kernel (picked per context by tempo_autotune_c).  Bit 0 = 0:
+// blocks of 128 threads, bits 1-2 select the minimum resident blocks per SM asked of
+// the register allocator (1, 3, 4 or 5: no cap, 170, 128 or 102 registers per thread).
+// Bit 0 = 1 (lockstep): the warps of a block run the stages and the process groups of
+// stage 0 between block barriers, so that an SM fetches each part of the kernel's code
+// for all of its warps at once (a thread's path through phase A is a long run of code
+// executed once, longer than the instruction cache); bits 1-2 select the block (128,
+// 256, 512 or 384 threads) and the resident blocks per SM asked (4, 2, 1, 1: 128, 128,
+// 128 and 170 registers per thread).
+__host__ __device__ constexpr int points_block(int v) {
+  return (v & 1) ? ((v >> 1) & 3) == 0 ? 128 : ((v >> 1) & 3) == 1 ? 256 : ((v >> 1) & 3) == 2 ? 512 : 384
+                 : 128;
+}
 __host__ __device__ constexpr int points_min_blocks(int v) {
-  return ((v >> 1) & 3) == 0 ? 1 : ((v >> 1) & 3) + 2;
+  return (v & 1) ? ((v >> 1) & 3) == 0 ? 4 : ((v >> 1) & 3) == 1 ? 2 : 1
+                 : ((v >> 1) & 3) == 0 ? 1 : ((v >> 1) & 3) + 2;
 }
 
 // mass- and number-weighted fall speeds of rain at a level with rain (rain_fallspeed,
@@ -433,12 +555,13 @@ __device__ __forceinline__ void graupel_speeds(const Lev<R>& L, const TempoConst
 // ---------------------------------------------------------------------------------
 // points: phase A at one (level, active slot)
 // ---------------------------------------------------------------------------------
-// Phase A at point (level k, active slot s); outputs go through the I/O policy.
+// Phase A at point (level k, active slot s); outputs go through the I/O policy.  go:
+// the block's barriers of the lockstep variants (V odd) are taken.
 template <class R, class S, int V, class IO>
 __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<Cst<R>>& T,
                                              const TempoConsts<Cst<R>>& cst,
                                              const IslandConsts<Isl<R>>& ci, int k, long s,
-                                             const IO& io) {
+                                             const IO& io, bool go = false) {
   using I = Isl<R>;
   const int nz = a.nz;
   const long c = a.act[s];
@@ -486,35 +609,27 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   // Where no later reader needs them, the thermodynamic fields are not recomputed:
   // rain evaporation reads them only where rain exists (it returns at once otherwise),
   // and after the last stage only the fall speeds' rhof and visco are read
-  // (thermo_tail).  The values read are the same as with every call made.
-  if constexpr (V & 1) {
-    int stage = 0;
-#pragma unroll 1
-    for (;;) {
-      if (stage == 3 || (stage == 2 && !L.l_qr))
-        thermo_tail(L);
-      else
-        thermo(L);
-      if (stage > 2) break;
-      points_stage(stage, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
-      stage = stage == 0 ? (do_cond ? 1 : do_evap ? 2 : 3) : stage == 1 ? (do_evap ? 2 : 3) : 3;
-    }
-  } else {
+  // (thermo_tail).  The values read are the same as with every call made.  The
+  // lockstep variants put a block barrier after each stage when go (do_cond and do_evap
+  // are the same for every thread).
+  constexpr bool kSync = (V & 1) != 0;
+  block_sync<kSync>(go);
+  thermo(L);
+  points_stage<R, kSync>(0, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in, go);
+  if (do_cond) {
     thermo(L);
-    points_stage(0, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
-    if (do_cond) {
-      thermo(L);
-      points_stage(1, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
-    }
-    if (do_evap) {
-      if (L.l_qr)
-        thermo(L);
-      else
-        thermo_tail(L);
-      points_stage(2, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in);
-    }
-    thermo_tail(L);
+    points_stage<R, kSync>(1, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in, go);
+    block_sync<kSync>(go);
   }
+  if (do_evap) {
+    if (L.l_qr)
+      thermo(L);
+    else
+      thermo_tail(L);
+    points_stage<R, kSync>(2, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in, go);
+    block_sync<kSync>(go);
+  }
+  thermo_tail(L);
 
   // fall-speed candidates (main:1770-1977), unfilled; < 0 marks "absent"
   const TempoConsts<Cst<R>>& cc = cst;
@@ -607,15 +722,23 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
 }
 
 template <class R, class S, int V>
-__global__ void __launch_bounds__(128, points_min_blocks(V)) tempo_points_kernel(const __grid_constant__ StepArgs<S> a,
+__global__ void __launch_bounds__(points_block(V), points_min_blocks(V)) tempo_points_kernel(const __grid_constant__ StepArgs<S> a,
                                                             const __grid_constant__ Tables<Cst<R>> T,
                                                             const __grid_constant__ TempoConsts<Cst<R>> cst,
                                                             const __grid_constant__ IslandConsts<Isl<R>> ci) {
-  const long nact = (long)*a.nact;
-  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nact * a.nz) return;
+  const long nact = (long)*a.nact, npts = nact * a.nz;
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  // lockstep variants: a block whose threads all have points takes the barriers; the
+  // last, partial block runs without them (its threads past the points return)
+  const bool go = (V & 1) && (long)(blockIdx.x + 1) * blockDim.x <= npts;
+  if (q >= npts) return;  // (never in a block with go)
+  long p = a.ord ? (long)a.ord[q] : q;  // level-major index of the point
+  if (p >= npts) {  // never for an order built by tempo_regime_order_kernel
+    if (!go) return;
+    p = npts - 1;
+  }
   const int k = (int)(p / nact);
-  points_point<R, S, V>(a, T, cst, ci, k, p - (long)k * nact, FwdIO<S>{a});
+  points_point<R, S, V>(a, T, cst, ci, k, p - (long)k * nact, FwdIO<S>{a}, go);
 }
 
 // ---------------------------------------------------------------------------------
@@ -754,7 +877,13 @@ __device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dz
 // Phase B on the column of active slot s.  SEMI: rain and graupel by the
 // semi-Lagrangian scheme (semi_sedi_flag, main:599-613, 640-671), which rechecks the
 // species and recomputes their fall speeds after every substep (needs cst and ci).
-template <class R, class S, bool SEMI>
+// Variants of the sedimentation kernel (picked per context by the autotuner): the
+// number of levels whose loads a sweep issues together, 1, 2 or 3 (more loads in flight
+// per thread against more registers per thread; 4 and 8 were measured slower still).
+constexpr int kSedimVariants = 3;
+__host__ __device__ constexpr int sedim_group(int v) { return v == 0 ? 1 : v == 1 ? 2 : 3; }
+
+template <class R, class S, bool SEMI, int G = 1>
 __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoConsts<Cst<R>>* cst,
                                              const IslandConsts<Isl<R>>* ci, long s) {
   using I = Isl<R>;
@@ -819,7 +948,10 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
     if (ktop == nz) ktop = nz - 1;
   };
   // one substep on a field whose fall speed sits in the R scratch (sedimentation,
-  // main:1516-1559): fluxes from the pre-substep state, level nz first, then ktop..1
+  // main:1516-1559): fluxes from the pre-substep state, level nz first, then ktop..1.
+  // The levels below ktop go in groups of G: a group's loads are issued
+  // together (no level's update reads another level's updated values), then the
+  // group's levels are updated in the serial order and stored.
   auto sweep = [&](int fx, int ften, int fv, double limit, int steps, int ktop, I* precip) {
     I* x = sd + fx * fsd;
     I* ten = sd + ften * fsd;
@@ -838,13 +970,36 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
       x[k * kSlotTile] = Max(lim, x[k * kSlotTile] - s_top * odz[k * kSlotTile] * cx);
       I s_up = (ktop == nz - 1) ? s_top : I(vt[ktop * kSlotTile]) * x[ktop * kSlotTile];
       I s0 = (nz == 1) ? s_top : I(vt[0]) * x[0];
-      for (k = ktop - 1; k >= 0; k--) {
-        const I s_k = I(vt[k * kSlotTile]) * x[k * kSlotTile];
-        const I dflux = s_up - s_k;
-        ten[k * kSlotTile] = ten[k * kSlotTile] + dflux * ozr[k * kSlotTile] * osteps;
-        x[k * kSlotTile] = Max(lim, x[k * kSlotTile] + dflux * odz[k * kSlotTile] * cx);
-        if (k == 0) s0 = s_k;
-        s_up = s_k;
+      for (k = ktop - 1; k >= 0; k -= G) {
+        R gv[G];
+        I gx[G], gt[G], go[G], gz[G];
+#pragma unroll
+        for (int u = 0; u < G; u++)
+          if (u <= k) {
+            const long o = (long)(k - u) * kSlotTile;
+            gv[u] = vt[o];
+            gx[u] = x[o];
+            gt[u] = ten[o];
+            go[u] = odz[o];
+            gz[u] = ozr[o];
+          }
+#pragma unroll
+        for (int u = 0; u < G; u++)
+          if (u <= k) {
+            const I s_k = I(gv[u]) * gx[u];
+            const I dflux = s_up - s_k;
+            gt[u] = gt[u] + dflux * gz[u] * osteps;
+            gx[u] = Max(lim, gx[u] + dflux * go[u] * cx);
+            if (k - u == 0) s0 = s_k;
+            s_up = s_k;
+          }
+#pragma unroll
+        for (int u = 0; u < G; u++)
+          if (u <= k) {
+            const long o = (long)(k - u) * kSlotTile;
+            ten[o] = gt[u];
+            x[o] = gx[u];
+          }
       }
       if (precip && x[0] > low_limit_mass_for_precip) *precip = *precip + s0 * dti * osteps;
       return;
@@ -856,14 +1011,37 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
     x[k * kSlotTile] = Max(lim, x[k * kSlotTile] - s_top * odz * dti * osteps);
     I s_up = (ktop == nz - 1) ? s_top : I(vt[ktop * kSlotTile]) * x[ktop * kSlotTile];
     I s0 = (nz == 1) ? s_top : I(vt[0]) * x[0];
-    for (k = ktop - 1; k >= 0; k--) {
-      I s_k = I(vt[k * kSlotTile]) * x[k * kSlotTile];
-      odz = 1.0 / ldi<I>(dzp + k * NI);
-      orho = 1.0 / rho[k * kSlotTile];
-      ten[k * kSlotTile] = ten[k * kSlotTile] + (s_up - s_k) * odz * osteps * orho;
-      x[k * kSlotTile] = Max(lim, x[k * kSlotTile] + (s_up - s_k) * odz * dti * osteps);
-      if (k == 0) s0 = s_k;
-      s_up = s_k;
+    for (k = ktop - 1; k >= 0; k -= G) {
+      R gv[G];
+      I gx[G], gt[G], gd[G], gr[G];
+#pragma unroll
+      for (int u = 0; u < G; u++)
+        if (u <= k) {
+          const long o = (long)(k - u) * kSlotTile;
+          gv[u] = vt[o];
+          gx[u] = x[o];
+          gt[u] = ten[o];
+          gd[u] = ldi<I>(dzp + (long)(k - u) * NI);
+          gr[u] = rho[o];
+        }
+#pragma unroll
+      for (int u = 0; u < G; u++)
+        if (u <= k) {
+          const I s_k = I(gv[u]) * gx[u];
+          odz = 1.0 / gd[u];
+          orho = 1.0 / gr[u];
+          gt[u] = gt[u] + (s_up - s_k) * odz * osteps * orho;
+          gx[u] = Max(lim, gx[u] + (s_up - s_k) * odz * dti * osteps);
+          if (k - u == 0) s0 = s_k;
+          s_up = s_k;
+        }
+#pragma unroll
+      for (int u = 0; u < G; u++)
+        if (u <= k) {
+          const long o = (long)(k - u) * kSlotTile;
+          ten[o] = gt[u];
+          x[o] = gx[u];
+        }
     }
     if (precip && x[0] > low_limit_mass_for_precip) *precip = *precip + s0 * dti * osteps;
   };
@@ -1012,11 +1190,11 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
   sc[SC_PC * cs] = prec_c;
 }
 
-template <class R, class S>
+template <class R, class S, int G = 1>
 __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant__ StepArgs<S> a) {
   const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= (long)*a.nact) return;
-  sedim_column<R, S, false>(a, nullptr, nullptr, s);
+  sedim_column<R, S, false, G>(a, nullptr, nullptr, s);
 }
 // phase B with semi-Lagrangian rain and graupel (F_SEMI), one thread per active column
 template <class R, class S>
@@ -1207,9 +1385,11 @@ template <class R, class S>
 __global__ void __launch_bounds__(128) tempo_final_kernel(const __grid_constant__ StepArgs<S> a,
                                                            const __grid_constant__ TempoConsts<Cst<R>> cst,
                                                            const __grid_constant__ IslandConsts<Isl<R>> ci) {
-  const long nact = (long)*a.nact;
-  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nact * a.nz) return;
+  const long nact = (long)*a.nact, npts = nact * a.nz;
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= npts) return;
+  const long p = a.ord ? (long)a.ord[q] : q;  // level-major index (phase A's point order)
+  if (p >= npts) return;
   const int k = (int)(p / nact);
   final_point<R, S>(a, cst, ci, k, p - (long)k * nact, FwdIO<S>{a});
 }

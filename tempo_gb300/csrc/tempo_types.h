@@ -113,7 +113,12 @@ struct StepArgs {
                         // tempo_set_ml_cloud_number_c
   void* ncw;          // R plane: the network's cloud number per point (F_MLNC)
   const S *qc_bl, *qcfrac_bl;  // boundary-layer cloud water and fraction (F_BLRE)
+  // phase A's points in regime order: thread q takes level-major point ord[q] (point p
+  // at level p / nact of slot p % nact); NULL = level-major order
+  unsigned* ord;
 };
+// regimes of a point (tempo_step.cuh: point_regime)
+constexpr int kRegimes = 64;
 // size of the cloud-number network: scaler means and variances (7 + 7), weights00
 // (24 x 7, column-major), bias00 (24), weights01 (24), bias01 (1)
 constexpr int kMlNet = 7 + 7 + 168 + 24 + 24 + 1;

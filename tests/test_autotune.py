@@ -1,6 +1,6 @@
 """The autotuner of the mixed form (tempo_autotune_dev_f32_c): it leaves the caller's
-state untouched, reports a time for every per-level kernel variant, keeps the fastest,
-and every variant computes the same step."""
+state untouched, reports a time for every per-level kernel variant in both point
+orders, keeps the fastest, and every variant and order computes the same step."""
 import numpy as np
 import pytest
 
@@ -25,9 +25,12 @@ def test_autotune_picks_fastest_and_keeps_state(tg):
     torch.cuda.synchronize()
     for k in f:
         assert torch.equal(f[k], before[k]), k
-    assert 0 <= chosen < 8
-    assert all(t > 0 for t in times)
-    assert times[chosen] == min(times)
+    assert 0 <= chosen < 16
+    assert len(times) == 19 and all(t > 0 for t in times)
+    assert times[chosen] == min(times[:16])
+    tun = ctx.tuning()
+    assert (tun["points_variant"], tun["points_order"]) == (chosen % 8, chosen // 8)
+    assert times[16 + tun["sedim_variant"]] == min(times[16:])
 
 
 def test_every_variant_computes_the_same_step(tg):
@@ -51,6 +54,39 @@ def test_every_variant_computes_the_same_step(tg):
             assert np.allclose(a, b, rtol=1e-6, atol=1e-30), (v, k, float(np.abs(a - b).max()))
 
 
+@pytest.mark.parametrize("precision,variant", [("mixed", 4), ("mixed", 5), ("fp64", 0)])
+def test_regime_order_is_bit_identical(tg, precision, variant):
+    """The regime order changes only which thread computes a point: two steps in
+    regime order and in level-major order give identical bits in every field (variant 5
+    runs its blocks in lockstep)."""
+    torch = pytest.importorskip("torch")
+    from tempo_gb300 import workloads as W
+    outs = []
+    for order in (0, 1):
+        ctx = tg.TempoContext(build_tables=True, cfgs=tg.default_cfgs(hailaware_flag=0))
+        if precision == "mixed":
+            ctx.set_precision(tg.PREC_MIXED)
+            ctx.set_points_variant(variant)
+            f, d = _fields(W, torch)
+        else:
+            f, d = _fields(W, torch)
+            f = {k: v.double() for k, v in f.items()}
+            d = {k: v.double() for k, v in d.items()}
+        ctx.set_points_order(order)
+        ctx.set_kernel_timing(True)
+        for it in (1, 2):
+            ctx.run_device(f, 30.0, it, diags=d)
+        times = ctx.kernel_times()
+        stats = ctx.stats()
+        torch.cuda.synchronize()
+        if order:
+            assert times["order"] > 0
+        assert stats["launches"] == 4 + order
+        outs.append({k: x.cpu().numpy() for k, x in list(f.items()) + list(d.items())})
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k], equal_nan=True), k
+
+
 def test_graph_replay_matches_direct_launches(tg):
     """Three steps replayed from captured CUDA graphs give the same state as three
     directly launched steps."""
@@ -68,3 +104,29 @@ def test_graph_replay_matches_direct_launches(tg):
         outs.append({k: x.cpu().numpy() for k, x in list(f.items()) + list(d.items())})
     for k in outs[0]:
         assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_sedim_variants_are_bit_identical(tg, precision):
+    """The sedimentation variants change only how many levels' loads a sweep issues
+    together: two steps with each give identical bits in every field."""
+    torch = pytest.importorskip("torch")
+    from tempo_gb300 import workloads as W
+    outs = []
+    for sv in range(3):
+        ctx = tg.TempoContext(build_tables=True, cfgs=tg.default_cfgs(hailaware_flag=0))
+        f, d = _fields(W, torch)
+        if precision == "mixed":
+            ctx.set_precision(tg.PREC_MIXED)
+        else:
+            f = {k: v.double() for k, v in f.items()}
+            d = {k: v.double() for k, v in d.items()}
+        ctx.set_sedim_variant(sv)
+        assert ctx.tuning()["sedim_variant"] == sv
+        for it in (1, 2):
+            ctx.run_device(f, 30.0, it, diags=d)
+        torch.cuda.synchronize()
+        outs.append({k: x.cpu().numpy() for k, x in list(f.items()) + list(d.items())})
+    for o in outs[1:]:
+        for k in outs[0]:
+            assert np.array_equal(outs[0][k], o[k], equal_nan=True), k
