@@ -122,12 +122,15 @@ int tempo_ctx_destroy(tempo_ctx_t *ctx);
 int tempo_set_precision(tempo_ctx_t *ctx, int precision);
 
 /* tempo_run (src/module_mp_tempo_driver.F90:187-513) on host arrays of doubles (the
- * reference's default kind_phys).  Copies the tile to the device, runs the step on
- * the context's stream, copies results back and synchronises.  Optional arrays: t
- * or (th and pii); nc, nwfa, nifa, ng, qb, land_input, qcfrac, qifrac and the *_bl /
- * thten_* inputs (the latter are accepted and, as in the reference, unused).
- * qc_bl with qcfrac_bl selects the reference's ML effective-radius path and returns
- * TEMPO_ERR_UNSUPPORTED. */
+ * reference's default kind_phys).  Copies the tile to the device, runs the step,
+ * copies results back and synchronises.  Large tiles (from 2^19 columns) go in up to
+ * 8 slabs of rows j, each slab's copies on two copy streams overlapping the other
+ * slabs' steps on the context's stream; only the tile's rows are copied.  Optional
+ * arrays: t or (th and pii); nc, nwfa, nifa, ng, qb, land_input, qcfrac, qifrac and
+ * the *_bl / thten_* inputs (qcfrac, qifrac, qvten_bl, qcten_bl, qiten_bl, thten_*
+ * are accepted and, as in the reference, unused).  qc_bl with qcfrac_bl adds the
+ * boundary-layer cloud to re_cloud (main:832-857) and needs the cloud-number network
+ * (tempo_set_ml_cloud_number_c; TEMPO_ERR_STATE without it). */
 int tempo_run_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double dt, int itimestep,
                 double *t, double *th, const double *pii, const double *p, const double *w,
                 const double *dz, double *qv, double *qc, double *qr, double *qi, double *qs,
@@ -311,7 +314,7 @@ int tempo_tuning_c(tempo_ctx_t *ctx, int out[3]);
 /* No reference counterpart.  With on != 0, a run captures its work (counter resets and
  * the four kernels) into a CUDA graph the first time it sees a given argument set
  * (pointers, bounds, dt, flags, precision, variant) and replays the graph on later
- * runs with the same set; up to 8 graphs are kept per context.  With kernel timing on,
+ * runs with the same set; up to 16 graphs are kept per context.  With kernel timing on,
  * the graph carries the timing events. */
 int tempo_set_graphs(tempo_ctx_t *ctx, int on);
 

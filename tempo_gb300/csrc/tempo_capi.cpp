@@ -65,7 +65,11 @@ struct Mirror {
 }  // namespace
 
 namespace {
-constexpr size_t kGraphCache = 8;
+constexpr size_t kGraphCache = 16;
+// host-array runs: at most this many slabs of tile rows, each of at least about this
+// many columns (the step kernels keep the GPU busy from about 2^18 columns up)
+constexpr long kMaxSlabs = 8;
+constexpr long kSlabColumns = 262144;
 struct GraphEntry {
   std::string key;  // bytes of the step arguments + precision, variant, storage size
   cudaGraphExec_t exec;
@@ -104,6 +108,11 @@ struct tempo_ctx {
   double* d_mlnet = nullptr;  // cloud-number network (tempo_set_ml_cloud_number_c)
   bool use_graphs = false;
   std::vector<GraphEntry> graphs;  // captured steps, oldest first
+  // host-array runs: copy streams and per-slab events of the pipelined copies, and
+  // whether a run keeps the step counters of the slabs before it
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  std::vector<cudaEvent_t> slab_ev;
+  bool keep_stats = false;
 };
 
 namespace {
@@ -528,13 +537,14 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   a.nact = (unsigned int*)sp;
   a.stats = c->d_stats;
   c->last_cols = a.ncol;
-  c->launches = kStepLaunches + (order ? kOrderLaunches : 0);
+  c->launches = kStepLaunches + (order ? kOrderLaunches : 0) + ((a.flags & F_MELT) ? 1 : 0);
   if (!mixed && sizeof(S) != sizeof(double))
     return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
   const bool timed = c->kernel_timing;
   // the step's work on stream st: counters reset, then the four kernels
   auto enqueue = [&](cudaStream_t st) -> cudaError_t {
-    cudaError_t e = cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), st);
+    cudaError_t e = c->keep_stats ? cudaSuccess
+                                  : cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.nact, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
     const cudaEvent_t* ev = timed ? c->kev : nullptr;
@@ -565,6 +575,7 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   key.push_back((char)c->precision);
   key.push_back((char)c->points_variant);  // (the regime order changes a.ord)
   key.push_back((char)c->sedim_variant);
+  key.push_back((char)c->keep_stats);
   key.push_back((char)sizeof(S));
   key.push_back((char)timed);  // event-record nodes around the kernels
   cudaGraphExec_t exec = nullptr;
@@ -725,30 +736,86 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
       m.bytes = bytes;
     }
     d[i] = m.d;
-    if (i <= n_in) CUDA_TRY(cudaMemcpyAsync(d[i], h, bytes, cudaMemcpyHostToDevice, c->stream));
   }
   RunArrays<S> D{(S*)d[0],  (S*)d[1],  (const S*)d[2], (const S*)d[3], (const S*)d[4],
                  (const S*)d[5], (S*)d[6],  (S*)d[7],  (S*)d[8],  (S*)d[9],
                  (S*)d[10], (S*)d[11], (S*)d[12], (S*)d[13], (S*)d[14],
                  (S*)d[15], (S*)d[16], (S*)d[17], (S*)d[18], (const int*)d[n_in],
                  (const S*)d[19], (const S*)d[20]};
-  tempo_diags_t ddg{};
-  void** ddp[15] = {&ddg.rain_precip, &ddg.ice_liquid_equiv_precip, &ddg.snow_liquid_equiv_precip,
-                    &ddg.graupel_liquid_equiv_precip, &ddg.frozen_fraction, &ddg.frz_rain_precip,
-                    &ddg.max_hail_diameter_sfc, &ddg.max_hail_diameter_column, &ddg.refl10cm,
-                    &ddg.re_cloud, &ddg.re_ice, &ddg.re_snow, &ddg.rain_med_vol_diam,
-                    &ddg.graupel_med_vol_diam, &ddg.cloud_number_mixing_ratio};
-  for (int i = 0; i < 15; i++) *ddp[i] = d[n_in + 1 + i];
-  int rc = run_dev(c, cfg, dt, itimestep, D, b, &ddg, c->stream);
+  // Slabs of tile rows j: the step is column-local and a slab of rows is one contiguous
+  // range of every array (j is the slowest index), so slab i's copy to the device
+  // (stream copy_in), its step (the context's stream) and its copy back (copy_out) run
+  // beside the other slabs' copies.  Rows outside the tile are neither read nor written
+  // by the step and are not copied.
+  const long ti = b.ite - b.its + 1, nz = b.kte - b.kts + 1, nrows = b.jte - b.jts + 1;
+  const long row3 = (long)(b.ime - b.ims + 1) * (b.kme - b.kms + 1), row2 = b.ime - b.ims + 1;
+  const int nslab = (int)std::min<long>(std::min<long>(kMaxSlabs, nrows),
+                                        std::max<long>(1, (long)t2 / kSlabColumns));
+  CUDA_TRY(cudaSetDevice(c->device));
+  if (!c->copy_in) CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking));
+  if (!c->copy_out) CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking));
+  while (c->slab_ev.size() < (size_t)(2 * kMaxSlabs)) {
+    cudaEvent_t e;
+    CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c->slab_ev.push_back(e);
+  }
+  int rc = TEMPO_OK;
+  long launches = 0;
+  for (int sl = 0; sl < nslab && rc == TEMPO_OK; sl++) {
+    const long ja = b.jts + (sl * nrows) / nslab, jb = b.jts + ((sl + 1) * nrows) / nslab - 1;
+    const long rows = jb - ja + 1;
+    const size_t o3 = (size_t)(ja - b.jms) * row3, c3 = (size_t)rows * row3;
+    const size_t o2 = (size_t)(ja - b.jms) * row2, c2 = (size_t)rows * row2;
+    const size_t od2 = (size_t)(ja - b.jts) * ti, cd2 = (size_t)rows * ti;
+    const size_t od3 = od2 * nz, cd3 = cd2 * nz;
+    cudaEvent_t in_done = c->slab_ev[2 * sl], step_done = c->slab_ev[2 * sl + 1];
+    for (int i = 0; i < n_in; i++)
+      if (d[i])
+        CUDA_TRY(cudaMemcpyAsync((S*)d[i] + o3, (const S*)in3[i] + o3, c3 * sizeof(S),
+                                 cudaMemcpyHostToDevice, c->copy_in));
+    if (d[n_in])
+      CUDA_TRY(cudaMemcpyAsync((int*)d[n_in] + o2, H.land + o2, c2 * sizeof(int),
+                               cudaMemcpyHostToDevice, c->copy_in));
+    CUDA_TRY(cudaEventRecord(in_done, c->copy_in));
+    CUDA_TRY(cudaStreamWaitEvent(c->stream, in_done, 0));
+    // the slab as a tile: rows ja..jb, diagnostics at the slab's offset in the tile
+    Bounds bs = b;
+    bs.jts = (int)ja;
+    bs.jte = (int)jb;
+    tempo_diags_t ddg{};
+    void** ddp[15] = {&ddg.rain_precip, &ddg.ice_liquid_equiv_precip, &ddg.snow_liquid_equiv_precip,
+                      &ddg.graupel_liquid_equiv_precip, &ddg.frozen_fraction, &ddg.frz_rain_precip,
+                      &ddg.max_hail_diameter_sfc, &ddg.max_hail_diameter_column, &ddg.refl10cm,
+                      &ddg.re_cloud, &ddg.re_ice, &ddg.re_snow, &ddg.rain_med_vol_diam,
+                      &ddg.graupel_med_vol_diam, &ddg.cloud_number_mixing_ratio};
+    for (int i = 0; i < 15; i++)
+      *ddp[i] = d[n_in + 1 + i] ? (void*)((S*)d[n_in + 1 + i] + (i < 8 ? od2 : od3)) : nullptr;
+    c->keep_stats = sl > 0;  // the counters sum (early exits) and take maxima over slabs
+    rc = run_dev(c, cfg, dt, itimestep, D, bs, &ddg, c->stream);
+    c->keep_stats = false;
+    if (rc) break;
+    launches += c->launches;
+    CUDA_TRY(cudaEventRecord(step_done, c->stream));
+    CUDA_TRY(cudaStreamWaitEvent(c->copy_out, step_done, 0));
+    for (int i = 0; i < n_in; i++)
+      if (d[i] && out3[i])
+        CUDA_TRY(cudaMemcpyAsync((S*)in3[i] + o3, (const S*)d[i] + o3, c3 * sizeof(S),
+                                 cudaMemcpyDeviceToHost, c->copy_out));
+    for (int i = 0; i < 15; i++)
+      if (d[n_in + 1 + i]) {
+        const size_t off = i < 8 ? od2 : od3, cnt = i < 8 ? cd2 : cd3;
+        CUDA_TRY(cudaMemcpyAsync((S*)dg_h[i] + off, (const S*)d[n_in + 1 + i] + off, cnt * sizeof(S),
+                                 cudaMemcpyDeviceToHost, c->copy_out));
+      }
+  }
+  cudaError_t e1 = cudaStreamSynchronize(c->copy_in), e2 = cudaStreamSynchronize(c->stream),
+              e3 = cudaStreamSynchronize(c->copy_out);
   if (rc) return rc;
-  for (int i = 0; i < n_in; i++)
-    if (d[i] && out3[i])
-      CUDA_TRY(cudaMemcpyAsync((void*)in3[i], d[i], n3 * sizeof(S), cudaMemcpyDeviceToHost, c->stream));
-  for (int i = 0; i < 15; i++)
-    if (d[n_in + 1 + i])
-      CUDA_TRY(cudaMemcpyAsync(dg_h[i], d[n_in + 1 + i], (i < 8 ? t2 : t3) * sizeof(S),
-                               cudaMemcpyDeviceToHost, c->stream));
-  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+    return fail(TEMPO_ERR_CUDA, "host-array run: %s",
+                cudaGetErrorString(e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3));
+  c->last_cols = (long)t2;
+  c->launches = launches;
   return TEMPO_OK;
 }
 
@@ -843,6 +910,9 @@ int tempo_ctx_destroy(tempo_ctx_t* c) {
   for (cudaEvent_t& e : c->kev)
     if (e) cudaEventDestroy(e);
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  for (cudaEvent_t e : c->slab_ev) cudaEventDestroy(e);
+  if (c->copy_in) cudaStreamDestroy(c->copy_in);
+  if (c->copy_out) cudaStreamDestroy(c->copy_out);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return TEMPO_OK;
