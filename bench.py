@@ -45,7 +45,10 @@ def parse():
     ap.add_argument("--nz", type=int, default=65)
     ap.add_argument("--dt", type=float, default=30.0)
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=6)
+    ap.add_argument("--tuning", default=None,
+                    help="points variant, point order, sedimentation variant (e.g. 5,1,5): "
+                         "set instead of autotuning (for profiling a fixed configuration)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-multi", action="store_true")
@@ -373,7 +376,14 @@ def main():
     for _ in range(max(args.warmup - 1, 1)):
         ctx.run_device(f32, args.dt, it, diags=diag)
         it += 1
-    variant, variant_ms = ctx.autotune_device(f32, args.dt, it, diags=diag, reps=6)
+    if args.tuning:
+        pv, po, sv = (int(x) for x in args.tuning.split(","))
+        ctx.set_points_variant(pv)
+        ctx.set_points_order(po)
+        ctx.set_sedim_variant(sv)
+        variant_ms = []
+    else:
+        variant, variant_ms = ctx.autotune_device(f32, args.dt, it, diags=diag, reps=6)
     tuning = ctx.tuning()
     ctx.set_kernel_timing(True)
     ctx.set_graphs(True)

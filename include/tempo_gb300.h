@@ -123,7 +123,7 @@ int tempo_set_precision(tempo_ctx_t *ctx, int precision);
 
 /* tempo_run (src/module_mp_tempo_driver.F90:187-513) on host arrays of doubles (the
  * reference's default kind_phys).  Copies the tile to the device, runs the step,
- * copies results back and synchronises.  Large tiles (from 2^19 columns) go in up to
+ * copies results back and synchronises.  Large tiles (from 2^18 columns) go in up to
  * 8 slabs of rows j, each slab's copies on two copy streams overlapping the other
  * slabs' steps on the context's stream; only the tile's rows are copied.  Optional
  * arrays: t or (th and pii); nc, nwfa, nifa, ng, qb, land_input, qcfrac, qifrac and
@@ -232,14 +232,14 @@ int tempo_set_kernel_timing(tempo_ctx_t *ctx, int on);
 int tempo_kernel_times_c(tempo_ctx_t *ctx, float ms[5]);
 
 /* No reference counterpart.  Autotuner of the mixed form on FP32 device storage.  For
- * each of 19 candidates it copies the given state and runs `reps` consecutive steps
+ * each of 22 candidates it copies the given state and runs `reps` consecutive steps
  * (itimestep, itimestep + 1, ...) on the copy -- the caller's arrays are not modified
  * -- timing kernels with CUDA events on `stream`, and scores the candidate by its
  * median step time.  Candidates 0-15: every variant of the per-level kernel (block
  * shape, barriers, register budget) in each order of the points (candidate v: variant
  * v % 8, order v / 8, as tempo_set_points_variant and tempo_set_points_order take
- * them), timed over the regime-order and per-level kernels; candidates 16-18: the
- * sedimentation variants 0-2 (tempo_set_sedim_variant) with the best of 0-15, timed
+ * them), timed over the regime-order and per-level kernels; candidates 16-21: the
+ * sedimentation variants 0-5 (tempo_set_sedim_variant) with the best of 0-15, timed
  * over the sedimentation kernel.  The best of each group is kept for later runs (all
  * precisions).  Tune on a state like the ones the runs will see: the work of a step
  * depends on the state it starts from.  Arguments as tempo_run_dev_f32_c; times_ms
@@ -302,10 +302,16 @@ int tempo_set_points_variant(tempo_ctx_t *ctx, int variant);
  * tempo_run_dev_f32_noalloc_c always runs level-major. */
 int tempo_set_points_order(tempo_ctx_t *ctx, int order);
 
-/* No reference counterpart.  Selects the sedimentation kernel variant directly: the
- * number of levels whose loads a sweep issues together, 1 (variant 0, the default),
- * 2 (1) or 3 (2).  Every variant computes the same values. */
+/* No reference counterpart.  Selects the sedimentation kernel variant directly (0..5):
+ * variant % 3 + 1 levels whose loads a sweep issues together, and for variants 3-5 a
+ * column's species split over two threads (rain and snow; graupel, ice and cloud).
+ * Variant 0 is the default.  Every variant computes the same values. */
 int tempo_set_sedim_variant(tempo_ctx_t *ctx, int variant);
+
+/* No reference counterpart.  Number of row slabs of later host-array runs (1..8; 0,
+ * the default, takes one slab per 2^17 tile columns, at most 8, at least 1).  Never
+ * changes a result. */
+int tempo_set_host_slabs(tempo_ctx_t *ctx, int slabs);
 
 /* No reference counterpart.  The context's kernel choices: out[0] the per-level kernel
  * variant, out[1] the point order, out[2] the sedimentation variant. */

@@ -142,6 +142,7 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
     lib.tempo_set_points_order.argtypes = [_VP, i]
     lib.tempo_set_sedim_variant.argtypes = [_VP, i]
     lib.tempo_tuning_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_int)]
+    lib.tempo_set_host_slabs.argtypes = [_VP, i]
     lib.tempo_set_graphs.argtypes = [_VP, i]
     lib.tempo_tl_dev_c.argtypes = ([_VP, ctypes.POINTER(TempoCfgs), ctypes.c_double, i, i,
                                     ctypes.POINTER(TempoState), ctypes.POINTER(TempoState),
@@ -313,7 +314,7 @@ class TempoContext:
         variant of the mixed form for this workload (tempo_autotune_dev_f32_c) on
         private copies of the float32 CUDA tensors; returns (chosen per-level
         candidate, per-candidate time in ms): candidates 0-15 are variant v % 8 in
-        order v // 8, candidates 16-18 the sedimentation variants."""
+        order v // 8, candidates 16-21 the sedimentation variants."""
         import torch
         lib = load_library()
         cfg = cfgs if cfgs is not None else self.cfgs
@@ -330,12 +331,12 @@ class TempoContext:
             if a is not None:
                 setattr(d, n, a.data_ptr())
         s = stream if stream is not None else torch.cuda.current_stream(p.device)
-        times = (ctypes.c_float * 19)()
+        times = (ctypes.c_float * 22)()
         chosen = ctypes.c_int(-1)
         _check(lib.tempo_autotune_dev_f32_c(
             self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs,
             land.data_ptr() if land is not None else None, *b[6:], ctypes.byref(d),
-            ctypes.c_void_p(s.cuda_stream), int(reps), times, 19, ctypes.byref(chosen)))
+            ctypes.c_void_p(s.cuda_stream), int(reps), times, 22, ctypes.byref(chosen)))
         return chosen.value, [float(x) for x in times]
 
     # ---- derivatives ----------------------------------------------------------------
@@ -405,8 +406,13 @@ class TempoContext:
         _check(load_library().tempo_set_points_order(self._h, int(order)))
 
     def set_sedim_variant(self, v: int):
-        """Levels loaded together by a sedimentation sweep: 0 -> 1, 1 -> 2, 2 -> 3."""
+        """Sedimentation kernel variant 0..5: v % 3 + 1 levels loaded together per
+        sweep; v >= 3 splits a column's species over two threads."""
         _check(load_library().tempo_set_sedim_variant(self._h, int(v)))
+
+    def set_host_slabs(self, n: int):
+        """Row slabs of later host-array runs (0: from the tile's size)."""
+        _check(load_library().tempo_set_host_slabs(self._h, int(n)))
 
     def tuning(self) -> dict:
         """The context's kernel choices (tempo_tuning_c)."""

@@ -67,9 +67,9 @@ struct Mirror {
 namespace {
 constexpr size_t kGraphCache = 16;
 // host-array runs: at most this many slabs of tile rows, each of at least about this
-// many columns (the step kernels keep the GPU busy from about 2^18 columns up)
+// many columns (the step kernels keep the GPU busy from about 2^17 columns up)
 constexpr long kMaxSlabs = 8;
-constexpr long kSlabColumns = 262144;
+constexpr long kSlabColumns = 131072;
 struct GraphEntry {
   std::string key;  // bytes of the step arguments + precision, variant, storage size
   cudaGraphExec_t exec;
@@ -103,7 +103,7 @@ struct tempo_ctx {
   cudaEvent_t kev[kStepPhases + 1] = {};
   int points_variant = 0;  // mixed form on FP32 storage (tempo_autotune_dev_f32_c)
   int points_order = 0;    // phase A's points level-major (0) or in regime order (1)
-  int sedim_variant = 0;   // levels loaded together by a sedimentation sweep: 1, 2, 3
+  int sedim_variant = 0;   // sedimentation kernel (tempo_set_sedim_variant)
   RadarConsts radar{};     // melting-layer reflectivity (FP64)
   double* d_mlnet = nullptr;  // cloud-number network (tempo_set_ml_cloud_number_c)
   bool use_graphs = false;
@@ -113,6 +113,7 @@ struct tempo_ctx {
   cudaStream_t copy_in = nullptr, copy_out = nullptr;
   std::vector<cudaEvent_t> slab_ev;
   bool keep_stats = false;
+  int host_slabs = 0;  // slabs of a host-array run (0: from the tile's size)
 };
 
 namespace {
@@ -749,8 +750,8 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
   // by the step and are not copied.
   const long ti = b.ite - b.its + 1, nz = b.kte - b.kts + 1, nrows = b.jte - b.jts + 1;
   const long row3 = (long)(b.ime - b.ims + 1) * (b.kme - b.kms + 1), row2 = b.ime - b.ims + 1;
-  const int nslab = (int)std::min<long>(std::min<long>(kMaxSlabs, nrows),
-                                        std::max<long>(1, (long)t2 / kSlabColumns));
+  const long want = c->host_slabs > 0 ? c->host_slabs : std::max<long>(1, (long)t2 / kSlabColumns);
+  const int nslab = (int)std::min<long>(std::min<long>(kMaxSlabs, nrows), want);
   CUDA_TRY(cudaSetDevice(c->device));
   if (!c->copy_in) CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking));
   if (!c->copy_out) CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking));
@@ -1113,6 +1114,13 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, 
   c->points_order = best_v / kPointsVariants;
   c->sedim_variant = best_s;
   if (chosen) *chosen = best_v;
+  return TEMPO_OK;
+}
+
+int tempo_set_host_slabs(tempo_ctx_t* c, int slabs) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (slabs < 0 || slabs > kMaxSlabs) return fail(TEMPO_ERR_ARG, "slabs %d outside [0, %ld]", slabs, kMaxSlabs);
+  c->host_slabs = slabs;
   return TEMPO_OK;
 }
 

@@ -22,7 +22,7 @@ cudaError_t launch_step_f64(const StepArgs<double>& a, const Tables<double>& t,
                             cudaStream_t s, const cudaEvent_t* ev, int sedim_variant);
 
 // tempo_step_f32.cu (mixed precision: FP32 bulk, double-float islands); sedim_variant
-// in [0, kSedimVariants) (tempo_step.cuh: sedim_group)
+// in [0, kSedimCandidates) (tempo_step.cuh: sedim_group, sedim_split)
 cudaError_t launch_step_mixed_f32(const StepArgs<float>& a, const Tables<float>& t,
                                   const TempoConsts<float>& c32, const IslandConsts<df>& idf,
                                   cudaStream_t s, const cudaEvent_t* ev, int points_variant,
@@ -75,8 +75,8 @@ cudaError_t launch_melt_refl(const StepArgs<S>& a, const TempoConsts<double>& c,
 // autotuner's candidates (each variant in level-major and in regime order)
 constexpr int kPointsVariants = 8;
 constexpr int kPointsCandidates = 2 * kPointsVariants;
-// number of sedimentation-kernel variants (tempo_step.cuh: sedim_group)
-constexpr int kSedimCandidates = 3;
+// number of sedimentation-kernel variants (tempo_step.cuh: sedim_group, sedim_split)
+constexpr int kSedimCandidates = 6;
 // kernels launched per step (prep, points, sedim, final), and one more when phase A's
 // points run in regime order
 constexpr int kStepLaunches = 4;

@@ -34,6 +34,16 @@ cudaError_t launch_points(const StepArgs<S>& a, const Tables<Cst<R>>& T, const T
   return cudaGetLastError();
 }
 
+// the explicit sedimentation kernel, variant sv (tempo_step.cuh: sedim_group,
+// sedim_split)
+template <class R, class S, int V = 0>
+void launch_sedim(const StepArgs<S>& a, int sv, unsigned gcol, cudaStream_t s) {
+  if constexpr (V + 1 < kSedimVariants)
+    if (sv != V) return launch_sedim<R, S, V + 1>(a, sv, gcol, s);
+  tempo_sedim_kernel<R, S, sedim_group(V), sedim_split(V)>
+      <<<dim3(gcol, sedim_split(V) ? 2 : 1), kBlock, 0, s>>>(a);
+}
+
 // regime order of phase A's points into a.ord (nothing when a.ord is NULL); the grid
 // covers every column's levels, windows past the active points return at once
 template <class S>
@@ -69,12 +79,8 @@ cudaError_t launch_step(const StepArgs<S>& a, const TempoConsts<Cst<R>>& c, cons
   if (ev) record_event(ev[3], s);
   if (a.flags & F_SEMI)
     tempo_sedim_semi_kernel<R, S><<<gcol, kBlock, 0, s>>>(a, c, ci);
-  else if (sv == 1)
-    tempo_sedim_kernel<R, S, sedim_group(1)><<<gcol, kBlock, 0, s>>>(a);
-  else if (sv == 2)
-    tempo_sedim_kernel<R, S, sedim_group(2)><<<gcol, kBlock, 0, s>>>(a);
   else
-    tempo_sedim_kernel<R, S, sedim_group(0)><<<gcol, kBlock, 0, s>>>(a);
+    launch_sedim<R, S>(a, sv, gcol, s);
   if (ev) record_event(ev[4], s);
   tempo_final_kernel<R, S><<<gpts, kBlock, 0, s>>>(a, c, ci);
   if (ev) record_event(ev[5], s);

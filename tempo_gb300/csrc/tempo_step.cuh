@@ -877,15 +877,22 @@ __device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dz
 // Phase B on the column of active slot s.  SEMI: rain and graupel by the
 // semi-Lagrangian scheme (semi_sedi_flag, main:599-613, 640-671), which rechecks the
 // species and recomputes their fall speeds after every substep (needs cst and ci).
-// Variants of the sedimentation kernel (picked per context by the autotuner): the
-// number of levels whose loads a sweep issues together, 1, 2 or 3 (more loads in flight
-// per thread against more registers per thread; 4 and 8 were measured slower still).
-constexpr int kSedimVariants = 3;
-__host__ __device__ constexpr int sedim_group(int v) { return v == 0 ? 1 : v == 1 ? 2 : 3; }
+// Variants of the sedimentation kernel (picked per context by the autotuner): v % 3
+// selects the number of levels whose loads a sweep issues together, 1, 2 or 3 (more
+// loads in flight per thread against more registers per thread; 4 and 8 were measured
+// slower still); v / 3 = 1 splits a column's species over two threads (rain and snow
+// -- snow's fall speed reads rain's state after rain sedimentation -- and graupel, ice
+// and cloud), twice the threads for the same serial chains.
+constexpr int kSedimVariants = 6;
+__host__ __device__ constexpr int sedim_group(int v) { return v % 3 + 1; }
+__host__ __device__ constexpr bool sedim_split(int v) { return v >= 3; }
 
+// Phase B of active slot s; part < 0: every species, 0: rain and snow, 1: graupel, ice
+// and cloud (each part writes the precipitation sums and substep counts of its own
+// species).
 template <class R, class S, bool SEMI, int G = 1>
 __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoConsts<Cst<R>>* cst,
-                                             const IslandConsts<Isl<R>>* ci, long s) {
+                                             const IslandConsts<Isl<R>>* ci, long s, int part = -1) {
   using I = Isl<R>;
   const int nz = a.nz;
   const long NI = a.NI;
@@ -947,104 +954,122 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
     }
     if (ktop == nz) ktop = nz - 1;
   };
-  // one substep on a field whose fall speed sits in the R scratch (sedimentation,
-  // main:1516-1559): fluxes from the pre-substep state, level nz first, then ktop..1.
-  // The levels below ktop go in groups of G: a group's loads are issued
-  // together (no level's update reads another level's updated values), then the
-  // group's levels are updated in the serial order and stored.
-  auto sweep = [&](int fx, int ften, int fv, double limit, int steps, int ktop, I* precip) {
-    I* x = sd + fx * fsd;
-    I* ten = sd + ften * fsd;
-    const R* vt = sr + fv * fsd;
+  // one substep of NF fields whose fall speeds sit in the R scratch (sedimentation,
+  // main:1516-1559), each field's arithmetic exactly that of a sweep of its own:
+  // fluxes from the pre-substep state, level nz first, then ktop..1.  The fields of
+  // one species share the levels' factors, loaded once.  The levels below ktop go in
+  // groups of G: a group's loads are issued together (no level's update reads
+  // another level's updated values), then the group's levels are updated in the
+  // serial order and stored.  Field 0 feeds the precipitation sum.
+  auto sweep = [&](auto nf, const int* fx, const int* ften, const int* fv, const double* limit,
+                   int steps, int ktop, I* precip) {
+    constexpr int NF = decltype(nf)::value;
+    constexpr bool kMixed = std::is_same<I, df>::value;
+    I* x[NF];
+    I* ten[NF];
+    const R* vt[NF];
+    I lim[NF], s_up[NF], s0[NF];
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+      x[f] = sd + fx[f] * fsd;
+      ten[f] = sd + ften[f] * fsd;
+      vt[f] = sr + fv[f] * fsd;
+      lim[f] = I(limit[f]);
+    }
     const I osteps = 1.0 / I(steps);
-    const I lim = I(limit);
-    if constexpr (std::is_same<I, df>::value) {
-      // mixed form: the same fluxes and order, with the per-level factors 1/dz and
-      // 1/(dz rho) precomputed in the points kernel
-      const I* odz = sd + SD_ODZ * fsd;
-      const I* ozr = sd + SD_OZR * fsd;
-      const I cx = dti * osteps;
-      int k = nz - 1;
-      I s_top = I(vt[k * kSlotTile]) * x[k * kSlotTile];
-      ten[k * kSlotTile] = ten[k * kSlotTile] - s_top * ozr[k * kSlotTile] * osteps;
-      x[k * kSlotTile] = Max(lim, x[k * kSlotTile] - s_top * odz[k * kSlotTile] * cx);
-      I s_up = (ktop == nz - 1) ? s_top : I(vt[ktop * kSlotTile]) * x[ktop * kSlotTile];
-      I s0 = (nz == 1) ? s_top : I(vt[0]) * x[0];
-      for (k = ktop - 1; k >= 0; k -= G) {
-        R gv[G];
-        I gx[G], gt[G], go[G], gz[G];
-#pragma unroll
-        for (int u = 0; u < G; u++)
-          if (u <= k) {
-            const long o = (long)(k - u) * kSlotTile;
-            gv[u] = vt[o];
-            gx[u] = x[o];
-            gt[u] = ten[o];
-            go[u] = odz[o];
-            gz[u] = ozr[o];
-          }
-#pragma unroll
-        for (int u = 0; u < G; u++)
-          if (u <= k) {
-            const I s_k = I(gv[u]) * gx[u];
-            const I dflux = s_up - s_k;
-            gt[u] = gt[u] + dflux * gz[u] * osteps;
-            gx[u] = Max(lim, gx[u] + dflux * go[u] * cx);
-            if (k - u == 0) s0 = s_k;
-            s_up = s_k;
-          }
-#pragma unroll
-        for (int u = 0; u < G; u++)
-          if (u <= k) {
-            const long o = (long)(k - u) * kSlotTile;
-            ten[o] = gt[u];
-            x[o] = gx[u];
-          }
+    // mixed form: the per-level factors 1/dz and 1/(dz rho) precomputed in the points
+    // kernel; FP64: 1/dz and 1/rho formed here, as the reference does
+    const I* odz = sd + SD_ODZ * fsd;
+    const I* ozr = sd + SD_OZR * fsd;
+    const I cx = dti * osteps;
+    {
+      const int k = nz - 1;
+      const long o = (long)k * kSlotTile;
+      I fo, fr;
+      if constexpr (kMixed) {
+        fo = odz[o];
+        fr = ozr[o];
+      } else {
+        fo = 1.0 / ldi<I>(dzp + k * NI);
+        fr = 1.0 / rho[o];
       }
-      if (precip && x[0] > low_limit_mass_for_precip) *precip = *precip + s0 * dti * osteps;
-      return;
+#pragma unroll
+      for (int f = 0; f < NF; f++) {
+        const I s_top = I(vt[f][o]) * x[f][o];
+        if constexpr (kMixed) {
+          ten[f][o] = ten[f][o] - s_top * fr * osteps;
+          x[f][o] = Max(lim[f], x[f][o] - s_top * fo * cx);
+        } else {
+          ten[f][o] = ten[f][o] - s_top * fo * osteps * fr;
+          x[f][o] = Max(lim[f], x[f][o] - s_top * fo * dti * osteps);
+        }
+        s_up[f] = (ktop == nz - 1) ? s_top : I(vt[f][ktop * kSlotTile]) * x[f][ktop * kSlotTile];
+        s0[f] = (nz == 1) ? s_top : I(vt[f][0]) * x[f][0];
+      }
     }
-    int k = nz - 1;
-    I s_top = I(vt[k * kSlotTile]) * x[k * kSlotTile];
-    I odz = 1.0 / ldi<I>(dzp + k * NI), orho = 1.0 / rho[k * kSlotTile];
-    ten[k * kSlotTile] = ten[k * kSlotTile] - s_top * odz * osteps * orho;
-    x[k * kSlotTile] = Max(lim, x[k * kSlotTile] - s_top * odz * dti * osteps);
-    I s_up = (ktop == nz - 1) ? s_top : I(vt[ktop * kSlotTile]) * x[ktop * kSlotTile];
-    I s0 = (nz == 1) ? s_top : I(vt[0]) * x[0];
-    for (k = ktop - 1; k >= 0; k -= G) {
-      R gv[G];
-      I gx[G], gt[G], gd[G], gr[G];
+    for (int k = ktop - 1; k >= 0; k -= G) {
+      R gv[NF][G];
+      I gx[NF][G], gt[NF][G], ga[G], gb[G];
 #pragma unroll
       for (int u = 0; u < G; u++)
         if (u <= k) {
           const long o = (long)(k - u) * kSlotTile;
-          gv[u] = vt[o];
-          gx[u] = x[o];
-          gt[u] = ten[o];
-          gd[u] = ldi<I>(dzp + (long)(k - u) * NI);
-          gr[u] = rho[o];
+          if constexpr (kMixed) {
+            ga[u] = odz[o];
+            gb[u] = ozr[o];
+          } else {
+            ga[u] = ldi<I>(dzp + (long)(k - u) * NI);
+            gb[u] = rho[o];
+          }
+#pragma unroll
+          for (int f = 0; f < NF; f++) {
+            gv[f][u] = vt[f][o];
+            gx[f][u] = x[f][o];
+            gt[f][u] = ten[f][o];
+          }
         }
 #pragma unroll
       for (int u = 0; u < G; u++)
         if (u <= k) {
-          const I s_k = I(gv[u]) * gx[u];
-          odz = 1.0 / gd[u];
-          orho = 1.0 / gr[u];
-          gt[u] = gt[u] + (s_up - s_k) * odz * osteps * orho;
-          gx[u] = Max(lim, gx[u] + (s_up - s_k) * odz * dti * osteps);
-          if (k - u == 0) s0 = s_k;
-          s_up = s_k;
+          I fo, fr;
+          if constexpr (kMixed) {
+            fo = ga[u];
+            fr = gb[u];
+          } else {
+            fo = 1.0 / ga[u];
+            fr = 1.0 / gb[u];
+          }
+#pragma unroll
+          for (int f = 0; f < NF; f++) {
+            const I s_k = I(gv[f][u]) * gx[f][u];
+            if constexpr (kMixed) {
+              const I dflux = s_up[f] - s_k;
+              gt[f][u] = gt[f][u] + dflux * fr * osteps;
+              gx[f][u] = Max(lim[f], gx[f][u] + dflux * fo * cx);
+            } else {
+              gt[f][u] = gt[f][u] + (s_up[f] - s_k) * fo * osteps * fr;
+              gx[f][u] = Max(lim[f], gx[f][u] + (s_up[f] - s_k) * fo * dti * osteps);
+            }
+            if (k - u == 0) s0[f] = s_k;
+            s_up[f] = s_k;
+          }
         }
 #pragma unroll
       for (int u = 0; u < G; u++)
         if (u <= k) {
           const long o = (long)(k - u) * kSlotTile;
-          ten[o] = gt[u];
-          x[o] = gx[u];
+#pragma unroll
+          for (int f = 0; f < NF; f++) {
+            ten[f][o] = gt[f][u];
+            x[f][o] = gx[f][u];
+          }
         }
     }
-    if (precip && x[0] > low_limit_mass_for_precip) *precip = *precip + s0 * dti * osteps;
+    if (precip && x[0][0] > low_limit_mass_for_precip) *precip = *precip + s0[0] * dti * osteps;
   };
+  using One = std::integral_constant<int, 1>;
+  using Two = std::integral_constant<int, 2>;
+  using Three = std::integral_constant<int, 3>;
   int steps, ktop;
   unsigned sub[5] = {0, 0, 0, 0, 0};
   // semi-Lagrangian path: one sweep on this column's work rows, and the level's state
@@ -1067,7 +1092,8 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
     thermo_tail(L);
   };
   [[maybe_unused]] const R odt_r = step_odt<R>(a);
-  if (any_qr) {
+  const bool p0 = part != 1, p1 = part != 0;
+  if (any_qr && p0) {
     fill(SR_VTR, SR_VTNR, true, false, steps, ktop);
     if constexpr (SEMI) {
       steps = max((int)(steps / 10.0) + 1, 1);  // semi_sedi_factor (main:595, 599)
@@ -1102,12 +1128,13 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
     } else {
       sub[0] = steps;
       for (int n = 0; n < steps; n++) {
-        sweep(SD_XRR, SD_TQR, SR_VTR, r1, steps, ktop, &prec_r);
-        sweep(SD_XNR, SD_TNR, SR_VTNR, r2, steps, ktop, nullptr);
+        const int fx[2] = {SD_XRR, SD_XNR}, ft[2] = {SD_TQR, SD_TNR}, fv[2] = {SR_VTR, SR_VTNR};
+        const double lim[2] = {r1, r2};
+        sweep(Two{}, fx, ft, fv, lim, steps, ktop, &prec_r);
       }
     }
   }
-  if (any_qg) {
+  if (any_qg && p1) {
     fill(SR_VTG, SR_VTNG, false, false, steps, ktop);
     if constexpr (SEMI) {
       const bool hail = a.flags & F_HAIL;
@@ -1147,24 +1174,28 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
     } else {
       sub[1] = steps;
       for (int n = 0; n < steps; n++) {
-        sweep(SD_XRG, SD_TQG, SR_VTG, r1, steps, ktop, &prec_g);
-        sweep(SD_XNG, SD_TNG, SR_VTNG, r2, steps, ktop, nullptr);
-        sweep(SD_XRB, SD_TQB, SR_VTG, meters3_to_liters * r1 / rho_gd(nrhg), steps, ktop, nullptr);
+        const int fx[3] = {SD_XRG, SD_XNG, SD_XRB}, ft[3] = {SD_TQG, SD_TNG, SD_TQB},
+                  fv[3] = {SR_VTG, SR_VTNG, SR_VTG};
+        const double lim[3] = {r1, r2, meters3_to_liters * r1 / rho_gd(nrhg)};
+        sweep(Three{}, fx, ft, fv, lim, steps, ktop, &prec_g);
       }
     }
   }
-  if (any_qs) {
+  if (any_qs && p0) {
     fill(SR_VTSA, SR_VTSA, false, true, steps, ktop);
     sub[2] = steps;
-    for (int n = 0; n < steps; n++) sweep(SD_XRS, SD_TQS, SR_VTSA, r1, steps, ktop, &prec_s);
+    const int fx[1] = {SD_XRS}, ft[1] = {SD_TQS}, fv[1] = {SR_VTSA};
+    const double lim[1] = {r1};
+    for (int n = 0; n < steps; n++) sweep(One{}, fx, ft, fv, lim, steps, ktop, &prec_s);
   }
-  if (any_qi) {
+  if (any_qi && p1) {
     fill(SR_VTI, SR_VTNI, false, false, steps, ktop);
     sub[3] = steps;
-    sweep(SD_XRI, SD_TQI, SR_VTI, r1, steps, ktop, &prec_i);
-    sweep(SD_XNI, SD_TNI, SR_VTNI, r2, steps, ktop, nullptr);
+    const int fx[2] = {SD_XRI, SD_XNI}, ft[2] = {SD_TQI, SD_TNI}, fv[2] = {SR_VTI, SR_VTNI};
+    const double lim[2] = {r1, r2};
+    sweep(Two{}, fx, ft, fv, lim, steps, ktop, &prec_i);
   }
-  if (any_qc) {  // cloud_fallspeed (main:1945-1977): settles only below 500 m
+  if (any_qc && p1) {  // cloud_fallspeed (main:1945-1977): settles only below 500 m
     int kt = 1;
     I hgtc = I(0.0);
     for (int k = 1; k <= nz - 1; k++) {
@@ -1177,24 +1208,31 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
       sr[SR_VTNC * fsd + (long)k * kSlotTile] = R(0);
     }
     sub[4] = 1;
-    sweep(SD_XRC, SD_TQC, SR_VTC, r1, 1, kt, &prec_c);
-    sweep(SD_XNC, SD_TNC, SR_VTNC, r2, 1, kt, nullptr);
+    const int fx[2] = {SD_XRC, SD_XNC}, ft[2] = {SD_TQC, SD_TNC}, fv[2] = {SR_VTC, SR_VTNC};
+    const double lim[2] = {r1, r2};
+    sweep(Two{}, fx, ft, fv, lim, 1, kt, &prec_c);
   }
   for (int q = 0; q < 5; q++)
     if (sub[q]) atomicMax(a.stats + 1 + q, (unsigned long long)sub[q]);
   I* sc = reinterpret_cast<I*>(a.sc) + s;
-  sc[SC_PR * cs] = prec_r;
-  sc[SC_PG * cs] = prec_g;
-  sc[SC_PS * cs] = prec_s;
-  sc[SC_PI * cs] = prec_i;
-  sc[SC_PC * cs] = prec_c;
+  if (p0) {
+    sc[SC_PR * cs] = prec_r;
+    sc[SC_PS * cs] = prec_s;
+  }
+  if (p1) {
+    sc[SC_PG * cs] = prec_g;
+    sc[SC_PI * cs] = prec_i;
+    sc[SC_PC * cs] = prec_c;
+  }
 }
 
-template <class R, class S, int G = 1>
+// phase B, one thread per active column (SPLIT: per active column and part, the part
+// in blockIdx.y)
+template <class R, class S, int G = 1, bool SPLIT = false>
 __global__ void __launch_bounds__(128) tempo_sedim_kernel(const __grid_constant__ StepArgs<S> a) {
   const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= (long)*a.nact) return;
-  sedim_column<R, S, false, G>(a, nullptr, nullptr, s);
+  sedim_column<R, S, false, G>(a, nullptr, nullptr, s, SPLIT ? (int)blockIdx.y : -1);
 }
 // phase B with semi-Lagrangian rain and graupel (F_SEMI), one thread per active column
 template <class R, class S>
