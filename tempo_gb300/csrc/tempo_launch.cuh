@@ -1,6 +1,8 @@
 // tempo_launch.cuh -- enqueues the four kernels of one column step on a stream.
 #pragma once
 
+#include <algorithm>
+
 #include "tempo_internal.h"
 #include "tempo_step.cuh"
 
@@ -30,7 +32,18 @@ template <class R, class S, int V>
 cudaError_t launch_points(const StepArgs<S>& a, const Tables<Cst<R>>& T, const TempoConsts<Cst<R>>& c,
                           const IslandConsts<Isl<R>>& ci, cudaStream_t s) {
   constexpr int block = points_block(V);
-  tempo_points_kernel<R, S, V><<<points_grid(a.ncol, a.nz, block), block, 0, s>>>(a, T, c, ci);
+  unsigned grid = points_grid(a.ncol, a.nz, block);
+  if constexpr (points_persistent(V)) {
+    // one resident block per SM (or fewer blocks than that when the points are few)
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tempo_points_kernel<R, S, V>, block, 0);
+    if (e != cudaSuccess) return e;
+    grid = std::min<unsigned>(grid, (unsigned)(std::max(per_sm, 1) * sms));
+  }
+  tempo_points_kernel<R, S, V><<<grid, block, 0, s>>>(a, T, c, ci);
   return cudaGetLastError();
 }
 

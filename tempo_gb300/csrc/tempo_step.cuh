@@ -513,12 +513,14 @@ __device__ __forceinline__ void points_stage(int stage, Lev<R>& L, Tend<R>& td, 
 // stage 0 between block barriers, so that an SM fetches each part of the kernel's code
 // for all of its warps at once (a thread's path through phase A is a long run of code
 // executed once, longer than the instruction cache); bits 1-2 select the block (128,
-// 256, 512 or 384 threads) and the resident blocks per SM asked (4, 2, 1, 1: 128, 128,
-// 128 and 170 registers per thread).
+// 256, 512 or 512 threads) and the resident blocks per SM asked (4, 2, 1, 1: 128
+// registers per thread).  Variant 7 is persistent: one block per SM takes chunks of
+// 512 points from a device work queue (a counter after the active-slot count) until
+// the points run out.
 __host__ __device__ constexpr int points_block(int v) {
-  return (v & 1) ? ((v >> 1) & 3) == 0 ? 128 : ((v >> 1) & 3) == 1 ? 256 : ((v >> 1) & 3) == 2 ? 512 : 384
-                 : 128;
+  return (v & 1) ? ((v >> 1) & 3) == 0 ? 128 : ((v >> 1) & 3) == 1 ? 256 : 512 : 128;
 }
+__host__ __device__ constexpr bool points_persistent(int v) { return v == 7; }
 __host__ __device__ constexpr int points_min_blocks(int v) {
   return (v & 1) ? ((v >> 1) & 3) == 0 ? 4 : ((v >> 1) & 3) == 1 ? 2 : 1
                  : ((v >> 1) & 3) == 0 ? 1 : ((v >> 1) & 3) + 2;
@@ -727,18 +729,38 @@ __global__ void __launch_bounds__(points_block(V), points_min_blocks(V)) tempo_p
                                                             const __grid_constant__ TempoConsts<Cst<R>> cst,
                                                             const __grid_constant__ IslandConsts<Isl<R>> ci) {
   const long nact = (long)*a.nact, npts = nact * a.nz;
-  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  // lockstep variants: a block whose threads all have points takes the barriers; the
-  // last, partial block runs without them (its threads past the points return)
-  const bool go = (V & 1) && (long)(blockIdx.x + 1) * blockDim.x <= npts;
-  if (q >= npts) return;  // (never in a block with go)
-  long p = a.ord ? (long)a.ord[q] : q;  // level-major index of the point
-  if (p >= npts) {  // never for an order built by tempo_regime_order_kernel
-    if (!go) return;
-    p = npts - 1;
+  if constexpr (points_persistent(V)) {
+    // work queue: a.nact[1] (zero before the step) counts the points handed out
+    __shared__ unsigned chunk;
+    for (;;) {
+      if (threadIdx.x == 0) chunk = atomicAdd(a.nact + 1, (unsigned)blockDim.x);
+      __syncthreads();
+      const long q0 = (long)chunk;
+      __syncthreads();
+      if (q0 >= npts) return;
+      const bool go = q0 + (long)blockDim.x <= npts;  // a full chunk takes the barriers
+      const long q = q0 + threadIdx.x;
+      if (q < npts) {
+        long p = a.ord ? (long)a.ord[q] : q;
+        if (p >= npts) p = npts - 1;  // never for an order built by tempo_regime_order_kernel
+        const int k = (int)(p / nact);
+        points_point<R, S, V>(a, T, cst, ci, k, p - (long)k * nact, FwdIO<S>{a}, go);
+      }
+    }
+  } else {
+    const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    // lockstep variants: a block whose threads all have points takes the barriers; the
+    // last, partial block runs without them (its threads past the points return)
+    const bool go = (V & 1) && (long)(blockIdx.x + 1) * blockDim.x <= npts;
+    if (q >= npts) return;  // (never in a block with go)
+    long p = a.ord ? (long)a.ord[q] : q;  // level-major index of the point
+    if (p >= npts) {  // never for an order built by tempo_regime_order_kernel
+      if (!go) return;
+      p = npts - 1;
+    }
+    const int k = (int)(p / nact);
+    points_point<R, S, V>(a, T, cst, ci, k, p - (long)k * nact, FwdIO<S>{a}, go);
   }
-  const int k = (int)(p / nact);
-  points_point<R, S, V>(a, T, cst, ci, k, p - (long)k * nact, FwdIO<S>{a}, go);
 }
 
 // ---------------------------------------------------------------------------------

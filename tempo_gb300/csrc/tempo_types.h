@@ -102,7 +102,8 @@ struct StepArgs {
   void* hgt;          // Cst<R> plane: level heights for the aerosol initial profiles
                       // (written only when nwfa or nifa is absent)
   int* act;           // [ncol_pad] column of each active slot
-  unsigned int* nact; // active-slot counter (zero before prep)
+  unsigned int* nact; // [0] active-slot counter, [1] work-queue counter of the
+                      // persistent points kernel (both zero before prep)
   uint8_t* pmask;     // plane: species present at the point after phase A
   uint8_t* cmask;     // [ncol_pad]
   unsigned long long* stats;  // [0] early exits, [1..5] max substeps
