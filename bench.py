@@ -498,7 +498,7 @@ def main():
                 "d2h_bytes_per_step": d2h, "path": "tempo_run_f32_c (host arrays)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic_from_profiles(),
-                     "kernel": "column step = tempo_{prep,regime_count,regime_scatter,points,sedim,final}_kernel",
+                     "kernel": "column step = tempo_{prep,regime_order,points,sedim,final}_kernel",
                      "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src,
                      "kernel_ms": kms,
                      "kernel_share": {k: v / step_kernel_ms for k, v in kms.items()}},

@@ -94,6 +94,12 @@ struct tempo_ctx {
         *f_qcfz = nullptr;
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
+  // second scratch and compute stream: host-array runs alternate slabs between the two
+  // so that one slab's kernels overlap the next one's
+  void* scratch2 = nullptr;
+  size_t scratch2_bytes = 0;
+  int scratch_slot = 0;
+  cudaStream_t stream2 = nullptr;
   unsigned long long* d_stats = nullptr;
   long last_cols = 0;
   long launches = 0;
@@ -338,15 +344,18 @@ double resolve_nc_value(const tempo_cfgs_t* cfg) {
   return v;
 }
 
+// the scratch of the context's current slot (c->scratch_slot), grown to `bytes`
 int ensure_scratch(tempo_ctx* c, size_t bytes) {
-  if (bytes <= c->scratch_bytes) return TEMPO_OK;
-  cudaFree(c->scratch);
-  c->scratch = nullptr;
-  c->scratch_bytes = 0;
-  cudaError_t e = cudaMalloc(&c->scratch, bytes);
+  void*& scratch = c->scratch_slot ? c->scratch2 : c->scratch;
+  size_t& have = c->scratch_slot ? c->scratch2_bytes : c->scratch_bytes;
+  if (bytes <= have) return TEMPO_OK;
+  cudaFree(scratch);
+  scratch = nullptr;
+  have = 0;
+  cudaError_t e = cudaMalloc(&scratch, bytes);
   if (e != cudaSuccess)
     return fail(TEMPO_ERR_NOMEM, "scratch of %zu bytes: %s", bytes, cudaGetErrorString(e));
-  c->scratch_bytes = bytes;
+  have = bytes;
   return TEMPO_OK;
 }
 
@@ -512,7 +521,7 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes +
                        sl_bytes + ml_bytes + nc_bytes + od_bytes + 256;
   if (int rc = ensure_scratch(c, total)) return rc;
-  char* sp = (char*)c->scratch;
+  char* sp = (char*)(c->scratch_slot ? c->scratch2 : c->scratch);
   a.sd = sp;
   sp += sd_bytes;
   a.sr = sp;
@@ -745,9 +754,11 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
                  (const S*)d[19], (const S*)d[20]};
   // Slabs of tile rows j: the step is column-local and a slab of rows is one contiguous
   // range of every array (j is the slowest index), so slab i's copy to the device
-  // (stream copy_in), its step (the context's stream) and its copy back (copy_out) run
-  // beside the other slabs' copies.  Rows outside the tile are neither read nor written
-  // by the step and are not copied.
+  // (stream copy_in), its step and its copy back (copy_out) run beside the other slabs'
+  // copies.  With two or more slabs (and no kernel timing) the steps alternate between
+  // two compute streams, each with its own scratch, so that one slab's kernels overlap
+  // the next one's.  Rows outside the tile are neither read nor written by the step
+  // and are not copied.
   const long ti = b.ite - b.its + 1, nz = b.kte - b.kts + 1, nrows = b.jte - b.jts + 1;
   const long row3 = (long)(b.ime - b.ims + 1) * (b.kme - b.kms + 1), row2 = b.ime - b.ims + 1;
   const long want = c->host_slabs > 0 ? c->host_slabs : std::max<long>(1, (long)t2 / kSlabColumns);
@@ -755,6 +766,10 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
   CUDA_TRY(cudaSetDevice(c->device));
   if (!c->copy_in) CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking));
   if (!c->copy_out) CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking));
+  const bool two = nslab > 1 && !c->kernel_timing;
+  if (two && !c->stream2) CUDA_TRY(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+  // the step counters start from zero before any slab (each slab then adds to them)
+  CUDA_TRY(cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), c->copy_in));
   while (c->slab_ev.size() < (size_t)(2 * kMaxSlabs)) {
     cudaEvent_t e;
     CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -777,8 +792,9 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
     if (d[n_in])
       CUDA_TRY(cudaMemcpyAsync((int*)d[n_in] + o2, H.land + o2, c2 * sizeof(int),
                                cudaMemcpyHostToDevice, c->copy_in));
+    cudaStream_t cs = (two && (sl & 1)) ? c->stream2 : c->stream;
     CUDA_TRY(cudaEventRecord(in_done, c->copy_in));
-    CUDA_TRY(cudaStreamWaitEvent(c->stream, in_done, 0));
+    CUDA_TRY(cudaStreamWaitEvent(cs, in_done, 0));
     // the slab as a tile: rows ja..jb, diagnostics at the slab's offset in the tile
     Bounds bs = b;
     bs.jts = (int)ja;
@@ -791,12 +807,14 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
                       &ddg.graupel_med_vol_diam, &ddg.cloud_number_mixing_ratio};
     for (int i = 0; i < 15; i++)
       *ddp[i] = d[n_in + 1 + i] ? (void*)((S*)d[n_in + 1 + i] + (i < 8 ? od2 : od3)) : nullptr;
-    c->keep_stats = sl > 0;  // the counters sum (early exits) and take maxima over slabs
-    rc = run_dev(c, cfg, dt, itimestep, D, bs, &ddg, c->stream);
+    c->keep_stats = true;  // the counters sum (early exits) and take maxima over slabs
+    c->scratch_slot = (two && (sl & 1)) ? 1 : 0;
+    rc = run_dev(c, cfg, dt, itimestep, D, bs, &ddg, cs);
     c->keep_stats = false;
+    c->scratch_slot = 0;
     if (rc) break;
     launches += c->launches;
-    CUDA_TRY(cudaEventRecord(step_done, c->stream));
+    CUDA_TRY(cudaEventRecord(step_done, cs));
     CUDA_TRY(cudaStreamWaitEvent(c->copy_out, step_done, 0));
     for (int i = 0; i < n_in; i++)
       if (d[i] && out3[i])
@@ -811,6 +829,10 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
   }
   cudaError_t e1 = cudaStreamSynchronize(c->copy_in), e2 = cudaStreamSynchronize(c->stream),
               e3 = cudaStreamSynchronize(c->copy_out);
+  if (c->stream2) {
+    const cudaError_t e4 = cudaStreamSynchronize(c->stream2);
+    if (e2 == cudaSuccess) e2 = e4;
+  }
   if (rc) return rc;
   if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
     return fail(TEMPO_ERR_CUDA, "host-array run: %s",
@@ -903,6 +925,7 @@ int tempo_ctx_destroy(tempo_ctx_t* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_tables(c);
   cudaFree(c->scratch);
+  cudaFree(c->scratch2);
   cudaFree(c->d_stats);
   cudaFree(c->d_mlnet);
   for (auto& m : c->mirrors) cudaFree(m.d);
@@ -914,6 +937,7 @@ int tempo_ctx_destroy(tempo_ctx_t* c) {
   for (cudaEvent_t e : c->slab_ev) cudaEventDestroy(e);
   if (c->copy_in) cudaStreamDestroy(c->copy_in);
   if (c->copy_out) cudaStreamDestroy(c->copy_out);
+  if (c->stream2) cudaStreamSynchronize(c->stream2), cudaStreamDestroy(c->stream2);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return TEMPO_OK;
