@@ -120,11 +120,16 @@ def peaks():
         return {}
 
 
-def traffic_from_profiles():
+def traffic_from_profiles(ncol: int):
+    """DRAM bytes of one step at ncol columns: the ncu figure of the 65 536-column step
+    in profiles/step_dram_traffic_65k.md, scaled by columns (every term of the traffic
+    grows with the number of columns)."""
+    import re
     try:
-        d = json.loads((REPO / "profiles" / "roofline_traffic.json").read_text())
-        return d.get("dram_bytes_per_launch_full_size")
-    except Exception:
+        txt = (REPO / "profiles" / "step_dram_traffic_65k.md").read_text()
+        m = re.search(r"dram_bytes_per_step_(\d+)_columns = (\d+)", txt)
+        return float(m.group(2)) * ncol / float(m.group(1)) if m else None
+    except OSError:
         return None
 
 
@@ -497,7 +502,8 @@ def main():
         "e2e": {"value": e2e_value, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "path": "tempo_run_f32_c (host arrays)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic_from_profiles(),
+                     "frac": achieved / hbm, "traffic": traffic_from_profiles(ncol),
+                     "traffic_source": "ncu dram bytes of one 65 536-column step scaled by columns",
                      "kernel": "column step = tempo_{prep,regime_order,points,sedim,final}_kernel",
                      "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src,
                      "kernel_ms": kms,
