@@ -98,12 +98,14 @@ __device__ __forceinline__ bool input_present(const StepArgs<T>& a, int i) {
 // phase A adjoint: one thread per (level, active slot), in the trajectory's point
 // order; primal arrays = the state before the step
 // ---------------------------------------------------------------------------------
-template <class T>
+// N directions: IN_N, or IN_NG without hail-aware graupel (ng and qb are then no
+// inputs, and the directions IN_NG and IN_QB are the last two)
+template <class T, int N = IN_N>
 __global__ void __launch_bounds__(128) tempo_points_adjoint_kernel(
     const __grid_constant__ StepArgs<T> a, const __grid_constant__ Tables<T> TT,
-    const __grid_constant__ TempoConsts<T> cst, const __grid_constant__ IslandConsts<Dual<T, IN_N>> ci,
+    const __grid_constant__ TempoConsts<T> cst, const __grid_constant__ IslandConsts<Dual<T, N>> ci,
     const __grid_constant__ AdjArgs<T> j) {
-  using R = Dual<T, IN_N>;
+  using R = Dual<T, N>;
   const long nact = (long)*a.nact;
   const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nact * a.nz) return;
@@ -111,15 +113,15 @@ __global__ void __launch_bounds__(128) tempo_points_adjoint_kernel(
   if (p >= nact * a.nz) return;
   const int k = (int)(p / nact);
   const long s = p - (long)k * nact;
-  T acc[IN_N];
+  T acc[N];
 #pragma unroll
-  for (int i = 0; i < IN_N; i++) acc[i] = T(0);
-  const AdjIO<T, IN_N> io{a, j, acc};
+  for (int i = 0; i < N; i++) acc[i] = T(0);
+  const AdjIO<T, N> io{a, j, acc};
   points_point<R, T, 0>(a, TT, cst, ci, k, s, io);
   const ColGeom g = col_geom(a, a.act[s]);
   const long e = g.base + (long)k * a.NI;
   // phase A overwrites every input but the temperature (the final qv included)
-  for (int i = 0; i < IN_N; i++) {
+  for (int i = 0; i < N; i++) {
     if (!input_present(a, i)) continue;
     T* slot = lam_slot(a, j, arr_of_in(i), e);
     if (!slot) continue;

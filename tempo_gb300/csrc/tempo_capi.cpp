@@ -1470,7 +1470,13 @@ int adjoint_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep,
   CUDA_TRY(DerivOps<T>::adj_sedim(aC, j, work, W, s));
   IslandConsts<Dual<T, IN_N>> ciA;
   make_island_consts(c->c64, &ciA);
-  CUDA_TRY(DerivOps<T>::adj_points(ap, TT, cst, ciA, j, s));
+  if (ap.flags & F_HAIL) {
+    CUDA_TRY(DerivOps<T>::adj_points(ap, TT, cst, ciA, j, s));
+  } else {  // ng and qb are no inputs: two directions fewer
+    IslandConsts<Dual<T, IN_NG>> ciA10;
+    make_island_consts(c->c64, &ciA10);
+    CUDA_TRY(DerivOps<T>::adj_points_nohail(ap, TT, cst, ciA10, j, s));
+  }
   CUDA_TRY(DerivOps<T>::colflag(colflag, st.a.act, st.a.nact, ap.ncol, s));
   CUDA_TRY(DerivOps<T>::adj_early(ap, cst, ciA, j, s));
   CUDA_TRY(cudaStreamSynchronize(s));

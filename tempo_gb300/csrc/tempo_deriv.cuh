@@ -75,10 +75,10 @@ cudaError_t adjoint_sedim(const StepArgs<T>& a, const AdjArgs<T>& j, T* work, co
   tempo_sedim_adjoint_kernel<T><<<(unsigned)((a.ncol + kBlock - 1) / kBlock), kBlock, 0, s>>>(a, j, work, W);
   return cudaGetLastError();
 }
-template <class T>
+template <class T, int N>
 cudaError_t adjoint_points(const StepArgs<T>& a, const Tables<T>& t, const TempoConsts<T>& c,
-                           const IslandConsts<Dual<T, IN_N>>& ci, const AdjArgs<T>& j, cudaStream_t s) {
-  tempo_points_adjoint_kernel<T><<<points_grid(a.ncol, a.nz), kBlock, 0, s>>>(a, t, c, ci, j);
+                           const IslandConsts<Dual<T, N>>& ci, const AdjArgs<T>& j, cudaStream_t s) {
+  tempo_points_adjoint_kernel<T, N><<<points_grid(a.ncol, a.nz), kBlock, 0, s>>>(a, t, c, ci, j);
   return cudaGetLastError();
 }
 template <class T>

@@ -35,7 +35,13 @@ template <> cudaError_t DerivOps<T_>::adj_sedim(const StepArgs<T_>& a, const Adj
 template <> cudaError_t DerivOps<T_>::adj_points(const StepArgs<T_>& a, const Tables<T_>& t,
                                                  const TempoConsts<T_>& c, const IslandConsts<Dual<T_, IN_N>>& ci,
                                                  const AdjArgs<T_>& j, cudaStream_t s) {
-  return adjoint_points<T_>(a, t, c, ci, j, s);
+  return adjoint_points<T_, IN_N>(a, t, c, ci, j, s);
+}
+template <> cudaError_t DerivOps<T_>::adj_points_nohail(const StepArgs<T_>& a, const Tables<T_>& t,
+                                                        const TempoConsts<T_>& c,
+                                                        const IslandConsts<Dual<T_, IN_NG>>& ci,
+                                                        const AdjArgs<T_>& j, cudaStream_t s) {
+  return adjoint_points<T_, IN_NG>(a, t, c, ci, j, s);
 }
 template <> cudaError_t DerivOps<T_>::adj_early(const StepArgs<T_>& a, const TempoConsts<T_>& c,
                                                 const IslandConsts<Dual<T_, IN_N>>& ci, const AdjArgs<T_>& j,

@@ -57,6 +57,10 @@ struct DerivOps {
                                cudaStream_t s);
   static cudaError_t adj_points(const StepArgs<T>& a, const Tables<T>& t, const TempoConsts<T>& c,
                                 const IslandConsts<Dual<T, IN_N>>& ci, const AdjArgs<T>& j, cudaStream_t s);
+  // the same without hail-aware graupel: IN_NG directions (ng and qb are no inputs)
+  static cudaError_t adj_points_nohail(const StepArgs<T>& a, const Tables<T>& t, const TempoConsts<T>& c,
+                                       const IslandConsts<Dual<T, IN_NG>>& ci, const AdjArgs<T>& j,
+                                       cudaStream_t s);
   static cudaError_t adj_early(const StepArgs<T>& a, const TempoConsts<T>& c,
                                const IslandConsts<Dual<T, IN_N>>& ci, const AdjArgs<T>& j, cudaStream_t s);
 };
