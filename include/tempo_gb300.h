@@ -309,8 +309,9 @@ int tempo_set_points_order(tempo_ctx_t *ctx, int order);
 int tempo_set_sedim_variant(tempo_ctx_t *ctx, int variant);
 
 /* No reference counterpart.  Number of row slabs of later host-array runs (1..8; 0,
- * the default, takes one slab per 2^17 tile columns, at most 8, at least 1).  Never
- * changes a result. */
+ * the default, takes one slab per 2^17 tile columns, at most 8, at least 1; from four
+ * slabs on, the first and last hold a quarter and the second and second-to-last half
+ * the rows of the others).  Never changes a result. */
 int tempo_set_host_slabs(tempo_ctx_t *ctx, int slabs);
 
 /* No reference counterpart.  The context's kernel choices: out[0] the per-level kernel

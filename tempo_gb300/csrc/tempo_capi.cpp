@@ -518,8 +518,8 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   // regime order: a point index per point
   const bool order = c->points_order != 0;
   const size_t od_bytes = order ? al(nzs * npad * sizeof(unsigned)) : 0;
-  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes +
-                       sl_bytes + ml_bytes + nc_bytes + od_bytes + 256;
+  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + 2 * cm_bytes +
+                       hg_bytes + sl_bytes + ml_bytes + nc_bytes + od_bytes + 256;
   if (int rc = ensure_scratch(c, total)) return rc;
   char* sp = (char*)(c->scratch_slot ? c->scratch2 : c->scratch);
   a.sd = sp;
@@ -533,6 +533,8 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   a.pmask = (uint8_t*)sp;
   sp += pm_bytes;
   a.cmask = (uint8_t*)sp;
+  sp += cm_bytes;
+  a.colcls = (uint8_t*)sp;
   sp += cm_bytes;
   a.hgt = sp;
   sp += hg_bytes;
@@ -555,7 +557,7 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   auto enqueue = [&](cudaStream_t st) -> cudaError_t {
     cudaError_t e = c->keep_stats ? cudaSuccess
                                   : cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(a.nact, 0, 2 * sizeof(unsigned int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.nact, 0, kCounters * sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
     const cudaEvent_t* ev = timed ? c->kev : nullptr;
     if (!mixed) {
@@ -636,7 +638,8 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
   const size_t pm_bytes = al(nzs * npad);
   const size_t cm_bytes = al(npad);
   const size_t hg_bytes = al(nzs * npad * sizeof(float));
-  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes + 256;
+  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + 2 * cm_bytes +
+                       hg_bytes + 256;
   if (total > kNoAllocScratchBytes)
     return fail(TEMPO_ERR_ARG,
                 "%ld columns x %d levels need %zu bytes of scratch; the fixed scratch of "
@@ -659,6 +662,8 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
   sp += pm_bytes;
   a.cmask = (uint8_t*)sp;
   sp += cm_bytes;
+  a.colcls = (uint8_t*)sp;
+  sp += cm_bytes;
   a.hgt = sp;
   sp += hg_bytes;
   a.nact = (unsigned int*)sp;
@@ -668,7 +673,7 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
   // the slot counter and the statistics accumulate with atomics: zero them first;
   // every other scratch field is written before it is read
   CUDA_TRY(cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s));
-  CUDA_TRY(cudaMemsetAsync(a.nact, 0, 2 * sizeof(unsigned int), s));
+  CUDA_TRY(cudaMemsetAsync(a.nact, 0, kCounters * sizeof(unsigned int), s));
   Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
                   c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
   CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->idf, s, nullptr, c->points_variant, c->sedim_variant));
@@ -775,10 +780,20 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
     CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     c->slab_ev.push_back(e);
   }
+  // slab weights: with four or more slabs the first and last are a quarter and the
+  // second and second-to-last half of the others, so that the pipeline fills (the
+  // first slab's copy in) and drains (the last slab's copy out) with little data
+  long wsum = 0, wcum[kMaxSlabs + 1] = {0};
+  for (int sl = 0; sl < nslab; sl++) {
+    const int edge = std::min(sl, nslab - 1 - sl);
+    wsum += (nslab >= 4) ? (edge == 0 ? 1 : edge == 1 ? 2 : 4) : 1;
+    wcum[sl + 1] = wsum;
+  }
   int rc = TEMPO_OK;
   long launches = 0;
   for (int sl = 0; sl < nslab && rc == TEMPO_OK; sl++) {
-    const long ja = b.jts + (sl * nrows) / nslab, jb = b.jts + ((sl + 1) * nrows) / nslab - 1;
+    const long ja = b.jts + (wcum[sl] * nrows) / wsum, jb = b.jts + (wcum[sl + 1] * nrows) / wsum - 1;
+    if (jb < ja) continue;  // (only when a tile has fewer rows than the weights need)
     const long rows = jb - ja + 1;
     const size_t o3 = (size_t)(ja - b.jms) * row3, c3 = (size_t)rows * row3;
     const size_t o2 = (size_t)(ja - b.jms) * row2, c2 = (size_t)rows * row2;
@@ -1306,12 +1321,13 @@ struct DualStep {
     if (!(a.sd = B.alloc<D1>((size_t)SD_N * nzs * npad)) || !(a.sr = B.alloc<D1>((size_t)SR_N * nzs * npad)) ||
         !(a.sc = B.alloc<D1>((size_t)SC_N * npad)) || !(a.act = B.alloc<int>(npad)) ||
         !(a.pmask = B.alloc<uint8_t>(nzs * npad)) || !(a.cmask = B.alloc<uint8_t>(npad)) ||
-        !(a.hgt = B.alloc<T>(nzs * npad)) || !(a.nact = B.alloc<unsigned>(2)))
+        !(a.hgt = B.alloc<T>(nzs * npad)) || !(a.nact = B.alloc<unsigned>(kCounters)) ||
+        !(a.colcls = B.alloc<uint8_t>(npad)))
       return fail(TEMPO_ERR_NOMEM, "derivative step: scratch");
     if (c->points_order && !(a.ord = B.alloc<unsigned>(nzs * npad)))
       return fail(TEMPO_ERR_NOMEM, "derivative step: point order");
     a.stats = c->d_stats;
-    if (cudaMemsetAsync(a.nact, 0, 2 * sizeof(unsigned), s) != cudaSuccess ||
+    if (cudaMemsetAsync(a.nact, 0, kCounters * sizeof(unsigned), s) != cudaSuccess ||
         cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s) != cudaSuccess)
       return fail(TEMPO_ERR_CUDA, "derivative step: counters");
     return TEMPO_OK;
