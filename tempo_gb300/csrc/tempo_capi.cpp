@@ -518,8 +518,8 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   // regime order: a point index per point
   const bool order = c->points_order != 0;
   const size_t od_bytes = order ? al(nzs * npad * sizeof(unsigned)) : 0;
-  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + 2 * cm_bytes +
-                       hg_bytes + sl_bytes + ml_bytes + nc_bytes + od_bytes + 256;
+  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes +
+                       sl_bytes + ml_bytes + nc_bytes + od_bytes + 256;
   if (int rc = ensure_scratch(c, total)) return rc;
   char* sp = (char*)(c->scratch_slot ? c->scratch2 : c->scratch);
   a.sd = sp;
@@ -533,8 +533,6 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   a.pmask = (uint8_t*)sp;
   sp += pm_bytes;
   a.cmask = (uint8_t*)sp;
-  sp += cm_bytes;
-  a.colcls = (uint8_t*)sp;
   sp += cm_bytes;
   a.hgt = sp;
   sp += hg_bytes;
@@ -557,7 +555,7 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   auto enqueue = [&](cudaStream_t st) -> cudaError_t {
     cudaError_t e = c->keep_stats ? cudaSuccess
                                   : cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(a.nact, 0, kCounters * sizeof(unsigned int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.nact, 0, 2 * sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
     const cudaEvent_t* ev = timed ? c->kev : nullptr;
     if (!mixed) {
@@ -638,8 +636,7 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
   const size_t pm_bytes = al(nzs * npad);
   const size_t cm_bytes = al(npad);
   const size_t hg_bytes = al(nzs * npad * sizeof(float));
-  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + 2 * cm_bytes +
-                       hg_bytes + 256;
+  const size_t total = sd_bytes + sr_bytes + sc_bytes + act_bytes + pm_bytes + cm_bytes + hg_bytes + 256;
   if (total > kNoAllocScratchBytes)
     return fail(TEMPO_ERR_ARG,
                 "%ld columns x %d levels need %zu bytes of scratch; the fixed scratch of "
@@ -662,8 +659,6 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
   sp += pm_bytes;
   a.cmask = (uint8_t*)sp;
   sp += cm_bytes;
-  a.colcls = (uint8_t*)sp;
-  sp += cm_bytes;
   a.hgt = sp;
   sp += hg_bytes;
   a.nact = (unsigned int*)sp;
@@ -673,7 +668,7 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
   // the slot counter and the statistics accumulate with atomics: zero them first;
   // every other scratch field is written before it is read
   CUDA_TRY(cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s));
-  CUDA_TRY(cudaMemsetAsync(a.nact, 0, kCounters * sizeof(unsigned int), s));
+  CUDA_TRY(cudaMemsetAsync(a.nact, 0, 2 * sizeof(unsigned int), s));
   Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
                   c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
   CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->idf, s, nullptr, c->points_variant, c->sedim_variant));
@@ -1321,13 +1316,12 @@ struct DualStep {
     if (!(a.sd = B.alloc<D1>((size_t)SD_N * nzs * npad)) || !(a.sr = B.alloc<D1>((size_t)SR_N * nzs * npad)) ||
         !(a.sc = B.alloc<D1>((size_t)SC_N * npad)) || !(a.act = B.alloc<int>(npad)) ||
         !(a.pmask = B.alloc<uint8_t>(nzs * npad)) || !(a.cmask = B.alloc<uint8_t>(npad)) ||
-        !(a.hgt = B.alloc<T>(nzs * npad)) || !(a.nact = B.alloc<unsigned>(kCounters)) ||
-        !(a.colcls = B.alloc<uint8_t>(npad)))
+        !(a.hgt = B.alloc<T>(nzs * npad)) || !(a.nact = B.alloc<unsigned>(2)))
       return fail(TEMPO_ERR_NOMEM, "derivative step: scratch");
     if (c->points_order && !(a.ord = B.alloc<unsigned>(nzs * npad)))
       return fail(TEMPO_ERR_NOMEM, "derivative step: point order");
     a.stats = c->d_stats;
-    if (cudaMemsetAsync(a.nact, 0, kCounters * sizeof(unsigned), s) != cudaSuccess ||
+    if (cudaMemsetAsync(a.nact, 0, 2 * sizeof(unsigned), s) != cudaSuccess ||
         cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s) != cudaSuccess)
       return fail(TEMPO_ERR_CUDA, "derivative step: counters");
     return TEMPO_OK;
