@@ -249,6 +249,8 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
         sqg = sqg + ldi<I>(a.qg + e);
         sng = sng + ldi<I>(a.ng + e);
         sqb = sqb + ldi<I>(a.qb + e);
+      } else if (do_micro || supersat) {
+        break;  // the column is active whatever the levels above hold
       }
     }
     do_ginit = hail && (f & F_FIRST) && sqg > r1 && sng < eps && sqb < eps;
