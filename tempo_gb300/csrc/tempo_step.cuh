@@ -1443,11 +1443,16 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
   io.diag2(a.mhd_sfc, t2, mhd);
 }
 
-// (8 resident blocks asked: 64 registers and a few spills, against 87 registers and 5
-// blocks unasked; the kernel waits on memory and gains from the resident warps: 4.6
-// against 4.8 ms with 6 blocks and 5.8 ms unasked at 1 M columns)
+// The mixed form asks for 8 resident blocks (64 registers and a few spills, against 87
+// registers and 5 blocks unasked; the kernel waits on memory and gains from the
+// resident warps: 4.6 against 4.8 ms with 6 blocks and 5.8 ms unasked at 1 M columns);
+// the FP64 and dual-number forms keep their registers.
+template <class R>
+__host__ __device__ constexpr int final_min_blocks() {
+  return std::is_same<R, float>::value ? 8 : 1;
+}
 template <class R, class S>
-__global__ void __launch_bounds__(128, 8) tempo_final_kernel(const __grid_constant__ StepArgs<S> a,
+__global__ void __launch_bounds__(128, final_min_blocks<R>()) tempo_final_kernel(const __grid_constant__ StepArgs<S> a,
                                                            const __grid_constant__ TempoConsts<Cst<R>> cst,
                                                            const __grid_constant__ IslandConsts<Isl<R>> ci) {
   const long nact = (long)*a.nact, npts = nact * a.nz;
