@@ -162,7 +162,7 @@ def cpu_baseline(seconds: float, nz: int, dt: float, sample_cols: int = 16384):
                       f"FP64 CPU restatement, {cores} OpenMP threads, {el:.1f} s"}
 
 
-# per-field floors below which differences are judged against the floor (the
+# per-field floors below which differences are measured against the floor (the
 # reference's existence thresholds r1 = 1e-12, r2 = 1e-6, in per-kg units)
 FLOORS = {"t": 1.0, "qv": 1e-12, "qc": 1e-12, "qr": 1e-12, "qi": 1e-12, "qs": 1e-12,
           "qg": 1e-12, "ni": 1e-6, "nr": 1e-6, "nc": 1e-6, "nwfa": 1.0, "nifa": 1.0,

@@ -5,7 +5,7 @@ from __future__ import annotations
 import numpy as np
 
 OUT3 = ("t", "qv", "qc", "qr", "qi", "qs", "qg", "ni", "nr", "nc", "nwfa", "nifa", "ng", "qb")
-# absolute floors below which differences are judged against the floor instead of the
+# absolute floors below which differences are measured against the floor instead of the
 # value (the reference's existence thresholds r1 = 1e-12 kg/m3, r2 = 1e-6 /m3 scaled
 # to per-kg mixing ratios)
 FLOOR = {"t": 1.0, "qv": 1e-12, "qc": 1e-12, "qr": 1e-12, "qi": 1e-12, "qs": 1e-12, "qg": 1e-12,
