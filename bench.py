@@ -133,6 +133,19 @@ def traffic_from_profiles(ncol: int):
         return None
 
 
+def fp32_ops_from_profiles(ncol: int):
+    """FP32 floating-point operations of one step at ncol columns (add, multiply and 2 per
+    fused multiply-add, thread instructions counted by ncu on a 65 536-column step in
+    profiles/step_fp32_ops_65k.md), scaled by columns."""
+    import re
+    try:
+        txt = (REPO / "profiles" / "step_fp32_ops_65k.md").read_text()
+        m = re.search(r"fp32_flops_per_step_(\d+)_columns = (\d+)", txt)
+        return float(m.group(2)) * ncol / float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
 def cpu_baseline(seconds: float, nz: int, dt: float, sample_cols: int = 16384):
     """The FP64 CPU restatement (oracle port) on all host cores, bounded sample."""
     import oracle
@@ -483,6 +496,18 @@ def main():
     hbm = hbm or 6800.0
     alg_bytes = ncol * (4 * nz * (N_IN3 + N_OUT3) + 4 * N_OUT2)
     achieved = alg_bytes / (step_kernel_ms / 1e3) / 1e9
+    # FP32 pipe roofline beside the HBM one: the step's FP32 operations over its kernel
+    # time, against SMs x 128 FP32 lanes x 2 x the maximum SM clock (nominal)
+    flops = fp32_ops_from_profiles(ncol)
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = sms * 128 * 2 * float(pk.get("sm_max_mhz") or 2070.0) * 1e6 / 1e12
+    fp32_roof = None
+    if flops:
+        fp32_ach = flops / (step_kernel_ms / 1e3) / 1e12
+        fp32_roof = {"achieved": fp32_ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": fp32_ach / fp32_peak, "flops_per_step": flops,
+                     "source": "ncu FP32 add/mul/fma thread instructions of one 65 536-column "
+                               "step scaled by columns; peak nominal (SMs x 128 x 2 x max clock)"}
     clocks = clk.summary()
     out = {
         "metric": METRIC, "value": value, "unit": "column-steps/s", "n_gpus": world,
@@ -508,6 +533,7 @@ def main():
                      "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src,
                      "kernel_ms": kms,
                      "kernel_share": {k: v / step_kernel_ms for k, v in kms.items()}},
+        "fp32_roofline": fp32_roof,
         "adjoint": adjoint,
         "multi_domain": multi,
         "gpu_launches": args.steps * stats.get("launches", 1),
