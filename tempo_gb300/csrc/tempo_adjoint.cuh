@@ -339,27 +339,30 @@ __global__ void __launch_bounds__(128) tempo_sedim_adjoint_kernel(
     }
     T lam_head = T(0);
     for (int k = 0; k <= ktop - 1; k++) {
+      // the level's factors once (the stores below may alias the loads for the compiler)
+      const T cxk = cx(k), ctk = ct(k), rk = rho(k);
       const T s_k = vv(k) * xs(k);
       const T s_upk = (k == ktop - 1) ? s_head : vv(k + 1) * xs(k + 1);
       const T dflux = s_upk - s_k;
-      const T xnew = xs(k) + dflux * cx(k);
+      const T xnew = xs(k) + dflux * cxk;
       const T gx = (lim > xnew) ? T(0) : lsd(f, k);
       const T lt = lsd(tf, k);
-      const T gd = gx * cx(k) + lt * ct(k);
+      const T gd = gx * cxk + lt * ctk;
       if (k == ktop - 1)
         lam_head += gd;
       else
         WR(W.ls(k + 1, nz)) += gd;
       WR(W.ls(k, nz)) -= gd;
-      lsd(SD_RHO, k) += lt * dflux * (-ct(k) / rho(k));
+      lsd(SD_RHO, k) += lt * dflux * (-ctk / rk);
       lsd(f, k) = gx;
     }
     {  // top level
-      const T xnew = xs(top) - s_top * cx(top);
+      const T cxt = cx(top), ctt = ct(top), rt = rho(top);
+      const T xnew = xs(top) - s_top * cxt;
       const T gx = (lim > xnew) ? T(0) : lsd(f, top);
       const T lt = lsd(tf, top);
-      WR(W.ls(top, nz)) += -gx * cx(top) - lt * ct(top);
-      lsd(SD_RHO, top) += lt * s_top * ct(top) / rho(top);
+      WR(W.ls(top, nz)) += -gx * cxt - lt * ctt;
+      lsd(SD_RHO, top) += lt * s_top * ctt / rt;
       lsd(f, top) = gx;
     }
     if (ktop == nz - 1)
