@@ -319,10 +319,10 @@ int tempo_set_host_slabs(tempo_ctx_t *ctx, int slabs);
 int tempo_tuning_c(tempo_ctx_t *ctx, int out[3]);
 
 /* No reference counterpart.  With on != 0, a run captures its work (counter resets and
- * the four kernels) into a CUDA graph the first time it sees a given argument set
- * (pointers, bounds, dt, flags, precision, variant) and replays the graph on later
- * runs with the same set; up to 16 graphs are kept per context.  With kernel timing on,
- * the graph carries the timing events. */
+ * the step's kernels) into a CUDA graph the first time it sees a given argument set
+ * (pointers, bounds, dt, flags, precision, kernel variants and point order) and replays
+ * the graph on later runs with the same set; up to 16 graphs are kept per context.
+ * With kernel timing on, the graph carries the timing events. */
 int tempo_set_graphs(tempo_ctx_t *ctx, int on);
 
 #ifdef __cplusplus
