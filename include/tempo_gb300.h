@@ -296,7 +296,7 @@ int tempo_set_points_variant(tempo_ctx_t *ctx, int variant);
 
 /* No reference counterpart.  Order in which the per-level kernel's threads take the
  * active points: 0 (the default) = level-major; 1 = grouped by regime (species present
- * in the input state and the side of 0 C) inside windows of 16384 consecutive
+ * in the input state and the side of 0 C) inside windows of 32768 consecutive
  * level-major points, one extra kernel per step, so that a warp's points take the same
  * branches.  The order never changes a result, only which thread computes a point.
  * tempo_run_dev_f32_noalloc_c always runs level-major. */
