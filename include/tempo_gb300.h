@@ -33,9 +33,11 @@ typedef enum {
   TEMPO_ERR_TABLE = -3,       /* missing, truncated or malformed lookup table */
   TEMPO_ERR_CUDA = -4,        /* CUDA runtime failure (message has the CUDA error string) */
   TEMPO_ERR_NOMEM = -5,       /* host or device allocation failed */
-  TEMPO_ERR_STATE = -6,       /* context not initialised / wrong precision for the call */
-  TEMPO_ERR_TIMEOUT = -7,     /* a bounded device wait gave up (status word set by the kernel) */
-  TEMPO_ERR_NONFINITE = -8    /* non-finite input detected by the validation pass */
+  TEMPO_ERR_STATE = -6,       /* context not initialised / wrong precision for the call /
+                                 the calling thread's current device is not the context's */
+  /* -7 is not used (no entry point waits on the device with a time limit) */
+  TEMPO_ERR_NONFINITE = -8    /* non-finite or non-physical input found by the validation
+                                 pass (tempo_set_validation); the state is left untouched */
 } tempo_status_t;
 
 /* ty_tempo_cfgs (src/module_mp_tempo_cfgs.F90:14-35); same field order and defaults
@@ -106,8 +108,10 @@ int tempo_default_cfgs(tempo_cfgs_t *cfgs);
  * nonzero, the three big-endian stream tables (qr_acr_qg_data_tempo_v3,
  * qr_acr_qs_data_tempo_v3, freeze_water_data_tempo_v3).  build_tables != 0 builds
  * the three tables on the GPU in FP64 instead of reading them (the reference builds
- * them offline with tools/build_tables.F90).  device: CUDA ordinal.  On success
- * *ctx receives a new context. */
+ * them offline with tools/build_tables.F90).  device: CUDA ordinal, or -1 for the
+ * calling thread's current device.  On success *ctx receives a new context.  Table
+ * files are checked as tempo_check_table_c does (existence, size, record markers,
+ * value range) and a bad file gives TEMPO_ERR_TABLE with the file's name. */
 int tempo_init_c(const int *aerosolaware_flag, const int *hailaware_flag,
                  const int *semi_sedi_flag, const int *cloud_condensation_flag,
                  const int *refl10cm_from_melting_flag, const int *ml_for_bl_nc_flag,
@@ -120,6 +124,26 @@ int tempo_ctx_destroy(tempo_ctx_t *ctx);
 
 /* Selects the kernel arithmetic for later run calls (default TEMPO_PREC_FP64). */
 int tempo_set_precision(tempo_ctx_t *ctx, int precision);
+
+/* check_before_table_read (src/module_mp_tempo_driver.F90:652-700) for one table file,
+ * on the host only (no device, no context): name is "ccn_activate" (Fortran sequential
+ * record of 8820 big-endian FP32 activated fractions, driver:625-649), "qr_acr_qg",
+ * "qr_acr_qs" or "freezewater" (big-endian FP64 stream files, driver:532-622).  Beyond
+ * the reference's existence and size checks it decodes the file: record markers, every
+ * value finite, collection and freezing values >= 0 and below 1e30 (a file written in
+ * the other byte order fails here), activated fractions in [0, 1].  TEMPO_OK or
+ * TEMPO_ERR_TABLE with the reason in tempo_last_error(); TEMPO_ERR_ARG for an unknown
+ * name. */
+int tempo_check_table_c(const char *name, const char *path);
+
+/* No reference counterpart (the reference trusts its inputs).  With on != 0, every later
+ * run first scans the tile's inputs: temperature (t, or th and pii), p, dz, qv and every
+ * present mass, number, aerosol and volume array must be finite; t (or th and pii), p and
+ * dz must be > 0.  A failed scan returns TEMPO_ERR_NONFINITE naming the first bad field
+ * and (i, k, j) index, before any array is modified.  Host-array runs scan on the host
+ * before the copy; device-array runs scan with one kernel and wait for its verdict (the
+ * call then synchronises with its stream).  Off by default. */
+int tempo_set_validation(tempo_ctx_t *ctx, int on);
 
 /* tempo_run (src/module_mp_tempo_driver.F90:187-513) on host arrays of doubles (the
  * reference's default kind_phys).  Copies the tile to the device, runs the step,
@@ -142,20 +166,29 @@ int tempo_run_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double dt, int
                 int jde, int kds, int kde, int ims, int ime, int jms, int jme, int kms, int kme,
                 int its, int ite, int jts, int jte, int kts, int kte, tempo_diags_t *tempo_diags);
 
-/* Same as tempo_run_c for host arrays of floats (the reference built with
- * -DSINGLE_PREC, src/machine.F90:13-17). */
+/* tempo_run (src/module_mp_tempo_driver.F90:187-513) on host arrays of floats: the
+ * reference built with -DSINGLE_PREC (src/machine.F90:13-17), whose tempo_run keeps the
+ * same argument list with real(wp) = real(4).  Same arguments, order and meaning as
+ * tempo_run_c; the step runs in the context's precision (TEMPO_PREC_MIXED for FP32
+ * storage). */
 int tempo_run_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float dt, int itimestep,
                     float *t, float *th, const float *pii, const float *p, const float *w,
                     const float *dz, float *qv, float *qc, float *qr, float *qi, float *qs,
                     float *qg, float *ni, float *nr, float *nc, float *nwfa, float *nifa,
-                    float *ng, float *qb, const int *land_input, int ims, int ime, int jms,
-                    int jme, int kms, int kme, int its, int ite, int jts, int jte, int kts,
-                    int kte, tempo_diags_t *tempo_diags);
+                    float *ng, float *qb, const float *qc_bl, const float *qcfrac_bl,
+                    float *qcfrac, float *qifrac, const float *thten_bl, const float *qvten_bl,
+                    const float *qcten_bl, const float *qiten_bl, const float *thten_lwrad,
+                    const float *thten_swrad, const int *land_input, int ids, int ide, int jds,
+                    int jde, int kds, int kde, int ims, int ime, int jms, int jme, int kms,
+                    int kme, int its, int ite, int jts, int jte, int kts, int kte,
+                    tempo_diags_t *tempo_diags);
 
 /* tempo_run on DEVICE arrays (doubles) already resident in HBM, enqueued on `stream`
  * (a cudaStream_t); returns after enqueueing.  Same
  * arguments as tempo_run_c minus the inert ones.  A NULL stream is the CUDA default
- * stream, so the call orders with other work issued there. */
+ * stream, so the call orders with other work issued there.  The calling thread's
+ * current device must be the context's device (the stream and the arrays belong to
+ * it); otherwise TEMPO_ERR_STATE before any work is enqueued. */
 int tempo_run_dev_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double dt,
                     int itimestep, double *t, double *th, const double *pii, const double *p,
                     const double *w, const double *dz, double *qv, double *qc, double *qr,
@@ -179,16 +212,22 @@ int tempo_run_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float 
  * memory: for hosts that must not allocate device memory inside their time step (a
  * model whose device memory pool is sized once at start-up with no headroom, or one
  * that must not let a physics call synchronise the device, as cudaFree does).  The
- * step's scratch is a fixed 64 MiB device array of the library, reserved when the
- * library's module loads on a device; its address is looked up on the first call for
- * each device (with that device current), so make that first call before any stream
- * capture and before any phase in which the host forbids CUDA runtime set-up.  Every
- * call reuses the array and finds the previous call's contents there; the step clears
- * what must start at zero (its active-column counter) itself.  Tiles that need more scratch (about 245 * nz + 45 bytes per column:
+ * step's scratch is a fixed 64 MiB device array of the library.  The array is reserved
+ * on a device when the library's device code is loaded there; with CUDA's lazy module
+ * loading (the default) that is the first use of the library's kernels on the device,
+ * so make the first call of this entry point (which also looks up the array's address,
+ * with that device current) before the host sizes its memory pool, before any stream
+ * capture and before any phase in which the host forbids CUDA runtime set-up.  The
+ * calling thread's current device must be the context's device (TEMPO_ERR_STATE
+ * otherwise, before any work).  Every call reuses the array and finds the previous
+ * call's contents there; the step clears what must start at zero (its active-column
+ * counter) itself.  Tiles that need more scratch (about 245 * nz + 45 bytes per column:
  * about 4 200 columns at 65 levels) are rejected with TEMPO_ERR_ARG.  The scratch is
  * shared by every context on a device: calls on one device must not overlap (issue
  * them on one stream, or wait for one call's work before the next starts on another
- * stream); overlapping calls race on the scratch.  Results equal tempo_run_dev_f32_c's. */
+ * stream); overlapping calls race on the scratch.  The call records no kernel timing:
+ * after it, tempo_kernel_times_c returns TEMPO_ERR_STATE until a timed run.  Results
+ * equal tempo_run_dev_f32_c's. */
 int tempo_run_dev_f32_noalloc_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, float dt,
                                 int itimestep, float *t, float *th, const float *pii,
                                 const float *p, const float *w, const float *dz, float *qv,
@@ -227,7 +266,8 @@ int tempo_last_stats_c(tempo_ctx_t *ctx, long out[8]);
 /* No reference counterpart.  With on != 0, each later run records CUDA events on its
  * stream around its kernels; tempo_kernel_times_c waits for the last run's events and
  * returns five durations in milliseconds: prep, the regime-order kernels (0 in
- * level-major order), points, sedim, final. */
+ * level-major order), points, sedim, final.  It returns TEMPO_ERR_STATE when the last
+ * run recorded no events (timing off, or tempo_run_dev_f32_noalloc_c). */
 int tempo_set_kernel_timing(tempo_ctx_t *ctx, int on);
 int tempo_kernel_times_c(tempo_ctx_t *ctx, float ms[5]);
 

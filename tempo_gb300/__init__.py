@@ -23,6 +23,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = ["TempoError", "TempoContext", "tempo_init", "tempo_run", "default_cfgs", "DIFF_FIELDS",
+           "check_table", "EXTRA_FIELDS",
            "PREC_FP64", "PREC_MIXED", "DIAG2", "DIAG3", "load_library", "REPO_TABLES"]
 
 PKG = Path(__file__).resolve().parent
@@ -36,6 +37,9 @@ DIAG3 = ("refl10cm", "re_cloud", "re_ice", "re_snow", "rain_med_vol_diam",
          "graupel_med_vol_diam", "cloud_number_mixing_ratio")
 FIELDS = ("t", "th", "pii", "p", "w", "dz", "qv", "qc", "qr", "qi", "qs", "qg", "ni", "nr",
           "nc", "nwfa", "nifa", "ng", "qb")
+# the optional inputs of tempo_run between qb and land_input (driver:191-195)
+EXTRA_FIELDS = ("qc_bl", "qcfrac_bl", "qcfrac", "qifrac", "thten_bl", "qvten_bl", "qcten_bl",
+                "qiten_bl", "thten_lwrad", "thten_swrad")
 CFG_FLAGS = ("aerosolaware_flag", "hailaware_flag", "ml_for_bl_nc_flag", "ml_for_nc_flag",
              "semi_sedi_flag", "refl10cm_from_melting_flag", "turn_off_micro_flag",
              "cloud_condensation_flag", "verbose", "check_tables")
@@ -44,7 +48,7 @@ DIAG_FLAGS = ("refl10cm_flag", "re_cloud_flag", "re_ice_flag", "re_snow_flag",
               "cloud_number_mixing_ratio_flag")
 STATUS = {0: "TEMPO_OK", -1: "TEMPO_ERR_ARG", -2: "TEMPO_ERR_UNSUPPORTED",
           -3: "TEMPO_ERR_TABLE", -4: "TEMPO_ERR_CUDA", -5: "TEMPO_ERR_NOMEM",
-          -6: "TEMPO_ERR_STATE", -7: "TEMPO_ERR_TIMEOUT", -8: "TEMPO_ERR_NONFINITE"}
+          -6: "TEMPO_ERR_STATE", -8: "TEMPO_ERR_NONFINITE"}
 
 
 class TempoError(RuntimeError):
@@ -118,7 +122,8 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
                                 + [_DP] * 19 + [_DP] * 10 + [_IP] + [i] * 18
                                 + [ctypes.POINTER(TempoDiags)])
     lib.tempo_run_f32_c.argtypes = ([_VP, ctypes.POINTER(TempoCfgs), ctypes.c_float, i]
-                                    + [_FP] * 19 + [_IP] + [i] * 12 + [ctypes.POINTER(TempoDiags)])
+                                    + [_FP] * 19 + [_FP] * 10 + [_IP] + [i] * 18
+                                    + [ctypes.POINTER(TempoDiags)])
     lib.tempo_run_dev_c.argtypes = ([_VP, ctypes.POINTER(TempoCfgs), ctypes.c_double, i]
                                     + [_VP] * 19 + [_VP] + [i] * 12
                                     + [ctypes.POINTER(TempoDiags), _VP])
@@ -152,6 +157,8 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
                                          ctypes.POINTER(TempoState), ctypes.POINTER(TempoState),
                                          ctypes.POINTER(TempoDiags)] + [i] * 12 + [_VP])
     lib.tempo_kernel_times_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_float)]
+    lib.tempo_check_table_c.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+    lib.tempo_set_validation.argtypes = [_VP, i]
     _lib = lib
     return lib
 
@@ -159,6 +166,13 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
 def _check(rc: int):
     if rc != 0:
         raise TempoError(rc, load_library().tempo_last_error().decode())
+
+
+def check_table(name: str, path: os.PathLike) -> None:
+    """tempo_check_table_c: validates one table file on the host (no GPU); raises
+    TempoError (TEMPO_ERR_TABLE) with the reason for a missing, truncated, byte-swapped
+    or otherwise malformed file."""
+    _check(load_library().tempo_check_table_c(name.encode(), str(path).encode()))
 
 
 def default_cfgs(**over) -> TempoCfgs:
@@ -218,6 +232,10 @@ class TempoContext:
     def set_precision(self, mode: int):
         _check(load_library().tempo_set_precision(self._h, int(mode)))
 
+    def set_validation(self, on: bool = True):
+        """tempo_set_validation: scan the inputs of later runs for non-finite values."""
+        _check(load_library().tempo_set_validation(self._h, int(bool(on))))
+
     # ---- host arrays -----------------------------------------------------------------
     def run(self, fields: dict, dt: float, itimestep: int, diags: Optional[dict] = None,
             bounds=None, cfgs: Optional[TempoCfgs] = None):
@@ -227,7 +245,6 @@ class TempoContext:
         p = fields["p"]
         nj, nk, ni = p.shape
         b = list(bounds) if bounds is not None else [1, ni, 1, nj, 1, nk] * 3
-        ids, ide, jds, jde, kds, kde, ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte = b
         d = TempoDiags()
         for n in DIAG2 + DIAG3:
             a = (diags or {}).get(n)
@@ -235,18 +252,12 @@ class TempoContext:
                 setattr(d, n, a.ctypes.data)
         land = fields.get("land_input")
         land_p = _np_ptr(land, ctypes.c_int) if land is not None else None
-        if p.dtype == np.float64:
-            ptrs = [_np_ptr(fields.get(n), ctypes.c_double) for n in FIELDS]
-            extra = [_np_ptr(fields.get(n), ctypes.c_double) for n in
-                     ("qc_bl", "qcfrac_bl", "qcfrac", "qifrac", "thten_bl", "qvten_bl",
-                      "qcten_bl", "qiten_bl", "thten_lwrad", "thten_swrad")]
-            _check(lib.tempo_run_c(self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs,
-                                   *extra, land_p, *b, ctypes.byref(d)))
-        else:
-            ptrs = [_np_ptr(fields.get(n), ctypes.c_float) for n in FIELDS]
-            _check(lib.tempo_run_f32_c(self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs,
-                                       land_p, ims, ime, jms, jme, kms, kme, its, ite, jts, jte,
-                                       kts, kte, ctypes.byref(d)))
+        ct = ctypes.c_double if p.dtype == np.float64 else ctypes.c_float
+        ptrs = [_np_ptr(fields.get(n), ct) for n in FIELDS]
+        extra = [_np_ptr(fields.get(n), ct) for n in EXTRA_FIELDS]
+        fn = lib.tempo_run_c if p.dtype == np.float64 else lib.tempo_run_f32_c
+        _check(fn(self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs, *extra, land_p,
+                  *b, ctypes.byref(d)))
 
     # ---- device tensors --------------------------------------------------------------
     def run_device(self, fields: dict, dt: float, itimestep: int, diags: Optional[dict] = None,

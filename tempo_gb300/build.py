@@ -34,6 +34,7 @@ UNITS = [
     ("tempo_deriv_f32.cu", [], "tempo_deriv_f32"),
     ("tempo_noalloc.cu", [], "tempo_noalloc"),
     ("tempo_melt.cu", ["-fmad=false"], "tempo_melt"),
+    ("tempo_validate.cu", [], "tempo_validate"),
 ]
 HOST_UNITS = ["tempo_capi.cpp", "tempo_host_init.cpp"]
 

@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "tempo_gb300.h"
@@ -120,6 +121,10 @@ struct tempo_ctx {
   std::vector<cudaEvent_t> slab_ev;
   bool keep_stats = false;
   int host_slabs = 0;  // slabs of a host-array run (0: from the tile's size)
+  bool times_valid = false;  // the last run recorded the kernel-timing events
+  bool validate = false;     // input scan before each run (tempo_set_validation)
+  bool in_host_run = false;  // run_dev called by run_host (inputs scanned on the host)
+  unsigned long long* d_first_bad = nullptr;  // verdict of the device input scan
 };
 
 namespace {
@@ -198,6 +203,111 @@ std::string join(const char* dir, const char* name) {
   return s + name;
 }
 
+// ---- table files (driver:532-700) ---------------------------------------------------
+// Largest value a collection or freezing table may hold: the tables are rates and
+// probabilities far below it, while FP64 read in the wrong byte order gives values of
+// any exponent.
+constexpr double kTableMax = 1e30;
+
+const char* table_file_of(const char* name) {
+  if (!std::strcmp(name, "ccn_activate")) return "ccn_activate.bin";
+  if (!std::strcmp(name, "qr_acr_qg")) return "qr_acr_qg_data_tempo_v3";
+  if (!std::strcmp(name, "qr_acr_qs")) return "qr_acr_qs_data_tempo_v3";
+  if (!std::strcmp(name, "freezewater")) return "freeze_water_data_tempo_v3";
+  return nullptr;
+}
+// bytes of a table file: one Fortran record of FP32 for the CCN table, FP64 streams of
+// the arrays in file order (tables.F90:122-127, 298-309, 438-442) for the others
+long table_file_bytes(const char* name) {
+  if (!std::strcmp(name, "ccn_activate")) return CCN_COUNT * 4 + 8;
+  if (!std::strcmp(name, "qr_acr_qg")) return 5 * QG_COUNT * 8;
+  if (!std::strcmp(name, "qr_acr_qs")) return 12 * QS_COUNT * 8;
+  if (!std::strcmp(name, "freezewater")) return (4 * QRFZ_COUNT + 2 * QCFZ_COUNT) * 8;
+  return -1;
+}
+
+// check_before_table_read (driver:652-700): the file exists and has the table's size
+int check_table_size(const char* name, const char* path) {
+  const long want = table_file_bytes(name);
+  if (want < 0) return fail(TEMPO_ERR_ARG, "unknown table \"%s\" (ccn_activate, qr_acr_qg, qr_acr_qs, freezewater)", name);
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(TEMPO_ERR_TABLE, "table file \"%s\" was not found", path);
+  std::fseek(f, 0, SEEK_END);
+  const long size = std::ftell(f);
+  std::fclose(f);
+  if (size != want)
+    return fail(TEMPO_ERR_TABLE, "table file \"%s\" has a size of %ld bytes but the %s table needs %ld bytes",
+                path, size, name, want);
+  return TEMPO_OK;
+}
+
+uint32_t be32(const uint8_t* b) {
+  return (uint32_t)b[0] << 24 | (uint32_t)b[1] << 16 | (uint32_t)b[2] << 8 | (uint32_t)b[3];
+}
+double be64_double(const uint8_t* b) {
+  uint64_t u = 0;
+  for (int k = 0; k < 8; k++) u = u << 8 | b[k];
+  double x;
+  std::memcpy(&x, &u, 8);
+  return x;
+}
+
+// The content of the CCN file: record markers equal to the record's length, fractions
+// in [0, 1].  buf holds the whole file.
+int check_ccn_bytes(const std::vector<uint8_t>& buf, const char* path) {
+  if (be32(buf.data()) != (uint32_t)(CCN_COUNT * 4) || std::memcmp(buf.data(), buf.data() + buf.size() - 4, 4))
+    return fail(TEMPO_ERR_TABLE, "%s: bad record markers (expected %ld in big-endian order)", path,
+                CCN_COUNT * 4);
+  for (long i = 0; i < CCN_COUNT; i++) {
+    const uint32_t u = be32(buf.data() + 4 + 4 * i);
+    float v;
+    std::memcpy(&v, &u, 4);
+    if (!std::isfinite(v) || v < 0.f || v > 1.f)
+      return fail(TEMPO_ERR_TABLE, "%s: activated fraction %g out of [0, 1] at %ld", path, (double)v, i);
+  }
+  return TEMPO_OK;
+}
+
+// one decoded value of a collection or freezing table
+bool table_value_ok(double x) { return std::isfinite(x) && x >= 0.0 && x < kTableMax; }
+
+// tempo_check_table_c: size, then every value
+int check_table_file(const char* name, const char* path) {
+  if (int rc = check_table_size(name, path)) return rc;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(TEMPO_ERR_TABLE, "cannot open %s", path);
+  int rc = TEMPO_OK;
+  if (!std::strcmp(name, "ccn_activate")) {
+    std::vector<uint8_t> buf(CCN_COUNT * 4 + 8);
+    if (std::fread(buf.data(), 1, buf.size(), f) != buf.size())
+      rc = fail(TEMPO_ERR_TABLE, "%s: short read", path);
+    else
+      rc = check_ccn_bytes(buf, path);
+  } else {
+    const long n = table_file_bytes(name) / 8;
+    std::vector<uint8_t> buf((size_t)1 << 23);
+    for (long i0 = 0; i0 < n && rc == TEMPO_OK;) {
+      const long m = std::min<long>(n - i0, (long)buf.size() / 8);
+      if ((long)std::fread(buf.data(), 8, m, f) != m) {
+        rc = fail(TEMPO_ERR_TABLE, "%s: short read", path);
+        break;
+      }
+      for (long i = 0; i < m; i++) {
+        const double x = be64_double(buf.data() + 8 * i);
+        if (!table_value_ok(x)) {
+          rc = fail(TEMPO_ERR_TABLE,
+                    "%s: value %g at element %ld is negative, not finite or above %g (a file in "
+                    "the wrong byte order reads so)", path, x, i0 + i, kTableMax);
+          break;
+        }
+      }
+      i0 += m;
+    }
+  }
+  std::fclose(f);
+  return rc;
+}
+
 // read_table_ccn (driver:625-649): Fortran sequential unformatted, big-endian FP32,
 // one record of 8820 values between 4-byte length markers.
 int read_ccn(tempo_ctx* c, const char* dir) {
@@ -210,16 +320,11 @@ int read_ccn(tempo_ctx* c, const char* dir) {
   std::fclose(f);
   if (got != buf.size() || extra != EOF)
     return fail(TEMPO_ERR_TABLE, "%s has the wrong size (expected %zu bytes)", path.c_str(), buf.size());
-  uint32_t m0 = (uint32_t)buf[0] << 24 | (uint32_t)buf[1] << 16 | (uint32_t)buf[2] << 8 | buf[3];
-  if (m0 != (uint32_t)(CCN_COUNT * 4) || std::memcmp(buf.data(), buf.data() + buf.size() - 4, 4))
-    return fail(TEMPO_ERR_TABLE, "%s: bad record markers", path.c_str());
+  if (int rc = check_ccn_bytes(buf, path.c_str())) return rc;
   std::vector<float> v(CCN_COUNT);
   for (long i = 0; i < CCN_COUNT; i++) {
-    const uint8_t* b = buf.data() + 4 + 4 * i;
-    uint32_t u = (uint32_t)b[0] << 24 | (uint32_t)b[1] << 16 | (uint32_t)b[2] << 8 | b[3];
+    const uint32_t u = be32(buf.data() + 4 + 4 * i);
     std::memcpy(&v[i], &u, 4);
-    if (!std::isfinite(v[i]) || v[i] < 0.f || v[i] > 1.f)
-      return fail(TEMPO_ERR_TABLE, "%s: activated fraction out of [0,1] at %ld", path.c_str(), i);
   }
   CUDA_TRY(cudaMemcpy(c->t64.tnccn, v.data(), CCN_COUNT * 4, cudaMemcpyHostToDevice));
   return TEMPO_OK;
@@ -267,11 +372,12 @@ int read_stream_table(tempo_ctx* c, const std::string& path, int narr, const lon
     }
     if (host_little()) bswap8(host.data(), counts[a]);
     for (long i = 0; i < counts[a]; i++)
-      if (!std::isfinite(host[i]) || host[i] < 0.0) {
+      if (!table_value_ok(host[i])) {
         std::fclose(f);
         cudaFree(dtmp);
-        return fail(TEMPO_ERR_TABLE, "%s: array %d entry %ld is negative or not finite",
-                    path.c_str(), a, i);
+        return fail(TEMPO_ERR_TABLE,
+                    "%s: array %d entry %ld = %g is negative, not finite or above %g (a file in the "
+                    "wrong byte order reads so)", path.c_str(), a, i, host[i], kTableMax);
       }
     cudaError_t e = cudaMemcpy(dtmp, host.data(), counts[a] * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = aos_scatter(aos[a], dtmp, counts[a], nfam[a], slot[a], c->stream);
@@ -384,10 +490,11 @@ struct RunArrays {
 
 // Validates the argument list and launches the step on device arrays.
 // Validates a run's arguments and fills the step arguments (everything but scratch).
+// The checks of a run's arguments that need no context, in the order a caller reads
+// them; run calls make them before they look at the context, so that a bad argument
+// list is reported as such (TEMPO_ERR_ARG) whatever the context.
 template <class S>
-int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, const RunArrays<S>& A,
-               const Bounds& b, const tempo_diags_t* dg, StepArgs<S>& a) {
-  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+int check_run_args(const tempo_cfgs_t* cfg, double dt, const RunArrays<S>& A, const Bounds& b) {
   if (!cfg) return fail(TEMPO_ERR_ARG, "NULL tempo_cfgs");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(TEMPO_ERR_ARG, "dt must be > 0 (got %g)", dt);
   if (int rc = check_bounds(b)) return rc;
@@ -395,6 +502,118 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
     return fail(TEMPO_ERR_ARG, "a required array (p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr) is NULL");
   if (!A.t && !(A.th && A.pii))
     return fail(TEMPO_ERR_ARG, "tempo_run requires either t or th and pii");
+  return TEMPO_OK;
+}
+
+// the calling thread's current device must be the context's: the caller's stream and
+// device arrays belong to it, and the context's tables live there
+int check_current_device(const tempo_ctx* c) {
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) return fail(TEMPO_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (cur != c->device)
+    return fail(TEMPO_ERR_STATE,
+                "the calling thread's current device is %d but the context lives on device %d "
+                "(cudaSetDevice(%d) before a device-array call)", cur, c->device, c->device);
+  return TEMPO_OK;
+}
+
+// The input fields of a run for the validation scan, with their names; t, th, pii, p
+// and dz must be > 0, the others finite.
+template <class S>
+ValidateFields<S> validate_fields(const RunArrays<S>& A, const Bounds& b, const char** names) {
+  ValidateFields<S> v{};
+  const S* f[] = {A.t, A.th, A.pii, A.p, A.dz, A.w, A.qv, A.qc, A.qr, A.qi, A.qs, A.qg,
+                  A.ni, A.nr, A.nc, A.nwfa, A.nifa, A.ng, A.qb};
+  static const char* nm[] = {"t", "th", "pii", "p", "dz", "w", "qv", "qc", "qr", "qi", "qs",
+                             "qg", "ni", "nr", "nc", "nwfa", "nifa", "ng", "qb"};
+  const int n = (int)(sizeof f / sizeof f[0]);
+  for (int i = 0; i < n; i++) {
+    v.p[i] = f[i];
+    v.positive[i] = i < 5;
+    names[i] = nm[i];
+  }
+  v.nf = n;
+  v.NI = (long)b.ime - b.ims + 1;
+  v.NK = (long)b.kme - b.kms + 1;
+  v.i0 = b.its - b.ims;
+  v.k0 = b.kts - b.kms;
+  v.j0 = b.jts - b.jms;
+  v.ti = b.ite - b.its + 1;
+  v.tj = b.jte - b.jts + 1;
+  v.nz = b.kte - b.kts + 1;
+  return v;
+}
+
+// the message of a failed scan: code = q * kValidateFields + f
+template <class S>
+int validation_failure(const ValidateFields<S>& v, const Bounds& b, const char** names,
+                       unsigned long long code, double value) {
+  const long q = (long)(code / kValidateFields);
+  const int f = (int)(code % kValidateFields);
+  const long i = q % v.ti, k = (q / v.ti) % v.nz, j = q / ((long)v.ti * v.nz);
+  return fail(TEMPO_ERR_NONFINITE, "input %s(%ld, %ld, %ld) = %g is %s", names[f], b.its + i,
+              b.kts + k, b.jts + j, value, v.positive[f] ? "not finite and > 0" : "not finite");
+}
+
+// The validation scan on host arrays, rows of the tile split over host threads.
+template <class S>
+int validate_host(const RunArrays<S>& A, const Bounds& b) {
+  const char* names[kValidateFields];
+  const ValidateFields<S> v = validate_fields(A, b, names);
+  const int nthr = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::vector<unsigned long long> first(nthr, ~0ull);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nthr; t++)
+    pool.emplace_back([&, t] {
+      for (long j = t; j < v.tj; j += nthr)
+        for (long k = 0; k < v.nz; k++)
+          for (long i = 0; i < v.ti; i++) {
+            const long e = (v.i0 + i) + (v.k0 + k) * v.NI + (v.j0 + j) * v.NI * v.NK;
+            const long q = i + v.ti * (k + (long)v.nz * j);
+            for (int f = 0; f < v.nf; f++) {
+              if (!v.p[f]) continue;
+              const double x = (double)v.p[f][e];
+              if (!std::isfinite(x) || (v.positive[f] && !(x > 0.0))) {
+                first[t] = std::min(first[t], (unsigned long long)q * kValidateFields + f);
+                break;
+              }
+            }
+          }
+    });
+  for (auto& th : pool) th.join();
+  const unsigned long long code = *std::min_element(first.begin(), first.end());
+  if (code == ~0ull) return TEMPO_OK;
+  const long q = (long)(code / kValidateFields);
+  const long i = q % v.ti, k = (q / v.ti) % v.nz, j = q / ((long)v.ti * v.nz);
+  const double x = (double)v.p[code % kValidateFields][(v.i0 + i) + (v.k0 + k) * v.NI + (v.j0 + j) * v.NI * v.NK];
+  return validation_failure(v, b, names, code, x);
+}
+
+// The validation scan on device arrays: one kernel on stream s, then a wait for its verdict.
+template <class S>
+int validate_dev(tempo_ctx* c, const RunArrays<S>& A, const Bounds& b, cudaStream_t s) {
+  const char* names[kValidateFields];
+  const ValidateFields<S> v = validate_fields(A, b, names);
+  unsigned long long code = ~0ull;
+  CUDA_TRY(cudaMemcpyAsync(c->d_first_bad, &code, sizeof code, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(launch_validate(v, c->d_first_bad, s));
+  CUDA_TRY(cudaMemcpyAsync(&code, c->d_first_bad, sizeof code, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (code == ~0ull) return TEMPO_OK;
+  const long q = (long)(code / kValidateFields);
+  const long i = q % v.ti, k = (q / v.ti) % v.nz, j = q / ((long)v.ti * v.nz);
+  S x{};
+  CUDA_TRY(cudaMemcpy(&x, v.p[code % kValidateFields] + (v.i0 + i) + (v.k0 + k) * v.NI + (v.j0 + j) * v.NI * v.NK,
+                      sizeof x, cudaMemcpyDeviceToHost));
+  return validation_failure(v, b, names, code, (double)x);
+}
+
+template <class S>
+int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, const RunArrays<S>& A,
+               const Bounds& b, const tempo_diags_t* dg, StepArgs<S>& a) {
+  if (int rc = check_run_args(cfg, dt, A, b)) return rc;
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
   if (A.qc_bl && A.qcfrac_bl && !c->d_mlnet)
     return fail(TEMPO_ERR_STATE, "the boundary-layer cloud path (qc_bl, qcfrac_bl) needs the "
                 "cloud-number network (tempo_set_ml_cloud_number_c)");
@@ -496,6 +715,9 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
             const Bounds& b, const tempo_diags_t* dg, cudaStream_t s) {
   StepArgs<S> a;
   if (int rc = build_args(c, cfg, dt, itimestep, A, b, dg, a)) return rc;
+  if (int rc = check_current_device(c)) return rc;
+  if (c->validate && !c->in_host_run)
+    if (int rc = validate_dev(c, A, b, s)) return rc;
   const bool mixed = c->precision == TEMPO_PREC_MIXED;
   // scratch: island-type point fields (double or double-float, 8 bytes either way),
   // bulk-type fall speeds, per-slot sums, slot map, masks and the slot counter
@@ -551,6 +773,7 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
   if (!mixed && sizeof(S) != sizeof(double))
     return fail(TEMPO_ERR_STATE, "FP32 arrays need TEMPO_PREC_MIXED (tempo_set_precision)");
   const bool timed = c->kernel_timing;
+  c->times_valid = timed;
   // the step's work on stream st: counters reset, then the four kernels
   auto enqueue = [&](cudaStream_t st) -> cudaError_t {
     cudaError_t e = c->keep_stats ? cudaSuccess
@@ -621,6 +844,9 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
                     cudaStream_t s) {
   StepArgs<float> a;
   if (int rc = build_args(c, cfg, dt, itimestep, A, b, dg, a)) return rc;
+  // the fixed scratch is looked up for c->device; kernels launched from another
+  // current device would reach that device's array without peer access
+  if (int rc = check_current_device(c)) return rc;
   if (a.flags & (F_SEMI | F_MELT | F_MLNC))
     return fail(TEMPO_ERR_UNSUPPORTED, "semi-Lagrangian sedimentation, the melting-layer reflectivity "
                 "and the ML cloud number need work space beyond the fixed scratch of "
@@ -665,6 +891,9 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
   a.stats = c->d_stats;
   c->last_cols = a.ncol;
   c->launches = kStepLaunches;
+  c->times_valid = false;  // no timing events: an earlier run's times are not this step's
+  if (c->validate)
+    if (int rc = validate_dev(c, A, b, s)) return rc;
   // the slot counter and the statistics accumulate with atomics: zero them first;
   // every other scratch field is written before it is read
   CUDA_TRY(cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s));
@@ -679,8 +908,10 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
 template <class S>
 int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, const RunArrays<S>& H,
              const Bounds& b, tempo_diags_t* dg) {
+  if (int rc = check_run_args(cfg, dt, H, b)) return rc;
   if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
-  if (int rc = check_bounds(b)) return rc;
+  if (c->validate)
+    if (int rc = validate_host(H, b)) return rc;
   const size_t n3 = (size_t)(b.ime - b.ims + 1) * (b.kme - b.kms + 1) * (b.jme - b.jms + 1);
   const size_t n2 = (size_t)(b.ime - b.ims + 1) * (b.jme - b.jms + 1);
   const size_t t2 = (size_t)(b.ite - b.its + 1) * (b.jte - b.jts + 1);
@@ -818,9 +1049,11 @@ int run_host(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, co
     for (int i = 0; i < 15; i++)
       *ddp[i] = d[n_in + 1 + i] ? (void*)((S*)d[n_in + 1 + i] + (i < 8 ? od2 : od3)) : nullptr;
     c->keep_stats = true;  // the counters sum (early exits) and take maxima over slabs
+    c->in_host_run = true;
     c->scratch_slot = (two && (sl & 1)) ? 1 : 0;
     rc = run_dev(c, cfg, dt, itimestep, D, bs, &ddg, cs);
     c->keep_stats = false;
+    c->in_host_run = false;
     c->scratch_slot = 0;
     if (rc) break;
     launches += c->launches;
@@ -890,6 +1123,16 @@ int tempo_init_c(const int* aerosolaware_flag, const int* hailaware_flag, const 
   if (cloud_condensation_flag) cfgs->cloud_condensation_flag = *cloud_condensation_flag != 0;
   if (refl10cm_from_melting_flag) cfgs->refl10cm_from_melting_flag = *refl10cm_from_melting_flag != 0;
 
+  // the table files first (existence and size, check_before_table_read, driver:652-700),
+  // before any device work
+  if (int rc = check_table_size("ccn_activate", join(table_dir, "ccn_activate.bin").c_str())) return rc;
+  if (!build_tables)
+    for (const char* nm : {"freezewater", "qr_acr_qs", "qr_acr_qg"})
+      if (int rc = check_table_size(nm, join(table_dir, table_file_of(nm)).c_str())) return rc;
+  if (device < 0) {
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return fail(TEMPO_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  }
   tempo_ctx* c = new (std::nothrow) tempo_ctx();
   if (!c) return fail(TEMPO_ERR_NOMEM, "context allocation failed");
   auto bail = [&](int rc) {
@@ -913,6 +1156,7 @@ int tempo_init_c(const int* aerosolaware_flag, const int* hailaware_flag, const 
   int rc;
   if ((rc = alloc_tables(c))) return bail(rc);
   if ((rc = dev_alloc(&c->d_stats, 8))) return bail(rc);
+  if ((rc = dev_alloc(&c->d_first_bad, 1))) return bail(rc);
   e = build_small_tables(c->t64, c->bins, c->c64, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return bail(fail(TEMPO_ERR_CUDA, "small tables: %s", cudaGetErrorString(e)));
@@ -937,6 +1181,7 @@ int tempo_ctx_destroy(tempo_ctx_t* c) {
   cudaFree(c->scratch);
   cudaFree(c->scratch2);
   cudaFree(c->d_stats);
+  cudaFree(c->d_first_bad);
   cudaFree(c->d_mlnet);
   for (auto& m : c->mirrors) cudaFree(m.d);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -961,6 +1206,17 @@ int tempo_set_precision(tempo_ctx_t* c, int precision) {
   return TEMPO_OK;
 }
 
+int tempo_set_validation(tempo_ctx_t* c, int on) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  c->validate = on != 0;
+  return TEMPO_OK;
+}
+
+int tempo_check_table_c(const char* name, const char* path) {
+  if (!name || !path) return fail(TEMPO_ERR_ARG, "NULL name or path");
+  return check_table_file(name, path);
+}
+
 int tempo_set_kernel_timing(tempo_ctx_t* c, int on) {
   if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
   CUDA_TRY(cudaSetDevice(c->device));
@@ -973,6 +1229,9 @@ int tempo_set_kernel_timing(tempo_ctx_t* c, int on) {
 int tempo_kernel_times_c(tempo_ctx_t* c, float ms[5]) {
   if (!c || !ms) return fail(TEMPO_ERR_ARG, "NULL argument");
   if (!c->kernel_timing) return fail(TEMPO_ERR_STATE, "kernel timing is off (tempo_set_kernel_timing)");
+  if (!c->times_valid)
+    return fail(TEMPO_ERR_STATE, "the last run recorded no kernel times (no timed run yet, or "
+                "tempo_run_dev_f32_noalloc_c, which records none)");
   CUDA_TRY(cudaSetDevice(c->device));
   CUDA_TRY(cudaEventSynchronize(c->kev[kStepPhases]));
   for (int i = 0; i < kStepPhases; i++) CUDA_TRY(cudaEventElapsedTime(&ms[i], c->kev[i], c->kev[i + 1]));
@@ -1003,9 +1262,17 @@ int tempo_run_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, float dt, int itime
                     float* th, const float* pii, const float* p, const float* w, const float* dz,
                     float* qv, float* qc, float* qr, float* qi, float* qs, float* qg, float* ni,
                     float* nr, float* nc, float* nwfa, float* nifa, float* ng, float* qb,
-                    const int* land_input, int ims, int ime, int jms, int jme, int kms, int kme,
-                    int its, int ite, int jts, int jte, int kts, int kte, tempo_diags_t* diags) {
+                    const float* qc_bl, const float* qcfrac_bl, float* qcfrac, float* qifrac,
+                    const float* thten_bl, const float* qvten_bl, const float* qcten_bl,
+                    const float* qiten_bl, const float* thten_lwrad, const float* thten_swrad,
+                    const int* land_input, int ids, int ide, int jds, int jde, int kds, int kde,
+                    int ims, int ime, int jms, int jme, int kms, int kme, int its, int ite,
+                    int jts, int jte, int kts, int kte, tempo_diags_t* diags) {
+  (void)qcfrac; (void)qifrac; (void)thten_bl; (void)qvten_bl; (void)qcten_bl; (void)qiten_bl;
+  (void)thten_lwrad; (void)thten_swrad; (void)ids; (void)ide; (void)jds; (void)jde; (void)kds; (void)kde;
   RunArrays<float> H{t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni, nr, nc, nwfa, nifa, ng, qb, land_input};
+  H.qc_bl = qc_bl;
+  H.qcfrac_bl = qcfrac_bl;
   return run_host(c, cfg, (double)dt, itimestep, H, Bounds{ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte}, diags);
 }
 

@@ -70,6 +70,22 @@ struct DerivOps {
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
 cudaError_t noalloc_scratch(int device, void** ptr);
 
+// tempo_validate.cu: the input scan of tempo_set_validation.  Field f of the tile is
+// bad where it is not finite or, with positive[f], not > 0; the scan keeps the least
+// (tile point q = i + ti * (k + nz * j)) * kValidateFields + f over all bad values
+// in *first (which the caller sets to ~0 first).
+constexpr int kValidateFields = 20;
+template <class S>
+struct ValidateFields {
+  const S* p[kValidateFields];
+  int positive[kValidateFields];
+  int nf;
+  long NI, NK;
+  int i0, k0, j0, ti, tj, nz;
+};
+template <class S>
+cudaError_t launch_validate(const ValidateFields<S>& v, unsigned long long* first, cudaStream_t s);
+
 // tempo_melt.cu: melting-layer reflectivity pass after phase C (F_MELT), FP64
 template <class S>
 cudaError_t launch_melt_refl(const StepArgs<S>& a, const TempoConsts<double>& c, const RadarConsts& rc,

@@ -126,8 +126,17 @@ def oracle_step_fn():
     return step
 
 
+def reference_root(argv) -> Path:
+    """The reference checkout: the first argument, else $TEMPO_REFERENCE."""
+    import os
+    root = argv[1] if len(argv) > 1 else os.environ.get("TEMPO_REFERENCE")
+    if not root:
+        raise SystemExit(f"usage: {argv[0]} <TEMPO reference checkout> (or set TEMPO_REFERENCE)")
+    return Path(root)
+
+
 def main(argv):
-    ref = Path(argv[1]) if len(argv) > 1 else Path("/root/reference")
+    ref = reference_root(argv)
     col = read_column(ref / "test" / "data" / "mpas_59lev_test.txt")
     np.savez_compressed(HERE / "mpas_59lev_column.npz", **col)
     step = oracle_step_fn()

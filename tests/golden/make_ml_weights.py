@@ -29,8 +29,11 @@ def parse(text: str) -> dict:
 
 
 def main():
-    src = Path(sys.argv[1] if len(sys.argv) > 1 else
-               "/root/reference/src/module_mp_tempo_ml.F90")
+    import os
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TEMPO_REFERENCE")
+    if not root:
+        raise SystemExit(f"usage: {sys.argv[0]} <TEMPO reference checkout> (or set TEMPO_REFERENCE)")
+    src = Path(root) / "src" / "module_mp_tempo_ml.F90"
     data = parse(src.read_text())
     out = Path(__file__).resolve().parent / "ml_cloud_number.npz"
     np.savez(out, **data)

@@ -59,3 +59,39 @@ def test_noalloc_rejects_tiles_beyond_its_scratch(tg, ctx_nohail):
     torch.cuda.synchronize()
     for k in f:   # rejected before any work: the state is untouched
         assert torch.equal(f[k], before[k]), k
+
+
+def test_noalloc_allocates_nothing_and_records_no_kernel_times(tg, ctx_nohail):
+    """After a first call (which looks up the fixed array), further steps leave the
+    device's free memory unchanged; and since the call records no timing events, the
+    kernel-times query refuses to report an earlier run's times as this step's."""
+    torch = pytest.importorskip("torch")
+    from tempo_gb300 import workloads as W
+    ctx = ctx_nohail
+    wl = W.config1(seed=7, ni=32, nj=20, steps=4, dt=30.0)       # 640 columns
+    f = {k: torch.tensor(v.astype(np.float32), device="cuda") for k, v in wl.fields.items()}
+    nj, nk, ni = f["p"].shape
+    d = _diags(torch, nj, nk, ni, tg)
+    ctx.set_precision(tg.PREC_MIXED)
+    try:
+        ctx.run_device_noalloc(f, wl.dt, 1, diags=d)
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        for it in (2, 3, 4):
+            ctx.run_device_noalloc(f, wl.dt, it, diags=d)
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0, (free0, free1)
+        ctx.set_kernel_timing(True)
+        try:
+            g = {k: v.clone() for k, v in f.items()}
+            ctx.run_device(g, wl.dt, 5, diags=d)
+            assert ctx.kernel_times()["points"] > 0
+            ctx.run_device_noalloc(f, wl.dt, 5, diags=d)
+            with pytest.raises(tg.TempoError) as e:
+                ctx.kernel_times()
+            assert e.value.code == -6
+        finally:
+            ctx.set_kernel_timing(False)
+    finally:
+        ctx.set_precision(tg.PREC_FP64)
