@@ -237,6 +237,30 @@ int tempo_run_dev_f32_noalloc_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs
                                 int jme, int kms, int kme, int its, int ite, int jts, int jte,
                                 int kts, int kte, tempo_diags_t *tempo_diags, void *stream);
 
+/* One domain of a multi-domain batch: its time step, step count, device arrays (floats)
+ * and tile bounds, with the meaning they have in tempo_run_dev_f32_c. */
+typedef struct {
+  float dt;
+  int itimestep;
+  tempo_state_t state;   /* device arrays; NULL = absent, as in tempo_run */
+  tempo_diags_t diags;   /* device arrays, tile-shaped; NULL = not requested */
+  int ims, ime, jms, jme, kms, kme, its, ite, jts, jte, kts, kte;
+} tempo_domain_t;
+
+/* No reference counterpart (a host with several domains calls tempo_run once per
+ * domain).  The mixed step (TEMPO_PREC_MIXED, FP32 device arrays) of `ndomains`
+ * independent domains, each with its own levels, dt, arrays and step count, as ONE
+ * sequence of launches on `stream`: every kernel of the step runs over the active work of
+ * all domains at once (the points kernel drawing (domain, point) items from one work
+ * queue), so small domains do not leave the GPU idle.  Each domain's results equal those
+ * of its own tempo_run_dev_f32_c call.  1 <= ndomains <= 256; the semi-Lagrangian,
+ * melting-layer and ML cloud-number paths are not supported (TEMPO_ERR_UNSUPPORTED).
+ * Uses the context's scratch (grown with cudaMalloc on demand), the sedimentation
+ * variant and point order of the context; returns after enqueueing.  The calling
+ * thread's current device must be the context's. */
+int tempo_run_batch_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, int ndomains,
+                              const tempo_domain_t *domains, void *stream);
+
 /* tempo_aerosol_surface_emissions (src/module_mp_tempo_driver.F90:516-529) on device
  * arrays: nwfa(i,kts,j) += nwfa2d(i,j)*dt over the memory range. */
 int tempo_aerosol_surface_emissions_dev_c(tempo_ctx_t *ctx, double dt, double *nwfa,

@@ -89,6 +89,7 @@ def load() -> ctypes.CDLL:
         lib.oracle_ccn_ptr.argtypes = [ctypes.POINTER(ctypes.c_long)]
         lib.oracle_ccn_ptr.restype = ctypes.POINTER(ctypes.c_float)
         lib.oracle_set_tie_sink.argtypes = [_IP]
+        lib.oracle_set_trace.argtypes = [_IP]
         lib.oracle_set_ml.argtypes = [_DP] * 6
         lib.oracle_param.argtypes = [ctypes.c_char_p, ctypes.c_int]
         lib.oracle_param.restype = ctypes.c_double
@@ -177,7 +178,8 @@ def _dp(a):
 
 
 def run(cfg: OCfg, dt: float, itimestep: int, fields: dict, diags: dict | None = None,
-        bounds=None, nthreads: int = 0, ties: np.ndarray | None = None) -> int:
+        bounds=None, nthreads: int = 0, ties: np.ndarray | None = None,
+        trace: np.ndarray | None = None) -> int:
     """tempo_run over 3-D fields shaped (nj, nk, ni) (Fortran (i,k,j), i fastest).
 
     ``fields`` maps argument names (t, th, pii, p, w, dz, qv, qc, qr, qi, qs, qg, ni,
@@ -186,7 +188,9 @@ def run(cfg: OCfg, dt: float, itimestep: int, fields: dict, diags: dict | None =
     preallocated float64 arrays (2-D (nj, ni), 3-D (nj, nk, ni)).  ``ties``: optional
     int32 array of the 2-D tile shape that receives, per column, 1 if the step passed
     an index computation within one rounding of its discontinuity (see
-    ``oracle_set_tie_sink``).
+    ``oracle_set_tie_sink``).  ``trace``: optional zeroed int32 array of
+    TRACE_POINT * ncol * nz + TRACE_COLUMN * ncol entries that receives every table index
+    and branch decision of the step (``trace_size``, ``oracle_set_trace``).
     """
     lib = load()
     ref = fields.get("p")
@@ -210,13 +214,28 @@ def run(cfg: OCfg, dt: float, itimestep: int, fields: dict, diags: dict | None =
     if ties is not None:
         assert ties.dtype == np.int32 and ties.flags.c_contiguous
         lib.oracle_set_tie_sink(ties.ctypes.data_as(_IP))
+    if trace is not None:
+        ncol = (bounds[13] - bounds[12] + 1) * (bounds[15] - bounds[14] + 1)
+        assert trace.dtype == np.int32 and trace.flags.c_contiguous
+        assert trace.size == trace_size(ncol, bounds[17] - bounds[16] + 1)
+        lib.oracle_set_trace(trace.ctypes.data_as(_IP))
     try:
         rc = lib.oracle_run(ctypes.byref(cfg), float(dt), int(itimestep),
                             *[_dp(a) for a in args], land_p, b, ctypes.byref(d), int(nthreads))
     finally:
         if ties is not None:
             lib.oracle_set_tie_sink(None)
+        if trace is not None:
+            lib.oracle_set_trace(None)
     return rc
+
+
+# decision trace layout (oracle_main.c TRP / TRC, the GPU library's TraceSlot)
+TRACE_POINT, TRACE_COLUMN = 16, 10
+
+
+def trace_size(ncol: int, nz: int) -> int:
+    return ncol * nz * TRACE_POINT + ncol * TRACE_COLUMN
 
 
 def last_stats() -> list[int]:

@@ -32,6 +32,28 @@ static inline int nint_tie(double x) {
   if (fabs(f - 0.5) <= 1e-12 * fmax2(1.0, fabs(x))) t_tie |= t_tie_bit;
   return nint(x);
 }
+/* Decision trace (checker-only instrumentation, no effect on results): every table index
+ * and branch decision of a step, per (tile column, level) point TRP ints and per column
+ * TRC ints, in the layout the GPU library's test build records (TraceSlot and
+ * TraceCheckBit in tempo_gb300/csrc/tempo_types.h), so a test compares them exactly. */
+enum { TR_CHECK = 0, TR_RW = 5, TR_RS = 6, TR_RG = 7, TR_FZR = 8, TR_FZC = 9, TR_ICE = 10,
+       TR_RIME = 11, TR_EVAP = 12, TR_LIMIT = 13, TRP = 16, TRC = 10 };
+enum { TB_QC = 1, TB_QC_HIT = 2, TB_QR = 4, TB_QR_HIT = 8, TB_QI = 16, TB_QI_HIT = 32,
+       TB_QS = 64, TB_QG = 128, TB_QG_HIT = 256 };
+static int *g_trace;                 /* [ncol * nz * TRP] points, then [ncol * TRC] columns */
+static _Thread_local int *t_trace;   /* the current column's point records (NULL = off) */
+static _Thread_local int *t_trace_col;
+static _Thread_local int t_tpass;    /* pass of the check routines */
+void oracle_set_trace(int *buf) { g_trace = buf; }
+#define TRACE(k, slot, bits)                                       \
+  do {                                                             \
+    if (t_trace) t_trace[(long)(k) * TRP + (slot)] |= (int)(bits); \
+  } while (0)
+#define TRACE_COL(j, v)                    \
+  do {                                     \
+    if (t_trace_col) t_trace_col[j] = (v); \
+  } while (0)
+
 static inline int int_tie(double y, int current_max) {
   if ((int)y + 1 >= current_max && fabs(y - nearbyint(y)) <= 1e-12 * fmax2(1.0, fabs(y)))
     t_tie |= 1;
@@ -229,6 +251,7 @@ static void cloud_check_and_update(int nz, const double *rho, int *l_qc, double 
       lamc = pow(nc[k] * am_r * CCG(2, nu_c) * OCG1(nu_c) / rc[k], obmr);
       ilamc[k] = 1.0 / lamc;
       mvd_c[k] = fmax2(fmin2((3.0 + nu_c + 0.672) * ilamc[k], d0r), d0c);
+      TRACE(k, TR_CHECK + t_tpass, TB_QC | (hit_limit ? TB_QC_HIT : 0) | (nu_c << 16));
     } else {
       l_qc[k] = 0;
       rc[k] = r1;
@@ -279,6 +302,7 @@ static void rain_check_and_update(int nz, const double *rho, int *l_qr, double *
       if (hit_limit) nrten[k] = (nr[k] / rho[k] - nr1d[k]) * odt;
       nr1d[k] = CRG(2) * org3 * qr1d[k] * pow(lamr, bm_r) / am_r;
       ilamr[k] = 1.0 / lamr;
+      TRACE(k, TR_CHECK + t_tpass, TB_QR | (hit_limit ? TB_QR_HIT : 0));
     } else {
       l_qr[k] = 0;
       rr[k] = r1;
@@ -325,6 +349,7 @@ static void ice_check_and_update(int nz, const double *rho, int *l_qi, double *q
       ni1d[k] = fmax2(r2 / rho[k], fmin2(CIG(1) * oig2 * qi1d[k] / am_i * pow(lami, bm_i),
                                          max_ni / rho[k]));
       ilami[k] = 1.0 / lami;
+      TRACE(k, TR_CHECK + t_tpass, TB_QI | (hit_limit ? TB_QI_HIT : 0));
     } else {
       l_qi[k] = 0;
       ri[k] = r1;
@@ -346,6 +371,7 @@ static void snow_check_and_update(int nz, const double *rho, int *l_qs, double *
       l_qs[k] = 1;
       rs[k] = (qs1d[k] + qsten[k] * dt) * rho[k];
       qs1d[k] = qs1d[k] + qsten[k] * dt;
+      TRACE(k, TR_CHECK + t_tpass, TB_QS);
     } else {
       l_qs[k] = 0;
       rs[k] = r1;
@@ -409,6 +435,7 @@ static void graupel_check_and_update(int nz, const double *rho, int *l_qg, doubl
       }
       ilamg[k] = 1.0 / lamg;
       mvd_g[k] = (3.0 + mu_g + 0.672) * ilamg[k];
+      TRACE(k, TR_CHECK + t_tpass, TB_QG | (hit_limit ? TB_QG_HIT : 0) | (idx[k] << 12));
     } else {
       l_qg[k] = 0;
       rg[k] = r1;
@@ -489,6 +516,7 @@ static void check_over_depletion(ws_t *w, double odt) {
     sump = TD(PRI_INU) + TD(PRI_IDE) + TD(PRS_IDE) + TD(PRS_SDE) + TD(PRG_GDE) + TD(PRI_IHA);
     rate_max = (w->qv[k] - w->qvsi[k]) * w->rho[k] * odt * 0.999;
     if ((sump > eps && sump > rate_max) || (sump < -eps && sump < rate_max)) {
+      TRACE(k, TR_LIMIT, 1 << 0);
       ratio = rate_max / sump;
       TD(PRI_INU) = TD(PRI_INU) * ratio;
       TD(PRI_IDE) = TD(PRI_IDE) * ratio;
@@ -502,6 +530,7 @@ static void check_over_depletion(ws_t *w, double odt) {
     rate_max = -w->rc[k] * odt;
     if (w->l_qc[k]) {
       if (sump < rate_max) {
+        TRACE(k, TR_LIMIT, 1 << 1);
         ratio = rate_max / sump;
         TD(PRR_WAU) = TD(PRR_WAU) * ratio;
         TD(PRI_WFZ) = TD(PRI_WFZ) * ratio;
@@ -515,6 +544,7 @@ static void check_over_depletion(ws_t *w, double odt) {
     rate_max = -w->ri[k] * odt;
     if (w->l_qi[k]) {
       if (sump < rate_max) {
+        TRACE(k, TR_LIMIT, 1 << 2);
         ratio = rate_max / sump;
         TD(PRI_IDE) = TD(PRI_IDE) * ratio;
         TD(PRS_IAU) = TD(PRS_IAU) * ratio;
@@ -526,6 +556,7 @@ static void check_over_depletion(ws_t *w, double odt) {
     rate_max = -w->rr[k] * odt;
     if (w->l_qr[k]) {
       if (sump < rate_max) {
+        TRACE(k, TR_LIMIT, 1 << 3);
         ratio = rate_max / sump;
         TD(PRG_RFZ) = TD(PRG_RFZ) * ratio;
         TD(PBG_RFZ) = TD(PBG_RFZ) * ratio;
@@ -539,6 +570,7 @@ static void check_over_depletion(ws_t *w, double odt) {
     rate_max = -w->rs[k] * odt;
     if (w->l_qs[k]) {
       if (sump < rate_max) {
+        TRACE(k, TR_LIMIT, 1 << 4);
         ratio = rate_max / sump;
         TD(PRS_SDE) = TD(PRS_SDE) * ratio;
         TD(PRS_IHM) = TD(PRS_IHM) * ratio;
@@ -550,6 +582,7 @@ static void check_over_depletion(ws_t *w, double odt) {
     rate_max = -w->rg[k] * odt;
     if (w->l_qg[k]) {
       if (sump < rate_max) {
+        TRACE(k, TR_LIMIT, 1 << 5);
         ratio = rate_max / sump;
         TD(PRG_GDE) = TD(PRG_GDE) * ratio;
         TD(PRG_IHM) = TD(PRG_IHM) * ratio;
@@ -1035,12 +1068,14 @@ static void warm_rain(ws_t *w, double odt) {
   for (int k = 0; k < nz; k++) {
     if (w->l_qr[k]) {
       if (w->mvd_r[k] > d0r) {
+        TRACE(k, TR_RW, 1 << 16);
         double ef_rr = fmax2(-0.1, 1.0 - exp(2300.0 * (w->mvd_r[k] - 1950.0e-6)));
         TD(PNR_RCR) = ef_rr * 2.0 * w->nr[k] * w->rr[k];
       }
     }
     if (w->l_qc[k]) {
       if (w->rc[k] > 0.01e-3) {
+        TRACE(k, TR_RW, 1 << 17);
         int nu_c = o_get_nuc(w->nc[k]);
         double lamc = 1.0 / w->ilamc[k];
         double xdc = fmax2(d0c * 1.e6, (pow(w->rc[k] / (am_r * w->nc[k]), obmr)) * 1.e6);
@@ -1063,6 +1098,7 @@ static void warm_rain(ws_t *w, double odt) {
         double lamr = (3.0 + mu_r + 0.672) / w->mvd_r[k];
         int idx = 1 + (int)(nbr * log(w->mvd_r[k] / dr[0]) / log(dr[nbr - 1] / dr[0]));
         idx = imin(idx, nbr);
+        TRACE(k, TR_RW, idx | ((int)(w->mvd_c[k] * 1.e6) << 8) | (1 << 18));
         double ef_rw = T_EFRW(idx, (int)(w->mvd_c[k] * 1.e6));
         double n0_r = w->nr[k] * org2 * pow(lamr, CRE(2));
         TD(PRR_RCW) = w->rhof[k] * t1_qr_qc * ef_rw * w->rc[k] * n0_r * pow(lamr + fv_r, -CRE(9));
@@ -1086,6 +1122,7 @@ static void riming(ws_t *w, double odt) {
       if ((w->mvd_c[k] > d0c) && (xds > d0s)) {
         int idxs = 1 + (int)(nbs * log(xds / ds[0]) / log(ds[nbs - 1] / ds[0]));
         idxs = imin(idxs, nbs);
+        TRACE(k, TR_RIME, idxs | ((int)(w->mvd_c[k] * 1.e6) << 8) | (1 << 16));
         double ef_sw = T_EFSW(idxs, (int)(w->mvd_c[k] * 1.e6));
         TD(PRS_SCW) = w->rhof[k] * t1_qs_qc * ef_sw * w->rc[k] * w->smoe[k];
         TD(PRS_SCW) = fmin2(w->rc[k] * odt, TD(PRS_SCW));
@@ -1170,6 +1207,7 @@ static void rain_snow_rain_graupel(ws_t *w, double odt) {
         get_temperature_table_index(w->temp[k], &idx_t);
         get_rain_table_index(w->rr[k], w->ilamr[k], &idx_r, &idx_r1);
         get_snow_table_index(w->rs[k], &idx_s);
+        TRACE(k, TR_RS, idx_s | (idx_t << 6) | (idx_r1 << 12) | (idx_r << 18) | (1 << 24));
 #define QSV(a) QS4(a, idx_s, idx_t, idx_r1, idx_r)
         if (w->temp[k] < t0) {
           TD(PRR_RCS) = -(QSV(tmr_racs2) + QSV(tcr_sacr2) + QSV(tmr_racs1) + QSV(tcr_sacr1));
@@ -1196,6 +1234,7 @@ static void rain_snow_rain_graupel(ws_t *w, double odt) {
         get_temperature_table_index(w->temp[k], &idx_t);
         get_rain_table_index(w->rr[k], w->ilamr[k], &idx_r, &idx_r1);
         get_graupel_table_index(w->rg[k], w->ilamg[k], ig, &idx_g, &idx_g1);
+        TRACE(k, TR_RG, idx_g1 | (idx_g << 6) | (idx_r1 << 12) | (idx_r << 18) | (1 << 24));
 #define QGV(a) QG5(a, idx_g1, idx_g, ig, idx_r1, idx_r)
         if (w->temp[k] < t0) {
           TD(PRG_RCG) = QGV(tmr_racg) + QGV(tcr_gacr);
@@ -1246,6 +1285,7 @@ static void ice_nucleation(ws_t *w, const double *w1d, const double *nwfa1d, con
       get_in_table_index(xni, &idx_in);
       if (w->rr[k] > r_r[0]) {
         get_rain_table_index(w->rr[k], w->ilamr[k], &idx_r, &idx_r1);
+        TRACE(k, TR_FZR, idx_r | (idx_r1 << 6) | (idx_tc << 12) | (idx_in << 18) | (1 << 24));
         TD(PRG_RFZ) = QRFZ(tpg_qrfz, idx_r, idx_r1, idx_tc, idx_in) * odt;
         TD(PRI_RFZ) = QRFZ(tpi_qrfz, idx_r, idx_r1, idx_tc, idx_in) * odt;
         TD(PNI_RFZ) = QRFZ(tni_qrfz, idx_r, idx_r1, idx_tc, idx_in) * odt;
@@ -1254,17 +1294,20 @@ static void ice_nucleation(ws_t *w, const double *w1d, const double *nwfa1d, con
         TD(PNR_RFZ) = fmin2(w->nr[k] * odt, TD(PNR_RFZ));
         TD(PNG_RFZ) = TD(PNR_RFZ) * fmax2(fmin2((pow(10.0, -0.1 * w1d[k]) + 0.1), 1.0), 0.1);
       } else if (w->rr[k] > r1 && w->temp[k] < hgfrz) {
+        TRACE(k, TR_FZR, 1 << 25);
         TD(PRI_RFZ) = w->rr[k] * odt;
         TD(PNI_RFZ) = w->nr[k] * odt;
       }
       TD(PBG_RFZ) = meters3_to_liters * TD(PRG_RFZ) / rho_i;
       if (w->rc[k] > r_c[0]) {
         get_cloud_table_index(w->rc[k], w->nc[k], &idx_c, &idx_n);
+        TRACE(k, TR_FZC, idx_c | (idx_n << 8) | (1 << 16));
         TD(PRI_WFZ) = QCFZ(tpi_qcfz, idx_c, idx_n, idx_tc, idx_in) * odt;
         TD(PRI_WFZ) = fmin2(w->rc[k] * odt, TD(PRI_WFZ));
         TD(PNI_WFZ) = QCFZ(tni_qcfz, idx_c, idx_n, idx_tc, idx_in) * odt;
         TD(PNI_WFZ) = fmin3(w->nc[k] * odt, TD(PRI_WFZ) / (2.0 * xm0i), TD(PNI_WFZ));
       } else if (w->rc[k] > r1 && w->temp[k] < hgfrz) {
+        TRACE(k, TR_FZC, 1 << 17);
         TD(PRI_WFZ) = w->rc[k] * odt;
         TD(PNI_WFZ) = w->nc[k] * odt;
       }
@@ -1324,6 +1367,7 @@ static void ice_processes(ws_t *w, const double *w1d, double odt) {
       if (w->l_qi[k]) {
         int idx_i, idx_i1;
         get_ice_table_index(w->ri[k], w->ni[k], &idx_i, &idx_i1);
+        TRACE(k, TR_ICE, idx_i | (idx_i1 << 8) | (1 << 16));
         double xdi = fmax2(d0i, (bm_i + mu_i + 1.) * w->ilami[k]);
         double xmi = am_i * pow(xdi, bm_i);
         double oxmi = 1.0 / xmi;
@@ -1565,6 +1609,7 @@ static void cloud_condensation(ws_t *w, const double *w1d, const double *nwfa1d,
         int idx_d = imax(1, imin((int)(1.e6 * dc_star), nbc));
         int idx_c, idx_n;
         get_cloud_table_index(w->rc[k], w->nc[k], &idx_c, &idx_n);
+        TRACE(k, TR_EVAP, idx_d | (idx_c << 8) | (idx_n << 16) | (1 << 24));
         TD(PRW_VCD) = fmax2(-w->rc[k] * 0.99 * orho * odt, TD(PRW_VCD));
         TD(PNC_WCD) = fmax2(-w->nc[k] * 0.99 * orho * odt,
                             -TNC_WEV(idx_d, idx_c, idx_n) * orho * odt);
@@ -2031,6 +2076,7 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
     init_aerosols(nz, dz1d, w->nifa, w->hgt, nain0, nain1);
   }
   aerosol_check_and_update(nz, w->rho, nwfa1d, nifa1d, w->nwfa, w->nifa, w->nwfaten, w->nifaten, dt);
+  t_tpass = 0;
   rain_check_and_update(nz, w->rho, w->l_qr, qr1d, nr1d, w->rr, w->nr, w->qrten, w->nrten,
                         w->ilamr, w->mvd_r, dt, odt);
   ice_check_and_update(nz, w->rho, w->l_qi, qi1d, ni1d, w->ri, w->ni, w->qiten, w->niten, w->ilami,
@@ -2112,6 +2158,7 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
     memcpy(w->xncx, nc1d, sizeof(double) * nz);
     xncx = w->xncx;
   }
+  t_tpass = 1;
   cloud_check_and_update(nz, w->rho, w->l_qc, w->xrx, xncx, have_ncsave ? w->ncsave : NULL, w->rc,
                          w->nc, w->qcten, w->ncten, w->ilamc, w->mvd_c, dt, odt);
   memcpy(w->xrx, qr1d, sizeof(double) * nz);
@@ -2152,6 +2199,7 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
     }
     memcpy(w->xrx, qc1d, sizeof(double) * nz);
     if (nc1d) memcpy(w->xncx, nc1d, sizeof(double) * nz);
+    t_tpass = 2;
     cloud_check_and_update(nz, w->rho, w->l_qc, w->xrx, xncx, have_ncsave ? w->ncsave : NULL,
                            w->rc, w->nc, w->qcten, w->ncten, w->ilamc, w->mvd_c, dt, odt);
     for (k = 0; k < nz; k++) {
@@ -2172,6 +2220,7 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
     }
     memcpy(w->xrx, qr1d, sizeof(double) * nz);
     memcpy(w->xnx, nr1d, sizeof(double) * nz);
+    t_tpass = 3;
     rain_check_and_update(nz, w->rho, w->l_qr, w->xrx, w->xnx, w->rr, w->nr, w->qrten, w->nrten,
                           w->ilamr, w->mvd_r, dt, odt);
     for (k = 0; k < nz; k++) {
@@ -2188,6 +2237,8 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
   for (k = 0; k < nz; k++) any |= w->l_qr[k];
   if (any) {
     rain_fallspeed(nz, w->rhof, w->rr, w->ilamr, dz1d, w->vtrr, w->vtnr, &steps, &ktop, dt);
+    TRACE_COL(0, steps);
+    TRACE_COL(4, ktop);
     if (cfg->semi_sedi_flag) { /* :599-613 */
       steps = imax((int)(steps / semi_sedi_factor) + 1, 1);
       md->substeps[0] = steps;
@@ -2218,6 +2269,8 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
   if (any) {
     graupel_fallspeed(nz, w->rhof, w->rho, w->visco, w->rg, w->rb, qb1d != NULL, w->idx_bg,
                       w->ilamg, dz1d, w->vtrg, w->vtng, &steps, &ktop, dt);
+    TRACE_COL(1, steps);
+    TRACE_COL(5, ktop);
     if (cfg->semi_sedi_flag) { /* :640-671 */
       steps = imax((int)(steps / semi_sedi_factor) + 1, 1);
       md->substeps[1] = steps;
@@ -2259,6 +2312,8 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
   if (any) {
     snow_fallspeed(nz, w->rhof, w->rs, tw + (long)PRR_SML * nz, w->smob, w->smoc, w->rr, w->vtrr,
                    dz1d, w->vtrs, w->vtboost, &steps, &ktop, dt);
+    TRACE_COL(2, steps);
+    TRACE_COL(6, ktop);
     md->substeps[2] = steps;
     for (int n = 1; n <= steps; n++)
       sedimentation(nz, w->rs, w->vtrs, dz1d, w->rho, w->qsten, r1, steps, ktop,
@@ -2268,6 +2323,8 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
   for (k = 0; k < nz; k++) any |= w->l_qi[k];
   if (any) {
     ice_fallspeed(nz, w->rhof, w->ri, w->ilami, dz1d, w->vtri, w->vtni, &steps, &ktop, dt);
+    TRACE_COL(3, steps);
+    TRACE_COL(7, ktop);
     md->substeps[3] = steps;
     sedimentation(nz, w->ri, w->vtri, dz1d, w->rho, w->qiten, r1, steps, ktop,
                   &md->ice_liquid_equiv_precip, dt, w->sed_r);
@@ -2277,6 +2334,7 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
   for (k = 0; k < nz; k++) any |= w->l_qc[k];
   if (any) {
     cloud_fallspeed(nz, w->rhof, w1d, w->rc, w->nc, w->ilamc, dz1d, w->vtrc, w->vtnc, &ktop);
+    TRACE_COL(8, ktop);
     md->substeps[4] = 1;
     sedimentation(nz, w->rc, w->vtrc, dz1d, w->rho, w->qcten, r1, 1, ktop, &md->cloud_precip, dt,
                   w->sed_r);
@@ -2293,6 +2351,7 @@ static void tempo_main_col(const ocfg_t *cfg, int is_first_step, double *qv1d, d
     if (nwfa1d) nwfa1d[k] = fmax2(nwfa_default, fmin2(aero_max, (nwfa1d[k] + w->nwfaten[k] * dt)));
     if (nifa1d) nifa1d[k] = fmax2(nifa_default, fmin2(aero_max, (nifa1d[k] + w->nifaten[k] * dt)));
   }
+  t_tpass = 4;
   cloud_check_and_update(nz, w->rho, w->l_qc, qc1d, nc1d, have_ncsave ? w->ncsave : NULL, w->rc,
                          w->nc, w->qcten, w->ncten, w->ilamc, w->mvd_c, dt, odt);
   rain_check_and_update(nz, w->rho, w->l_qr, qr1d, nr1d, w->rr, w->nr, w->qrten, w->nrten, w->ilamr,
@@ -2461,6 +2520,11 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep, double *t, double *t
       mdiag_t md;
       t_tie = 0;
       t_tie_bit = 1;
+      {
+        const long ct = (long)(i - its) + (long)(j - jts) * (ite - its + 1);
+        t_trace = g_trace ? g_trace + ct * nz * TRP : NULL;
+        t_trace_col = g_trace ? g_trace + ncols * nz * TRP + ct * TRC : NULL;
+      }
       tempo_main_col(cfg, is_first_step, qv1d, qc1d, qi1d, qr1d, qs1d, qg1d, qb ? qb1d : NULL,
                      ni1d, nr1d, nc ? nc1d : NULL, ng ? ng1d : NULL, nwfa ? nwfa1d : NULL,
                      nifa ? nifa1d : NULL, t1d, p1d, w1d, dz1d, land_input ? &land1d : NULL, dt, w,

@@ -93,6 +93,13 @@ class TempoDiags(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in DIAG2 + DIAG3]
 
 
+class TempoDomain(ctypes.Structure):
+    """tempo_domain_t: one domain of a multi-domain batch (include/tempo_gb300.h)."""
+    _fields_ = [("dt", ctypes.c_float), ("itimestep", ctypes.c_int), ("state", TempoState),
+                ("diags", TempoDiags)] + [(n, ctypes.c_int) for n in (
+                    "ims", "ime", "jms", "jme", "kms", "kme", "its", "ite", "jts", "jte", "kts", "kte")]
+
+
 _lib = None
 _DP = ctypes.POINTER(ctypes.c_double)
 _FP = ctypes.POINTER(ctypes.c_float)
@@ -158,6 +165,8 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
                                          ctypes.POINTER(TempoDiags)] + [i] * 12 + [_VP])
     lib.tempo_kernel_times_c.argtypes = [_VP, ctypes.POINTER(ctypes.c_float)]
     lib.tempo_check_table_c.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+    lib.tempo_run_batch_dev_f32_c.argtypes = [_VP, ctypes.POINTER(TempoCfgs), i,
+                                              ctypes.POINTER(TempoDomain), _VP]
     lib.tempo_set_validation.argtypes = [_VP, i]
     _lib = lib
     return lib
@@ -317,6 +326,34 @@ class TempoContext:
             self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs,
             land.data_ptr() if land is not None else None, *b[6:], ctypes.byref(d),
             ctypes.c_void_p(s.cuda_stream)))
+
+    def run_batch_device(self, domains: list, stream=None, cfgs: Optional[TempoCfgs] = None):
+        """tempo_run_batch_dev_f32_c: the mixed step of several domains (float32 CUDA
+        tensors) as one launch sequence.  ``domains``: dicts with ``fields`` (as for
+        run_device), ``dt``, ``itimestep`` and optional ``diags``."""
+        import torch
+        lib = load_library()
+        cfg = cfgs if cfgs is not None else self.cfgs
+        arr = (TempoDomain * len(domains))()
+        for d, dom in zip(arr, domains):
+            f = dom["fields"]
+            if f["p"].dtype != torch.float32:
+                raise TempoError(-1, "the batch step works on float32 device arrays")
+            nj, nk, ni = f["p"].shape
+            d.dt = float(dom["dt"])
+            d.itimestep = int(dom["itimestep"])
+            d.state = _state_of(f)
+            for n in DIAG2 + DIAG3:
+                a = (dom.get("diags") or {}).get(n)
+                if a is not None:
+                    setattr(d.diags, n, a.data_ptr())
+            for n, v in zip(("ims", "ime", "jms", "jme", "kms", "kme", "its", "ite", "jts", "jte",
+                             "kts", "kte"), [1, ni, 1, nj, 1, nk] * 2):
+                setattr(d, n, v)
+        dev = domains[0]["fields"]["p"].device
+        s = stream if stream is not None else torch.cuda.current_stream(dev)
+        _check(lib.tempo_run_batch_dev_f32_c(self._h, ctypes.byref(cfg), len(domains), arr,
+                                             ctypes.c_void_p(s.cuda_stream)))
 
     def autotune_device(self, fields: dict, dt: float, itimestep: int, diags: Optional[dict] = None,
                         bounds=None, stream=None, cfgs: Optional[TempoCfgs] = None,

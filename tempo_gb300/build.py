@@ -18,6 +18,10 @@ REPO = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libtempo_gb300.so"
+# test-only variant that records every table index and branch decision of a step
+# (TEMPO_TRACE; tests/test_decision_trace.py); never loaded by the product
+TRACE_BUILD = PKG / "_build_trace"
+TRACE_LIB = PKG / "libtempo_gb300_trace.so"
 INCLUDE = REPO / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -35,6 +39,7 @@ UNITS = [
     ("tempo_noalloc.cu", [], "tempo_noalloc"),
     ("tempo_melt.cu", ["-fmad=false"], "tempo_melt"),
     ("tempo_validate.cu", [], "tempo_validate"),
+    ("tempo_batch.cu", [], "tempo_batch"),
 ]
 HOST_UNITS = ["tempo_capi.cpp", "tempo_host_init.cpp"]
 
@@ -55,25 +60,28 @@ def _sources():
     return sorted(CSRC.glob("*")) + sorted(INCLUDE.glob("*.h")) + [Path(__file__)]
 
 
-def up_to_date() -> bool:
-    if not LIB.exists():
+def up_to_date(lib: Path = LIB) -> bool:
+    if not lib.exists():
         return False
-    t = LIB.stat().st_mtime
+    t = lib.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _sources())
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    if not force and up_to_date():
-        return LIB
-    BUILD.mkdir(exist_ok=True)
+def build(force: bool = False, verbose: bool = False, trace: bool = False) -> Path:
+    """Compiles the library (trace=True: the test-only decision-trace variant)."""
+    lib, bdir = (TRACE_LIB, TRACE_BUILD) if trace else (LIB, BUILD)
+    if not force and up_to_date(lib):
+        return lib
+    bdir.mkdir(exist_ok=True)
     nvcc = _nvcc()
+    defs = ["-DTEMPO_TRACE"] if trace else []
     jobs = []
     for src, extra, name in UNITS:
-        obj = BUILD / (name + ".o")
-        jobs.append([nvcc, *NVCC_COMMON, *extra, "-c", str(CSRC / src), "-o", str(obj)])
+        obj = bdir / (name + ".o")
+        jobs.append([nvcc, *NVCC_COMMON, *defs, *extra, "-c", str(CSRC / src), "-o", str(obj)])
     for src in HOST_UNITS:
-        obj = BUILD / (Path(src).stem + ".o")
-        jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall",
+        obj = bdir / (Path(src).stem + ".o")
+        jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", *defs,
                      "-I", str(INCLUDE), "-I", str(CSRC), "-I", _cuda_include(),
                      "-c", str(CSRC / src), "-o", str(obj)])
 
@@ -86,12 +94,12 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(run, jobs))
-    objs = [str(BUILD / (name + ".o")) for _, _, name in UNITS] + \
-           [str(BUILD / (Path(s).stem + ".o")) for s in HOST_UNITS]
-    tmp = LIB.with_suffix(f".so.tmp{os.getpid()}")
+    objs = [str(bdir / (name + ".o")) for _, _, name in UNITS] + \
+           [str(bdir / (Path(s).stem + ".o")) for s in HOST_UNITS]
+    tmp = lib.with_suffix(f".so.tmp{os.getpid()}")
     run([nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart_static"])
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

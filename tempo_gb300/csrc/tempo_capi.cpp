@@ -125,6 +125,9 @@ struct tempo_ctx {
   bool validate = false;     // input scan before each run (tempo_set_validation)
   bool in_host_run = false;  // run_dev called by run_host (inputs scanned on the host)
   unsigned long long* d_first_bad = nullptr;  // verdict of the device input scan
+#ifdef TEMPO_TRACE
+  int* trace = nullptr;  // decision-trace buffer of a test build (tempo_set_trace_c)
+#endif
 };
 
 namespace {
@@ -134,6 +137,7 @@ void free_tables(tempo_ctx* c) {
                  c->t64.tni_iaus, c->t64.tpi_ide, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
   for (double* p : d) cudaFree(p);
   cudaFree(c->t64.tnccn);
+  cudaFree(c->t64.edges);
   float* f[] = {c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
                 c->f_qg,   c->f_qs,   c->f_qrfz,    c->f_qcfz};
   for (float* p : f) cudaFree(p);
@@ -155,7 +159,20 @@ int alloc_tables(tempo_ctx* c) {
   if ((rc = dev_alloc(&t.qrfz, (size_t)QRFZ_COUNT * 4))) return rc;
   if ((rc = dev_alloc(&t.qcfz, (size_t)QCFZ_COUNT * 2))) return rc;
   if ((rc = dev_alloc(&t.tnccn, (size_t)CCN_COUNT))) return rc;
+  if ((rc = dev_alloc(&t.edges, (size_t)kEdgesCount))) return rc;
   return TEMPO_OK;
+}
+
+// the context's tables for the kernels of element type T (FP32 copies for float)
+template <class T> Tables<T> tables_of(const tempo_ctx* c);
+template <> Tables<double> tables_of<double>(const tempo_ctx* c) {
+  return Tables<double>{c->t64.t_efrw, c->t64.t_efsw, c->t64.tnc_wev, c->t64.tps_iaus, c->t64.tni_iaus,
+                        c->t64.tpi_ide, c->t64.tnccn, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz,
+                        c->t64.edges};
+}
+template <> Tables<float> tables_of<float>(const tempo_ctx* c) {
+  return Tables<float>{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
+                       c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz, c->t64.edges};
 }
 
 int make_f32_tables(tempo_ctx* c) {
@@ -703,6 +720,9 @@ int build_args(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, 
   a.nc_single = resolve_nc_value(cfg);
   a.flags = f;
   a.mlnet = (f & (F_MLNC | F_BLRE)) ? c->d_mlnet : nullptr;
+#ifdef TEMPO_TRACE
+  a.trace = c->trace;
+#endif
   // decay rates of the aerosol initial profiles (init_*_friendly_aerosols,
   // aerosols:14-73; h_01 = 0.8 km), host libm as in the reference
   a.niccn3 = -1.0 * std::log(naccn1 / naccn0) / 0.8;
@@ -783,15 +803,13 @@ int run_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, con
     const cudaEvent_t* ev = timed ? c->kev : nullptr;
     if (!mixed) {
       if constexpr (sizeof(S) == sizeof(double)) {
-        Tables<double> T{c->t64.t_efrw, c->t64.t_efsw, c->t64.tnc_wev, c->t64.tps_iaus, c->t64.tni_iaus,
-                         c->t64.tpi_ide, c->t64.tnccn, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
+        const Tables<double> T = tables_of<double>(c);
         e = launch_step_f64(a, T, c->c64, c->i64, st, ev, c->sedim_variant);
         return e == cudaSuccess ? launch_melt_refl(a, c->c64, c->radar, st) : e;
       }
       return cudaErrorInvalidValue;
     }
-    Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
-                    c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
+    const Tables<float> T = tables_of<float>(c);
     if constexpr (sizeof(S) == sizeof(double))
       e = launch_step_mixed_f64(a, T, c->c32, c->idf, st, ev, c->sedim_variant);
     else
@@ -898,9 +916,122 @@ int run_dev_noalloc(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimes
   // every other scratch field is written before it is read
   CUDA_TRY(cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s));
   CUDA_TRY(cudaMemsetAsync(a.nact, 0, 2 * sizeof(unsigned int), s));
-  Tables<float> T{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
-                  c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
+  const Tables<float> T = tables_of<float>(c);
   CUDA_TRY(launch_step_mixed_f32(a, T, c->c32, c->idf, s, nullptr, c->points_variant, c->sedim_variant));
+  return TEMPO_OK;
+}
+
+// The mixed step of a multi-domain batch on FP32 device arrays: each domain's arguments
+// as run_dev builds them, scratch for every domain in the context's scratch, the batch's
+// descriptors after them, one launch sequence (tempo_batch.cu).
+int run_batch(tempo_ctx* c, const tempo_cfgs_t* cfg, int nd, const tempo_domain_t* doms, cudaStream_t s) {
+  if (!doms || nd < 1 || nd > kMaxDomains)
+    return fail(TEMPO_ERR_ARG, "ndomains must be in 1..%d with a domain array (got %d)", kMaxDomains, nd);
+  if (!cfg) return fail(TEMPO_ERR_ARG, "NULL tempo_cfgs");
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  if (c->precision != TEMPO_PREC_MIXED)
+    return fail(TEMPO_ERR_STATE, "the batch step runs the mixed form: tempo_set_precision(TEMPO_PREC_MIXED)");
+  if (int rc = check_current_device(c)) return rc;
+  std::vector<StepArgs<float>> A((size_t)nd);
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  struct Sizes {
+    size_t sd, sr, sc, act, pm, cm, hg;
+  };
+  std::vector<Sizes> Z((size_t)nd);
+  std::vector<long> col_start((size_t)nd + 1, 0);
+  size_t total = 0;
+  long npts_max = 0;
+  for (int d = 0; d < nd; d++) {
+    const tempo_domain_t& D = doms[d];
+    const tempo_state_t& x = D.state;
+    RunArrays<float> R{(float*)x.t, (float*)x.th, (const float*)x.pii, (const float*)x.p,
+                       (const float*)x.w, (const float*)x.dz, (float*)x.qv, (float*)x.qc,
+                       (float*)x.qr, (float*)x.qi, (float*)x.qs, (float*)x.qg, (float*)x.ni,
+                       (float*)x.nr, (float*)x.nc, (float*)x.nwfa, (float*)x.nifa, (float*)x.ng,
+                       (float*)x.qb, x.land_input};
+    const Bounds b{D.ims, D.ime, D.jms, D.jme, D.kms, D.kme, D.its, D.ite, D.jts, D.jte, D.kts, D.kte};
+    if (int rc = build_args(c, cfg, (double)D.dt, D.itimestep, R, b, &D.diags, A[d])) {
+      const std::string why = g_err;
+      return fail(rc, "domain %d: %s", d, why.c_str());
+    }
+    if (A[d].flags & (F_SEMI | F_MELT | F_MLNC | F_BLRE))
+      return fail(TEMPO_ERR_UNSUPPORTED, "domain %d: the semi-Lagrangian, melting-layer and ML "
+                  "cloud-number paths are not part of the batch step (tempo_run_dev_f32_c runs them)", d);
+    const size_t npad = (size_t)A[d].ncol_pad, nzs = (size_t)A[d].nz;
+    Sizes& z = Z[d];
+    z.sd = al((size_t)SD_N * nzs * npad * 8);
+    z.sr = al((size_t)SR_N * nzs * npad * sizeof(float));
+    z.sc = al((size_t)SC_N * npad * 8);
+    z.act = al(npad * sizeof(int));
+    z.pm = al(nzs * npad);
+    z.cm = al(npad);
+    z.hg = al(nzs * npad * sizeof(float));
+    total += z.sd + z.sr + z.sc + z.act + z.pm + z.cm + z.hg;
+    col_start[d + 1] = col_start[d] + A[d].ncol;
+    npts_max += A[d].ncol * A[d].nz;
+  }
+  if (npts_max >= (1L << 32))
+    return fail(TEMPO_ERR_ARG, "a batch holds at most 2^32 - 1 column levels (got %ld)", npts_max);
+  const bool order = c->points_order != 0;
+  const size_t cnt_bytes = al((size_t)nd * 2 * sizeof(unsigned));   // each domain's counters
+  const size_t dom_bytes = al((size_t)nd * sizeof(StepArgs<float>));
+  const size_t cs_bytes = al(((size_t)nd + 1) * sizeof(long));
+  const size_t plan_bytes = al((2 * ((size_t)nd + 1) + 1) * sizeof(unsigned));
+  const size_t ord_bytes = order ? al((size_t)npts_max * sizeof(unsigned)) : 0;
+  total += cnt_bytes + dom_bytes + cs_bytes + plan_bytes + ord_bytes + 256;
+  if (int rc = ensure_scratch(c, total)) return rc;
+  char* sp = (char*)c->scratch;
+  unsigned* counters = (unsigned*)sp;
+  sp += cnt_bytes;
+  for (int d = 0; d < nd; d++) {
+    StepArgs<float>& a = A[d];
+    const Sizes& z = Z[d];
+    a.sd = sp;
+    sp += z.sd;
+    a.sr = sp;
+    sp += z.sr;
+    a.sc = sp;
+    sp += z.sc;
+    a.act = (int*)sp;
+    sp += z.act;
+    a.pmask = (uint8_t*)sp;
+    sp += z.pm;
+    a.cmask = (uint8_t*)sp;
+    sp += z.cm;
+    a.hgt = sp;
+    sp += z.hg;
+    a.nact = counters + 2 * d;
+    a.stats = c->d_stats;
+    a.ord = nullptr;
+  }
+  StepArgs<float>* d_dom = (StepArgs<float>*)sp;
+  sp += dom_bytes;
+  long* d_cs = (long*)sp;
+  sp += cs_bytes;
+  unsigned* plan = (unsigned*)sp;
+  sp += plan_bytes;
+  unsigned* d_ord = order ? (unsigned*)sp : nullptr;
+  BatchArgs<float> B{};
+  B.dom = d_dom;
+  B.col_start = d_cs;
+  B.slot_start = plan;
+  B.pt_start = plan + (nd + 1);
+  B.queue = plan + 2 * (nd + 1);
+  B.ord = d_ord;
+  B.nd = nd;
+  B.ncol = col_start[nd];
+  B.npts_max = npts_max;
+  c->last_cols = B.ncol;
+  c->launches = kStepLaunches + 1 + (order ? kOrderLaunches : 0);
+  const bool timed = c->kernel_timing;
+  c->times_valid = timed;
+  // descriptors from pageable host memory (staged before the call returns), counters zeroed
+  CUDA_TRY(cudaMemcpyAsync(d_dom, A.data(), (size_t)nd * sizeof(StepArgs<float>), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(d_cs, col_start.data(), ((size_t)nd + 1) * sizeof(long), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemsetAsync(counters, 0, (size_t)nd * 2 * sizeof(unsigned), s));
+  CUDA_TRY(cudaMemsetAsync(c->d_stats, 0, 8 * sizeof(unsigned long long), s));
+  CUDA_TRY(launch_batch_mixed_f32(B, tables_of<float>(c), c->c32, c->idf, s, timed ? c->kev : nullptr,
+                                  c->sedim_variant));
   return TEMPO_OK;
 }
 
@@ -1155,6 +1286,12 @@ int tempo_init_c(const int* aerosolaware_flag, const int* hailaware_flag, const 
   make_bins(&c->bins);
   int rc;
   if ((rc = alloc_tables(c))) return bail(rc);
+  {
+    double edges[kEdgesCount];
+    make_index_edges(c->bins, edges);
+    if ((e = cudaMemcpy(c->t64.edges, edges, sizeof edges, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return bail(fail(TEMPO_ERR_CUDA, "index edges: %s", cudaGetErrorString(e)));
+  }
   if ((rc = dev_alloc(&c->d_stats, 8))) return bail(rc);
   if ((rc = dev_alloc(&c->d_first_bad, 1))) return bail(rc);
   e = build_small_tables(c->t64, c->bins, c->c64, c->stream);
@@ -1205,6 +1342,18 @@ int tempo_set_precision(tempo_ctx_t* c, int precision) {
   c->precision = precision;
   return TEMPO_OK;
 }
+
+#ifdef TEMPO_TRACE
+// Test builds only (not part of the ABI): later runs record every table index and
+// branch decision into the zeroed device buffer (TraceSlot layout, tempo_types.h),
+// kTracePoint ints per (tile column, level) point and kTraceColumn per tile column; one
+// tile per run (device-array runs, or host-array runs of one slab).  NULL: off.
+int tempo_set_trace_c(tempo_ctx_t* c, void* dev_buffer) {
+  if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
+  c->trace = (int*)dev_buffer;
+  return TEMPO_OK;
+}
+#endif
 
 int tempo_set_validation(tempo_ctx_t* c, int on) {
   if (!c) return fail(TEMPO_ERR_STATE, "NULL context");
@@ -1527,15 +1676,6 @@ void copy_scalars(A& d, const B& s) {
 template <class T> const TempoConsts<T>& consts_of(const tempo_ctx* c);
 template <> const TempoConsts<double>& consts_of<double>(const tempo_ctx* c) { return c->c64; }
 template <> const TempoConsts<float>& consts_of<float>(const tempo_ctx* c) { return c->c32; }
-template <class T> Tables<T> tables_of(const tempo_ctx* c);
-template <> Tables<double> tables_of<double>(const tempo_ctx* c) {
-  return Tables<double>{c->t64.t_efrw, c->t64.t_efsw, c->t64.tnc_wev, c->t64.tps_iaus, c->t64.tni_iaus,
-                        c->t64.tpi_ide, c->t64.tnccn, c->t64.qg, c->t64.qs, c->t64.qrfz, c->t64.qcfz};
-}
-template <> Tables<float> tables_of<float>(const tempo_ctx* c) {
-  return Tables<float>{c->f_efrw, c->f_efsw, c->f_tnc_wev, c->f_tps, c->f_tni, c->f_tpi,
-                       c->t64.tnccn, c->f_qg, c->f_qs, c->f_qrfz, c->f_qcfz};
-}
 
 // Packed (value, tangent) copies of a state and the step's scratch for Dual<T, 1>.
 template <class T>
@@ -1785,6 +1925,11 @@ int tempo_adjoint_dev_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, double dt, int 
   cudaStream_t s = (cudaStream_t)stream;
   return fp64 ? adjoint_dev<double>(c, cfg, dt, itimestep, x, lam, lam_diags, b, s)
               : adjoint_dev<float>(c, cfg, dt, itimestep, x, lam, lam_diags, b, s);
+}
+
+int tempo_run_batch_dev_f32_c(tempo_ctx_t* c, const tempo_cfgs_t* cfg, int ndomains,
+                              const tempo_domain_t* domains, void* stream) {
+  return run_batch(c, cfg, ndomains, domains, (cudaStream_t)stream);
 }
 
 int tempo_aerosol_surface_emissions_dev_c(tempo_ctx_t* c, double dt, double* nwfa,

@@ -115,4 +115,14 @@ struct TempoBins {
 };
 void make_bins(TempoBins* b);
 
+// Least values of the bins of the three table indices that the reference computes
+// with libm's log of a state value (main:2341, 2391, 2607): the rain-cloud
+// efficiency bin of mvd_r (nbr bins), the snow-cloud efficiency bin of the snow
+// diameter (nbs) and the droplet-number bin of nc (nbc).  edges[off + m - 1] is the
+// least double x whose index is >= m (edges[off] = 0), found on the host by bisection
+// over doubles with the host's libm, so that the device takes the bin the host
+// arithmetic gives for the same value.
+constexpr int kEdgesR = 0, kEdgesS = nbr, kEdgesN = nbr + nbs, kEdgesCount = nbr + nbs + nbc;
+void make_index_edges(const TempoBins& b, double* edges);
+
 }  // namespace tg

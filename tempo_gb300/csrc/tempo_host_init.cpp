@@ -5,7 +5,9 @@
 // initialize_bins_for_tables (:613-658), initialize_bins_for_hail_size (:661-671)
 // and create_bins (:695-722).  Gamma values use the C library tgamma, the same
 // routine the Fortran GAMMA intrinsic calls under gfortran.
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <complex>
 #include <cstdio>
 #include <cstdlib>
@@ -317,6 +319,51 @@ void make_radar_consts(RadarConsts* r) {
   r->mi_im = mi.imag();
   const double kw1 = std::abs((mw * mw - 1.0) / (mw * mw + 2.0));
   r->k_w = kw1 * kw1;
+}
+
+
+// ---- bin edges of the log-based table indices ------------------------------------
+namespace {
+uint64_t dbits(double x) {
+  uint64_t u;
+  std::memcpy(&u, &x, 8);
+  return u;
+}
+double dval(uint64_t u) {
+  double x;
+  std::memcpy(&x, &u, 8);
+  return x;
+}
+// least positive double x in [lo, hi] with f(x) >= m, for f non-decreasing, f(lo) < m
+// <= f(hi); positive doubles order as their bit patterns
+template <class F>
+double least_with(F f, int m, double lo, double hi) {
+  uint64_t a = dbits(lo), b = dbits(hi);
+  while (b - a > 1) {
+    const uint64_t mid = a + (b - a) / 2;
+    if (f(dval(mid)) >= m)
+      b = mid;
+    else
+      a = mid;
+  }
+  return dval(b);
+}
+}  // namespace
+
+void make_index_edges(const TempoBins& b, double* e) {
+  const double dr1 = b.dr[0], drn = b.dr[nbr - 1], ds1 = b.ds[0], dsn = b.ds[nbs - 1];
+  const double t_nc1 = b.t_nc[0], nic1 = std::log(b.t_nc[nbc - 1] / b.t_nc[0]);
+  // the reference's expressions, evaluated as the reference evaluates them
+  auto f_r = [&](double x) { return std::min(1 + (int)(nbr * std::log(x / dr1) / std::log(drn / dr1)), nbr); };
+  auto f_s = [&](double x) { return std::min(1 + (int)(nbs * std::log(x / ds1) / std::log(dsn / ds1)), nbs); };
+  auto f_n = [&](double x) {
+    return std::max(1, std::min((int)std::lround(1.0 + (double)nbc * std::log(x / t_nc1) / nic1), nbc));
+  };
+  const double lo = 1e-30, hi = 1e30;
+  e[kEdgesR] = e[kEdgesS] = e[kEdgesN] = 0.0;
+  for (int m = 2; m <= nbr; m++) e[kEdgesR + m - 1] = least_with(f_r, m, lo, hi);
+  for (int m = 2; m <= nbs; m++) e[kEdgesS + m - 1] = least_with(f_s, m, lo, hi);
+  for (int m = 2; m <= nbc; m++) e[kEdgesN + m - 1] = least_with(f_n, m, lo, hi);
 }
 
 }  // namespace tg

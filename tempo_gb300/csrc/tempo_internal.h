@@ -14,6 +14,7 @@ namespace tg {
 
 template <class R> struct Tables;
 template <class S> struct StepArgs;
+template <class S> struct BatchArgs;
 template <class I> struct IslandConsts;
 
 // tempo_step_f64.cu (FP64 drop-in, compiled without FMA contraction)
@@ -65,6 +66,12 @@ struct DerivOps {
                                const IslandConsts<Dual<T, IN_N>>& ci, const AdjArgs<T>& j, cudaStream_t s);
 };
 
+// tempo_batch.cu: the mixed step over a multi-domain batch (FP32 storage), one launch
+// sequence for every domain
+cudaError_t launch_batch_mixed_f32(const BatchArgs<float>& b, const Tables<float>& t,
+                                   const TempoConsts<float>& c32, const IslandConsts<df>& idf,
+                                   cudaStream_t s, const cudaEvent_t* ev, int sedim_variant);
+
 // tempo_noalloc.cu: the fixed scratch of tempo_run_dev_f32_noalloc_c (bytes, and its
 // address on `device`, looked up on the first call for that device)
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
@@ -109,6 +116,7 @@ struct DevTables64 {
   double *t_efrw, *t_efsw, *tpc_wev, *tnc_wev, *tps_iaus, *tni_iaus, *tpi_ide;
   double *qg, *qs, *qrfz, *qcfz;  // AoS layouts described in tempo_level.cuh
   float* tnccn;
+  double* edges;  // [kEdgesCount] bin edges of the log-based indices (make_index_edges)
 };
 // small init tables: compute_efrw/efsw, compute_drop_evap, qi_aut_qs
 // (tc: the constant set; the small tables use only its hail-independent members)

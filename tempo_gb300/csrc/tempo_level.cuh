@@ -14,6 +14,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 #include "tempo_consts.h"
 #include "tempo_dfloat.cuh"
@@ -154,8 +155,30 @@ struct Lev {
   R pres;
   R rhof, rhof2, diffu, visco, vsc2, tcond, lvap, ocp, lvt2;
   R qcten, ncten, qiten, niten, qrten, nrten, qsten, qgten, ngten, qbten, nwfaten, nifaten;
+  // magnitudes of the terms summed into each tendency (sums of absolute values; used by
+  // the mixed form only, see updated())
+  Cst<R> qcmag = 0, ncmag = 0, qimag = 0, nimag = 0, qrmag = 0, nrmag = 0, qsmag = 0, qgmag = 0,
+         ngmag = 0, qbmag = 0;
   R vtboost;
+#ifdef TEMPO_TRACE
+  int* tr = nullptr;  // this point's decision-trace record (TraceSlot), NULL = off
+  int tpass = 0;      // pass of the check routines (TR_CHECK + tpass)
+#endif
 };
+
+// decision trace of a test build: OR bits into a slot of the level's record
+#ifdef TEMPO_TRACE
+#define TG_TRACE(L, slot, bits)                    \
+  do {                                             \
+    if ((L).tr) (L).tr[(slot)] |= (int)(bits);     \
+  } while (0)
+#define TG_TRACE_PASS(L, p) ((L).tpass = (p))
+#else
+#define TG_TRACE(L, slot, bits) \
+  do {                          \
+  } while (0)
+#define TG_TRACE_PASS(L, p) ((void)0)
+#endif
 
 // process rates (ty_tend, main:47-64)
 template <class R>
@@ -277,6 +300,56 @@ __device__ void snow_moments(Lev<R>& L, R tc, int which) {
 // ---------------------------------------------------------------------------------
 // check_and_update routines (main:867-1260), one level
 // ---------------------------------------------------------------------------------
+// A value updated by its tendency, q + ten * dt, as the existence and clipping tests of
+// the check routines see it.  Where a step uses a species up completely -- a sink capped
+// at q / dt, or scaled by the over-depletion limiter to exactly what is there, or a
+// source used up by a sink in the same step -- the sum cancels: FP64 leaves about 1e-16
+// of the terms, far below the existence thresholds (r1 for masses, r2 or the minimum
+// number for numbers), and takes the species as gone.  FP32 leaves a few 1e-8 of the
+// terms, which can pass them.  So in the mixed form a sum within kCancelUlps rounding
+// units of its terms counts as cancelled (zero), and the decision is the one FP64 takes;
+// a value so close to zero is at the rounding level of the terms either way.  The terms'
+// scale is the larger of |q| + |ten dt| and |q| + mag dt, mag being the sum of the
+// magnitudes of the rates summed into ten.  The FP64 drop-in keeps the reference's sum.
+constexpr float kCancelUlps = 32.0f;
+template <class T> __device__ __forceinline__ T mag(T x) { return Fabs(x); }
+template <class T, int N> __device__ __forceinline__ T mag(const Dual<T, N>& x) { return Fabs(x.v); }
+template <class R>
+__device__ __forceinline__ R updated(R q, R ten, R dt, Cst<R> tmag = Cst<R>(0)) {
+  const R tdt = ten * dt;
+  const R v = q + tdt;
+  if constexpr (std::is_same<Cst<R>, float>::value) {
+    const float scale = mag(q) + Max(mag(tdt), tmag * mag(dt));
+    if (mag(v) <= kCancelUlps * 5.9604645e-8f * scale) return R(0.0f);
+  }
+  return v;
+}
+
+// The size clamps of the check routines (cloud, rain, ice and graupel diameters).  A later
+// pass re-checks a state that an earlier pass clamped: the diameter then comes out at the
+// clamp to within rounding, and the limit is taken again or not by the last bits (FP64
+// takes it again; both branches give the same state to rounding).  In the mixed form a
+// diameter within kTieUlps rounding units of its clamp counts as at the clamp, so that it
+// takes the limit as FP64 does.  The FP64 drop-in keeps the reference's comparisons.
+constexpr float kTieUlps = 16.0f;
+template <class R> __device__ __forceinline__ bool over_clamp(R x, R bound) {
+  if constexpr (std::is_same<Cst<R>, float>::value)
+    return x > bound * R(1.0f - kTieUlps * 5.9604645e-8f);
+  else
+    return x > bound;
+}
+template <class R> __device__ __forceinline__ bool under_clamp(R x, R bound) {
+  if constexpr (std::is_same<Cst<R>, float>::value)
+    return x < bound * R(1.0f + kTieUlps * 5.9604645e-8f);
+  else
+    return x < bound;
+}
+
+// the magnitudes of a level's tendencies start at zero (no rate summed yet)
+template <class R> __device__ __forceinline__ void clear_mags(Lev<R>& L) {
+  L.qcmag = L.ncmag = L.qimag = L.nimag = L.qrmag = L.nrmag = L.qsmag = L.qgmag = L.ngmag =
+      L.qbmag = Cst<R>(0);
+}
 template <class R>
 __device__ __forceinline__ void aerosol_check(Lev<R>& L, uint32_t f, R dt) {  // main:867-888
   R rho = R(L.rho);
@@ -294,12 +367,13 @@ __device__ void cloud_check(Lev<R>& L, R& q, R& n, bool has_nc, R ncsave, R dt, 
   bool hit_limit = false;
   int nu_c;
   R lamc, xdc;
-  if (q + L.qcten * dt > R(r1)) {
+  const R qn = updated(q, L.qcten, dt, L.qcmag);
+  if (qn > R(r1)) {
     L.l_qc = true;
-    L.rc = (q + L.qcten * dt) * rho;
-    q = q + L.qcten * dt;
+    L.rc = qn * rho;
+    q = qn;
     if (has_nc) {
-      L.nc = Max(R(nt_c_min), (n + L.ncten * dt) * rho);
+      L.nc = Max(R(nt_c_min), updated(n, L.ncten, dt, L.ncmag) * rho);
       if (L.nc <= R(nt_c_min)) {
         hit_limit = true;
         L.nc = R(nt_c_min);
@@ -311,10 +385,10 @@ __device__ void cloud_check(Lev<R>& L, R& q, R& n, bool has_nc, R ncsave, R dt, 
       nu_c = get_nuc(L.nc);
       lamc = Pow(L.nc * c.am_r * c.ccg[nu_c - 1][1] * c.ocg1[nu_c - 1] / L.rc, c.obmr);
       xdc = (R(bm_r) + R(nu_c) + R(1.0)) / lamc;
-      if (xdc < R(d0c)) {
+      if (under_clamp(xdc, R(d0c))) {
         lamc = c.cce[nu_c - 1][1] / R(d0c);
         hit_limit = true;
-      } else if (xdc > R(d0r) * R(2.0)) {
+      } else if (over_clamp(xdc, R(d0r) * R(2.0))) {
         lamc = c.cce[nu_c - 1][1] / (R(d0r) * R(2.0));
         hit_limit = true;
       }
@@ -330,6 +404,7 @@ __device__ void cloud_check(Lev<R>& L, R& q, R& n, bool has_nc, R ncsave, R dt, 
     lamc = Pow(L.nc * c.am_r * c.ccg[nu_c - 1][1] * c.ocg1[nu_c - 1] / L.rc, c.obmr);
     L.ilamc = R(1.0) / lamc;
     L.mvd_c = Max(Min((R(3.0) + R(nu_c) + R(0.672)) * L.ilamc, R(d0r)), R(d0c));
+    TG_TRACE(L, TR_CHECK + L.tpass, TB_QC | (hit_limit ? TB_QC_HIT : 0) | (nu_c << 16));
   } else {
     L.l_qc = false;
     L.rc = R(r1);
@@ -352,11 +427,12 @@ __device__ void rain_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
   R rho = R(L.rho);
   bool hit_limit = false;
   R lamr;
-  if (q + L.qrten * dt > R(r1)) {
+  const R qn = updated(q, L.qrten, dt, L.qrmag);
+  if (qn > R(r1)) {
     L.l_qr = true;
-    L.rr = (q + L.qrten * dt) * rho;
-    q = q + L.qrten * dt;
-    L.nr = Max(R(r2), (n + L.nrten * dt) * rho);
+    L.rr = qn * rho;
+    q = qn;
+    L.nr = Max(R(r2), updated(n, L.nrten, dt, L.nrmag) * rho);
     if (L.nr <= R(r2)) {
       hit_limit = true;
       L.mvd_r = R(1.0e-3);
@@ -365,12 +441,12 @@ __device__ void rain_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
     }
     lamr = Pow(c.am_r * c.crg[2] * c.org2 * L.nr / L.rr, c.obmr);
     L.mvd_r = (R(3.0) + R(mu_r) + R(0.672)) / lamr;
-    if (L.mvd_r > R(d0r_max)) {
+    if (over_clamp(L.mvd_r, R(d0r_max))) {
       hit_limit = true;
       L.mvd_r = R(d0r_max);
       lamr = (R(3.0) + R(mu_r) + R(0.672)) / L.mvd_r;
       L.nr = c.crg[1] * c.org3 * L.rr * Pow(lamr, R(bm_r)) / c.am_r;
-    } else if (L.mvd_r < R(d0r) * R(0.75)) {
+    } else if (under_clamp(L.mvd_r, R(d0r) * R(0.75))) {
       hit_limit = true;
       L.mvd_r = R(d0r) * R(0.75);
       lamr = (R(3.0) + R(mu_r) + R(0.672)) / L.mvd_r;
@@ -379,6 +455,7 @@ __device__ void rain_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
     if (hit_limit) L.nrten = (L.nr / rho - n) * odt;
     n = c.crg[1] * c.org3 * q * Pow(lamr, R(bm_r)) / c.am_r;
     L.ilamr = R(1.0) / lamr;
+    TG_TRACE(L, TR_CHECK + L.tpass, TB_QR | (hit_limit ? TB_QR_HIT : 0));
   } else {
     L.l_qr = false;
     L.rr = R(r1);
@@ -399,11 +476,12 @@ __device__ void ice_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
   R rho = R(L.rho);
   bool hit_limit = false;
   R lami, xdi;
-  if (q + L.qiten * dt > R(r1)) {
+  const R qn = updated(q, L.qiten, dt, L.qimag);
+  if (qn > R(r1)) {
     L.l_qi = true;
-    L.ri = (q + L.qiten * dt) * rho;
-    q = q + L.qiten * dt;
-    L.ni = Max(R(r2), (n + L.niten * dt) * rho);
+    L.ri = qn * rho;
+    q = qn;
+    L.ni = Max(R(r2), updated(n, L.niten, dt, L.nimag) * rho);
     if (L.ni <= R(r2)) {
       hit_limit = true;
       lami = c.cie[1] / R(5.e-6);
@@ -411,11 +489,11 @@ __device__ void ice_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
     }
     lami = Pow(c.am_i * c.cig[1] * c.oig1 * L.ni / L.ri, c.obmi);
     xdi = (R(bm_i) + R(mu_i) + R(1.0)) / lami;
-    if (xdi < R(5.e-6)) {
+    if (under_clamp(xdi, R(5.e-6))) {
       hit_limit = true;
       lami = c.cie[1] / R(5.e-6);
       L.ni = Min(R(max_ni), c.cig[0] * c.oig2 * L.ri / c.am_i * Pow(lami, R(bm_i)));
-    } else if (xdi > R(d0s)) {
+    } else if (over_clamp(xdi, R(d0s))) {
       hit_limit = true;
       lami = c.cie[1] / R(d0s);
       L.ni = c.cig[0] * c.oig2 * L.ri / c.am_i * Pow(lami, R(bm_i));
@@ -423,6 +501,7 @@ __device__ void ice_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
     if (hit_limit) L.niten = (L.ni / rho - n) * odt;
     n = Max(R(r2) / rho, Min(c.cig[0] * c.oig2 * q / c.am_i * Pow(lami, R(bm_i)), R(max_ni) / rho));
     L.ilami = R(1.0) / lami;
+    TG_TRACE(L, TR_CHECK + L.tpass, TB_QI | (hit_limit ? TB_QI_HIT : 0));
   } else {
     L.l_qi = false;
     L.ri = R(r1);
@@ -439,10 +518,12 @@ __device__ void ice_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
 template <class R>
 __device__ __forceinline__ void snow_check(Lev<R>& L, R& q, R dt, R odt) {
   R rho = R(L.rho);
-  if (q + L.qsten * dt > R(r1)) {
+  const R qn = updated(q, L.qsten, dt, L.qsmag);
+  if (qn > R(r1)) {
     L.l_qs = true;
-    L.rs = (q + L.qsten * dt) * rho;
-    q = q + L.qsten * dt;
+    L.rs = qn * rho;
+    q = qn;
+    TG_TRACE(L, TR_CHECK + L.tpass, TB_QS);
   } else {
     L.l_qs = false;
     L.rs = R(r1);
@@ -471,14 +552,15 @@ __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R od
   R rho = R(L.rho);
   bool hit_limit = false;
   R lamg;
-  if (q + L.qgten * dt > R(r1)) {
+  const R qn = updated(q, L.qgten, dt, L.qgmag);
+  if (qn > R(r1)) {
     L.l_qg = true;
-    L.rg = (q + L.qgten * dt) * rho;
-    q = q + L.qgten * dt;
+    L.rg = qn * rho;
+    q = qn;
     if (hail) {
-      L.ng = Max(R(r2), (n + L.ngten * dt) * rho);
+      L.ng = Max(R(r2), updated(n, L.ngten, dt, L.ngmag) * rho);
       const R rb_hi = L.rg * R(meters3_to_liters) / rho_g<R>(1);
-      L.rb = Min(Max(L.rg * R(meters3_to_liters) / rho_g<R>(nrhg), (b + L.qbten * dt) * rho), rb_hi);
+      L.rb = Min(Max(L.rg * R(meters3_to_liters) / rho_g<R>(nrhg), updated(b, L.qbten, dt, L.qbmag) * rho), rb_hi);
       L.idx_bg = density_class(R(10.0) * L.rg / L.rb, L.rb, rb_hi);
       const int ig = L.idx_bg;
       if (L.ng <= R(r2)) {
@@ -489,12 +571,12 @@ __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R od
       }
       lamg = Pow(c.am_g[ig - 1] * c.cgg[0][2] * c.ogg2 * L.ng / L.rg, c.obmg);
       L.mvd_g = (R(3.0) + R(mu_g) + R(0.672)) / lamg;
-      if (L.mvd_g > R(25.4e-3)) {
+      if (over_clamp(L.mvd_g, R(25.4e-3))) {
         hit_limit = true;
         L.mvd_g = R(25.4e-3);
         lamg = (R(3.0) + R(mu_g) + R(0.672)) / L.mvd_g;
         L.ng = c.cgg[0][1] * c.ogg3 * L.rg * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
-      } else if (L.mvd_g < R(d0r)) {
+      } else if (under_clamp(L.mvd_g, R(d0r))) {
         hit_limit = true;
         L.mvd_g = R(d0r);
         lamg = (R(3.0) + R(mu_g) + R(0.672)) / L.mvd_g;
@@ -503,7 +585,7 @@ __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R od
       if (hit_limit) L.ngten = (L.ng / rho - n) * odt;
       n = c.cgg[0][1] * c.ogg3 * q * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
       const R b_hi = R(meters3_to_liters) * q / rho_g<R>(1);
-      b = Min(Max(q * R(meters3_to_liters) / rho_g<R>(nrhg), b + L.qbten * dt), b_hi);
+      b = Min(Max(q * R(meters3_to_liters) / rho_g<R>(nrhg), updated(b, L.qbten, dt, L.qbmag)), b_hi);
       L.idx_bg = density_class(R(10.0) * q / b, b, b_hi);
     } else {
       L.idx_bg = idx_bg1;
@@ -517,6 +599,7 @@ __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R od
     }
     L.ilamg = R(1.0) / lamg;
     L.mvd_g = (R(3.0) + R(mu_g) + R(0.672)) * L.ilamg;
+    TG_TRACE(L, TR_CHECK + L.tpass, TB_QG | (hit_limit ? TB_QG_HIT : 0) | (L.idx_bg << 12));
   } else {
     L.l_qg = false;
     L.rg = R(r1);

@@ -46,11 +46,27 @@ __device__ __forceinline__ void graupel_index(const TempoConsts<C>& c, R rg, R i
   R n0_exp = c.ogg1 * rg / c.am_g[idx - 1] * Pow(lam_exp, c.cge[0][0]);
   idx_g1 = decade_index(n0_exp, c.nig3, ntb_g1);
 }
+// The bin of a value whose reference index is a non-decreasing function of it built on
+// libm's log (main:2341, 2391, 2607).  `guess` is that function in this device's
+// arithmetic; the edges (least value of each bin, tempo_consts.h make_index_edges,
+// computed with the host's libm) settle the bin exactly, so the index is the host
+// arithmetic's for the same value even where the device's log differs in its last bit.
+__device__ __forceinline__ double edge_arg(double x) { return x; }
+__device__ __forceinline__ double edge_arg(float x) { return (double)x; }
+template <class T, int N> __device__ __forceinline__ double edge_arg(const Dual<T, N>& x) { return (double)x.v; }
+__device__ __forceinline__ int edge_index(const double* e, int n, double x, int guess) {
+  int g = max(1, min(guess, n));
+  while (g < n && x >= __ldg(e + g)) g++;
+  while (g > 1 && x < __ldg(e + g - 1)) g--;
+  return g;
+}
+
 template <class C, class R>
-__device__ __forceinline__ void cloud_index(const TempoConsts<C>& c, R rc, R nc, int& idx_c, int& idx_n) {  // :2591-2609
+__device__ __forceinline__ void cloud_index(const TempoConsts<C>& c, const double* edges, R rc, R nc,
+                                            int& idx_c, int& idx_n) {  // :2591-2609
   idx_c = decade_index(rc, c.nic2, ntb_c);
   int in = Nint(R(1.0) + R(nbc) * Log(nc / c.t_nc1) / c.nic1);
-  idx_n = max(1, min(in, nbc));
+  idx_n = edge_index(edges + kEdgesN, nbc, edge_arg(nc), in);
 }
 
 // ---------------------------------------------------------------------------------
@@ -62,12 +78,14 @@ __device__ void warm_rain(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, 
   const TempoConsts<Cst<R>>& c = *L.cs;
   if (L.l_qr) {
     if (L.mvd_r > R(d0r)) {
+      TG_TRACE(L, TR_RW, 1 << 16);
       R ef_rr = Max(R(-0.1), R(1.0) - Exp(R(2300.0) * (L.mvd_r - R(1950.0e-6))));
       t.pnr_rcr = ef_rr * R(2.0) * L.nr * L.rr;
     }
   }
   if (L.l_qc) {
     if (L.rc > R(0.01e-3)) {
+      TG_TRACE(L, TR_RW, 1 << 17);
       int nu_c = get_nuc(L.nc);
       R lamc = R(1.0) / L.ilamc;
       R xdc = Max(R(d0c) * R(1.e6), (Pow(L.rc / (c.am_r * L.nc), c.obmr)) * R(1.e6));
@@ -89,7 +107,8 @@ __device__ void warm_rain(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, 
     if (L.mvd_r > R(d0r) && L.mvd_c > R(d0c)) {
       R lamr = (R(3.0) + R(mu_r) + R(0.672)) / L.mvd_r;
       int idx = 1 + Int(R(nbr) * Log(L.mvd_r / c.dr1) / Log(c.drn / c.dr1));
-      idx = min(idx, nbr);
+      idx = edge_index(T.edges + kEdgesR, nbr, edge_arg(L.mvd_r), idx);
+      TG_TRACE(L, TR_RW, idx | (Int(L.mvd_c * R(1.e6)) << 8) | (1 << 18));
       R ef_rw = ld(T.t_efrw + (idx - 1) + (long)(Int(L.mvd_c * R(1.e6)) - 1) * nbr);
       R n0_r = L.nr * c.org2 * Pow(lamr, c.cre[1]);
       t.prr_rcw = L.rhof * c.t1_qr_qc * ef_rw * L.rc * n0_r * Pow(lamr + R(fv_r), -c.cre[8]);
@@ -109,6 +128,7 @@ __device__ void rain_snow_rain_graupel(const Lev<R>& L, Tend<R>& t, const Tables
       int idx_t = temperature_index<R>(L.temp), idx_r, idx_r1;
       rain_index(c, L.rr, L.ilamr, idx_r, idx_r1);
       int idx_s = decade_index(L.rs, c.nis2, ntb_s);
+      TG_TRACE(L, TR_RS, idx_s | (idx_t << 6) | (idx_r1 << 12) | (idx_r << 18) | (1 << 24));
       const Cst<R>* e = T.qs + 12L * ((idx_s - 1) + (long)(idx_t - 1) * ntb_s +
                                  (long)(idx_r1 - 1) * ntb_s * ntb_t +
                                  (long)(idx_r - 1) * ntb_s * ntb_t * ntb_r1);
@@ -139,6 +159,7 @@ __device__ void rain_snow_rain_graupel(const Lev<R>& L, Tend<R>& t, const Tables
       int idx_r, idx_r1, idx_g, idx_g1;
       rain_index(c, L.rr, L.ilamr, idx_r, idx_r1);
       graupel_index(c, L.rg, L.ilamg, ig, idx_g, idx_g1);
+      TG_TRACE(L, TR_RG, idx_g1 | (idx_g << 6) | (idx_r1 << 12) | (idx_r << 18) | (1 << 24));
       const Cst<R>* e = T.qg + 5L * ((idx_g1 - 1) + (long)(idx_g - 1) * ntb_g1 +
                                 (long)(ig - 1) * ntb_g1 * ntb_g +
                                 (long)(idx_r1 - 1) * ntb_g1 * ntb_g * nrhg +
@@ -207,6 +228,7 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
   if (L.rr > c.r_r1) {
     int idx_r, idx_r1;
     rain_index(c, L.rr, L.ilamr, idx_r, idx_r1);
+    TG_TRACE(L, TR_FZR, idx_r | (idx_r1 << 6) | (idx_tc << 12) | (idx_in << 18) | (1 << 24));
     const Cst<R>* e = T.qrfz + 4L * ((idx_r - 1) + (long)(idx_r1 - 1) * ntb_r +
                                 (long)(idx_tc - 1) * ntb_r * ntb_r1 +
                                 (long)(idx_in - 1) * ntb_r * ntb_r1 * ntb_t1);
@@ -218,13 +240,15 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
     t.pnr_rfz = Min(L.nr * odt, t.pnr_rfz);
     t.png_rfz = t.pnr_rfz * Max(Min((Pow(R(10.0), -(R(0.1) * w)) + R(0.1)), R(1.0)), R(0.1));
   } else if (L.rr > R(r1) && L.temp < hgfrz) {
+    TG_TRACE(L, TR_FZR, 1 << 25);
     t.pri_rfz = L.rr * odt;
     t.pni_rfz = L.nr * odt;
   }
   t.pbg_rfz = R(meters3_to_liters) * t.prg_rfz / R(rho_i);
   if (L.rc > c.r_c1) {
     int idx_c, idx_n;
-    cloud_index(c, L.rc, L.nc, idx_c, idx_n);
+    cloud_index(c, T.edges, L.rc, L.nc, idx_c, idx_n);
+    TG_TRACE(L, TR_FZC, idx_c | (idx_n << 8) | (1 << 16));
     const Cst<R>* e = T.qcfz + 2L * ((idx_c - 1) + (long)(idx_n - 1) * ntb_c +
                                 (long)(idx_tc - 1) * ntb_c * nbc +
                                 (long)(idx_in - 1) * ntb_c * nbc * ntb_t1);
@@ -233,6 +257,7 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
     t.pni_wfz = ld(e + 1) * odt;
     t.pni_wfz = Min3(L.nc * odt, t.pri_wfz / (R(2.0) * R(xm0i)), t.pni_wfz);
   } else if (L.rc > R(r1) && L.temp < hgfrz) {
+    TG_TRACE(L, TR_FZC, 1 << 17);
     t.pri_wfz = L.rc * odt;
     t.pni_wfz = L.nc * odt;
   }
@@ -288,6 +313,7 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>&
   R ssati = R(L.ssati);
   if (L.l_qi) {
     int idx_i = decade_index(L.ri, c.nii2, ntb_i), idx_i1 = decade_index(L.ni, c.nii3, ntb_i1);
+    TG_TRACE(L, TR_ICE, idx_i | (idx_i1 << 8) | (1 << 16));
     R xdi = Max(R(c.d0i), (R(bm_i) + R(mu_i) + R(1.)) * L.ilami);
     R xmi = c.am_i * Pow(xdi, R(bm_i));
     R oxmi = R(1.0) / xmi;
@@ -376,7 +402,8 @@ __device__ void riming(Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, R odt) {
     R xds = L.smoc / L.smob;
     if ((L.mvd_c > R(d0c)) && (xds > R(d0s))) {
       int idxs = 1 + Int(R(nbs) * Log(xds / c.ds1) / Log(c.dsn / c.ds1));
-      idxs = min(idxs, nbs);
+      idxs = edge_index(T.edges + kEdgesS, nbs, edge_arg(xds), idxs);
+      TG_TRACE(L, TR_RIME, idxs | (Int(L.mvd_c * R(1.e6)) << 8) | (1 << 16));
       R ef_sw = ld(T.t_efsw + (idxs - 1) + (long)(Int(L.mvd_c * R(1.e6)) - 1) * nbs);
       t.prs_scw = L.rhof * c.t1_qs_qc * ef_sw * L.rc * L.smoe;
       t.prs_scw = Min(L.rc * odt, t.prs_scw);
@@ -593,6 +620,7 @@ __device__ void check_over_depletion(const Lev<R>& L, Tend<R>& t, R odt) {
   sump = t.pri_inu + t.pri_ide + t.prs_ide + t.prs_sde + t.prg_gde + t.pri_iha;
   rate_max = R((L.qv - L.qvsi) * L.rho) * odt * R(0.999);
   if ((sump > R(eps) && sump > rate_max) || (sump < R(-eps) && sump < rate_max)) {
+    TG_TRACE(L, TR_LIMIT, 1 << 0);
     ratio = rate_max / sump;
     t.pri_inu = t.pri_inu * ratio;
     t.pri_ide = t.pri_ide * ratio;
@@ -605,6 +633,7 @@ __device__ void check_over_depletion(const Lev<R>& L, Tend<R>& t, R odt) {
   sump = -t.prr_wau - t.pri_wfz - t.prr_rcw - t.prs_scw - t.prg_scw - t.prg_gcw;
   rate_max = -L.rc * odt;
   if (L.l_qc && sump < rate_max) {
+    TG_TRACE(L, TR_LIMIT, 1 << 1);
     ratio = rate_max / sump;
     t.prr_wau = t.prr_wau * ratio;
     t.pri_wfz = t.pri_wfz * ratio;
@@ -616,6 +645,7 @@ __device__ void check_over_depletion(const Lev<R>& L, Tend<R>& t, R odt) {
   sump = t.pri_ide - t.prs_iau - t.prs_sci - t.pri_rci;
   rate_max = -L.ri * odt;
   if (L.l_qi && sump < rate_max) {
+    TG_TRACE(L, TR_LIMIT, 1 << 2);
     ratio = rate_max / sump;
     t.pri_ide = t.pri_ide * ratio;
     t.prs_iau = t.prs_iau * ratio;
@@ -625,6 +655,7 @@ __device__ void check_over_depletion(const Lev<R>& L, Tend<R>& t, R odt) {
   sump = -t.prg_rfz - t.pri_rfz - t.prr_rci + t.prr_rcs + t.prr_rcg;
   rate_max = -L.rr * odt;
   if (L.l_qr && sump < rate_max) {
+    TG_TRACE(L, TR_LIMIT, 1 << 3);
     ratio = rate_max / sump;
     t.prg_rfz = t.prg_rfz * ratio;
     t.pbg_rfz = t.pbg_rfz * ratio;
@@ -636,6 +667,7 @@ __device__ void check_over_depletion(const Lev<R>& L, Tend<R>& t, R odt) {
   sump = t.prs_sde - t.prs_ihm - t.prr_sml + t.prs_rcs;
   rate_max = -L.rs * odt;
   if (L.l_qs && sump < rate_max) {
+    TG_TRACE(L, TR_LIMIT, 1 << 4);
     ratio = rate_max / sump;
     t.prs_sde = t.prs_sde * ratio;
     t.prs_ihm = t.prs_ihm * ratio;
@@ -645,6 +677,7 @@ __device__ void check_over_depletion(const Lev<R>& L, Tend<R>& t, R odt) {
   sump = t.prg_gde - t.prg_ihm - t.prr_gml + t.prg_rcg;
   rate_max = -L.rg * odt;
   if (L.l_qg && sump < rate_max) {
+    TG_TRACE(L, TR_LIMIT, 1 << 5);
     ratio = rate_max / sump;
     t.prg_gde = t.prg_gde * ratio;
     t.prg_ihm = t.prg_ihm * ratio;
@@ -691,6 +724,30 @@ __device__ void sum_tendencies(Lev<R>& L, const Tend<R>& t) {
   L.qbten = L.qbten + (t.pbg_scw + t.pbg_rfz + t.pbg_gcw + t.pbg_rci + t.pbg_rcs + t.pbg_rcg +
                        t.pbg_sml - t.pbg_gml +
                        R(meters3_to_liters) * (t.prg_gde - t.prg_ihm) / rho_g<R>(L.idx_bg)) * orho;
+  if constexpr (std::is_same<Cst<R>, float>::value) {
+    // magnitudes of the summed terms (the cancellation test of the checks, updated())
+    using C = Cst<R>;
+    const C om = mag(orho);
+    auto M = [](auto... x) { return (mag(x) + ...); };
+    L.qcmag = L.qcmag + M(t.prr_wau, t.pri_wfz, t.prr_rcw, t.prs_scw, t.prg_scw, t.prg_gcw) * om;
+    L.ncmag = L.ncmag + M(t.pnc_wau, t.pnc_rcw, t.pni_wfz, t.pnc_scw, t.pnc_gcw) * om;
+    L.qimag = L.qimag + M(t.pri_inu, t.pri_iha, t.pri_ihm, t.pri_wfz, t.pri_rfz, t.pri_ide, t.prs_iau,
+                          t.prs_sci, t.pri_rci) * om;
+    L.nimag = L.nimag + M(t.pni_inu, t.pni_iha, t.pni_ihm, t.pni_wfz, t.pni_rfz, t.pni_ide, t.pni_iau,
+                          t.pni_sci, t.pni_rci) * om;
+    L.qrmag = L.qrmag + M(t.prr_wau, t.prr_rcw, t.prr_sml, t.prr_gml, t.prr_rcs, t.prr_rcg, t.prg_rfz,
+                          t.pri_rfz, t.prr_rci) * om;
+    L.nrmag = L.nrmag + M(t.pnr_wau, t.pnr_sml, t.pnr_gml, t.pnr_rfz, t.pnr_rcr, t.pnr_rcg, t.pnr_rcs,
+                          t.pnr_rci, t.pni_rfz) * om;
+    L.qsmag = L.qsmag + M(t.prs_iau, t.prs_sde, t.prs_sci, t.prs_scw, t.prs_rcs, t.prs_ide, t.prs_ihm,
+                          t.prr_sml) * om;
+    L.qgmag = L.qgmag + M(t.prg_scw, t.prg_rfz, t.prg_gde, t.prg_rcg, t.prg_gcw, t.prg_rci, t.prg_rcs,
+                          t.prg_ihm, t.prr_gml) * om;
+    L.ngmag = L.ngmag + M(t.png_scw, t.png_rfz, t.png_rcg, t.png_rci, t.png_rcs, t.png_gde, t.pnr_gml) * om;
+    L.qbmag = L.qbmag + (M(t.pbg_scw, t.pbg_rfz, t.pbg_gcw, t.pbg_rci, t.pbg_rcs, t.pbg_rcg, t.pbg_sml,
+                           t.pbg_gml) +
+                         C(meters3_to_liters) * M(t.prg_gde, t.prg_ihm) / C(rho_gd(L.idx_bg))) * om;
+  }
   I ocp = I(L.ocp);
   if (L.temp < t0) {
     L.tten = L.tten + (lsub * ocp * I(t.pri_inu + t.pri_ide + t.prs_ide + t.prs_sde + t.prg_gde + t.pri_iha) +
@@ -802,7 +859,8 @@ __device__ void cloud_condensation(const Lev<R>& L, Tend<R>& t, const Tables<Cst
       R dc_star = Sqrt(-(R(2.0) * dt) * t1_evap / (R(2.0) * R(pi)) * R(4.0) * L.diffu * R(L.ssatw) * rvs / R(rho_w));
       int idx_d = max(1, min(Int(R(1.e6) * dc_star), nbc));
       int idx_c, idx_n;
-      cloud_index(c, L.rc, L.nc, idx_c, idx_n);
+      cloud_index(c, T.edges, L.rc, L.nc, idx_c, idx_n);
+      TG_TRACE(L, TR_EVAP, idx_d | (idx_c << 8) | (idx_n << 16) | (1 << 24));
       R tnc = ld(T.tnc_wev + (idx_d - 1) + (long)(idx_c - 1) * nbc + (long)(idx_n - 1) * nbc * ntb_c);
       t.prw_vcd = Max(-(L.rc * R(0.99) * orho * odt), t.prw_vcd);
       t.pnc_wcd = Max(-(L.nc * R(0.99) * orho * odt), -(tnc * orho * odt));

@@ -183,6 +183,7 @@ template <class R>
 __device__ __forceinline__ void initial_checks(Lev<R>& L, uint32_t f, R& ncsave, bool do_ginit, R dt,
                                                R odt, const double* mlnet = nullptr, R w = R(0)) {
   using I = Isl<R>;
+  TG_TRACE_PASS(L, 0);
   rain_check(L, L.qr1d, L.nr1d, dt, odt);
   ice_check(L, L.qi1d, L.ni1d, dt, odt);
   snow_check(L, L.qs1d, dt, odt);
@@ -217,13 +218,14 @@ __device__ __forceinline__ void store_checked(const StepArgs<S>& a, long e, cons
 // ---------------------------------------------------------------------------------
 // prep: early-exit test, early columns, compaction
 // ---------------------------------------------------------------------------------
+// Prep of column c of a's tile (valid: c < a.ncol).  Every lane of the warp calls it;
+// lanes with the same `group` (the domain of a multi-domain batch; 0 for one tile) take
+// their slots with one atomic on their tile's counter.
 template <class R, class S>
-__global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__ StepArgs<S> a,
-                                                          const __grid_constant__ TempoConsts<Cst<R>> cst,
-                                                          const __grid_constant__ IslandConsts<Isl<R>> ci) {
+__device__ __forceinline__ void prep_column(const StepArgs<S>& a, const TempoConsts<Cst<R>>& cst,
+                                            const IslandConsts<Isl<R>>& ci, long c, bool valid,
+                                            int group) {
   using I = Isl<R>;
-  const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = c < a.ncol;
   const uint32_t f = a.flags;
   const int nz = a.nz;
   const bool hail = f & F_HAIL;
@@ -257,16 +259,14 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
     early = !do_micro && !supersat;
   }
 
-  // compaction: one atomic per warp, slots in lane order
+  // compaction: one atomic per warp (per group of the warp), slots in lane order
   const bool active = valid && !early;
-  const unsigned lanes = __ballot_sync(0xffffffffu, active);
+  const unsigned lanes = __ballot_sync(0xffffffffu, active) & __match_any_sync(0xffffffffu, group);
   const int lane = threadIdx.x & 31;
   unsigned first = 0;
-  if (lanes) {
-    const int leader = __ffs(lanes) - 1;
-    if (lane == leader) first = atomicAdd(a.nact, (unsigned)__popc(lanes));
-    first = __shfl_sync(0xffffffffu, first, leader);
-  }
+  const int leader = lanes ? __ffs(lanes) - 1 : lane;
+  if (lanes && lane == leader) first = atomicAdd(a.nact, (unsigned)__popc(lanes));
+  first = __shfl_sync(0xffffffffu, first, leader);
   if (!valid) return;
   if (active) {
     const long s = first + __popc(lanes & ((1u << lane) - 1u));
@@ -293,6 +293,9 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
     Lev<R> L;
     L.cs = &cst;
     L.ci = &ci;
+#ifdef TEMPO_TRACE
+    L.tr = a.trace ? a.trace + (c * nz + k) * kTracePoint : nullptr;
+#endif
     const FwdIO<S> io{a};
     load_level(a, e, L, io);
     R ncsave = ncsave_of<R>(a, g);
@@ -319,6 +322,14 @@ __global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__
     if (a.ncmr) a.ncmr[e3] = S(0);
   }
   atomicAdd(a.stats, 1ull);
+}
+
+template <class R, class S>
+__global__ void __launch_bounds__(128) tempo_prep_kernel(const __grid_constant__ StepArgs<S> a,
+                                                          const __grid_constant__ TempoConsts<Cst<R>> cst,
+                                                          const __grid_constant__ IslandConsts<Isl<R>> ci) {
+  const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  prep_column<R, S>(a, cst, ci, c, c < a.ncol, 0);
 }
 
 // ---------------------------------------------------------------------------------
@@ -353,15 +364,14 @@ __device__ __forceinline__ int point_regime(const StepArgs<S>& a, long e) {
 // one block per window: the regime of each of its points, then their positions in the
 // window (regime by regime from regime 63 down; inside a regime, warp w's points after
 // those of the warps below w, each warp's in the order of its items and lanes)
-template <class S>
-__global__ void __launch_bounds__(kRegimeBlock) tempo_regime_order_kernel(const __grid_constant__ StepArgs<S> a) {
+// The body of one block: window q0 of npts points, regime_of(q) the regime of point q,
+// ord the output.
+template <class RegimeOf>
+__device__ __forceinline__ void regime_order_window(long q0, long npts, RegimeOf regime_of, unsigned* ord) {
   constexpr int kWarps = kRegimeBlock / 32;
   __shared__ unsigned wcnt[kWarps][kRegimes];  // per warp: count, then offset in the window
   __shared__ unsigned start[kRegimes];         // first position of a regime in the window
   __shared__ unsigned wtot;
-  const long nact = (long)*a.nact, npts = nact * a.nz;
-  const long q0 = (long)blockIdx.x * kRegimeWindow;
-  if (q0 >= npts) return;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < kWarps * kRegimes; i += kRegimeBlock) (&wcnt[0][0])[i] = 0;
   __syncthreads();
@@ -371,12 +381,7 @@ __global__ void __launch_bounds__(kRegimeBlock) tempo_regime_order_kernel(const 
 #pragma unroll
   for (int j = 0; j < kRegimeItems; j++) {
     const long q = q0 + (long)j * kRegimeBlock + threadIdx.x;
-    reg[j] = -1;
-    if (q < npts) {
-      const int k = (int)(q / nact);
-      const long s = q - (long)k * nact;
-      reg[j] = point_regime(a, col_geom(a, a.act[s]).base + (long)k * a.NI);
-    }
+    reg[j] = q < npts ? regime_of(q) : -1;
   }
 #pragma unroll
   for (int j = 0; j < kRegimeItems; j++) {
@@ -417,8 +422,20 @@ __global__ void __launch_bounds__(kRegimeBlock) tempo_regime_order_kernel(const 
   for (int j = 0; j < kRegimeItems; j++)
     if (reg[j] >= 0) {
       const long pos = q0 + (long)(start[reg[j]] + wcnt[wid][reg[j]] + rank[j]);
-      if (pos < npts) a.ord[pos] = (unsigned)(q0 + (long)j * kRegimeBlock + threadIdx.x);
+      if (pos < npts) ord[pos] = (unsigned)(q0 + (long)j * kRegimeBlock + threadIdx.x);
     }
+}
+
+template <class S>
+__global__ void __launch_bounds__(kRegimeBlock) tempo_regime_order_kernel(const __grid_constant__ StepArgs<S> a) {
+  const long nact = (long)*a.nact, npts = nact * a.nz;
+  const long q0 = (long)blockIdx.x * kRegimeWindow;
+  if (q0 >= npts) return;
+  regime_order_window(q0, npts, [&](long q) {
+    const int k = (int)(q / nact);
+    const long s = q - (long)k * nact;
+    return point_regime(a, col_geom(a, a.act[s]).base + (long)k * a.NI);
+  }, a.ord);
 }
 
 // One stage of phase A, each followed by thermo_vars in the caller: 0 = process
@@ -468,6 +485,7 @@ __device__ __forceinline__ void points_stage(int stage, Lev<R>& L, Tend<R>& td, 
     aerosol_check(L, f, dt);
 
     // checks on temporaries (main:475-522)
+    TG_TRACE_PASS(L, 1);
     R xq = L.qc1d, xn = L.nc1d, xb;
     cloud_check(L, xq, xn, has_nc, ncsave, dt, odt);
     xq = L.qr1d;
@@ -489,6 +507,9 @@ __device__ __forceinline__ void points_stage(int stage, Lev<R>& L, Tend<R>& td, 
     L.qvten = L.qvten - I(td.prw_vcd);
     L.qcten = L.qcten + td.prw_vcd;
     L.ncten = L.ncten + td.pnc_wcd;
+    L.qcmag = L.qcmag + mag(td.prw_vcd);
+    L.ncmag = L.ncmag + mag(td.pnc_wcd);
+    TG_TRACE_PASS(L, 2);
     L.nwfaten = L.nwfaten - td.pnc_wcd;
     L.tten = L.tten + I(L.lvap) * L.ocp * td.prw_vcd;
     R xq = L.qc1d, xn = L.nc1d;
@@ -501,6 +522,9 @@ __device__ __forceinline__ void points_stage(int stage, Lev<R>& L, Tend<R>& td, 
     L.qrten = L.qrten - td.prv_rev;
     L.qvten = L.qvten + I(td.prv_rev);
     L.nrten = L.nrten - td.pnr_rev;
+    L.qrmag = L.qrmag + mag(td.prv_rev);
+    L.nrmag = L.nrmag + mag(td.pnr_rev);
+    TG_TRACE_PASS(L, 3);
     L.nwfaten = L.nwfaten + td.pnr_rev;
     L.tten = L.tten - I(L.lvap) * L.ocp * td.prv_rev;
     R xq = L.qr1d, xn = L.nr1d;
@@ -587,6 +611,9 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   Lev<R> L;
   L.cs = &cst;
   L.ci = &ci;
+#ifdef TEMPO_TRACE
+  L.tr = a.trace ? a.trace + ((long)c * nz + k) * kTracePoint : nullptr;
+#endif
   load_level(a, e, L, io);
   const R w = R(a.w[e]);
   R nwfa_in, nifa_in;
@@ -607,6 +634,7 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   const R ncsave_cond = has_nc ? R(nt_c_l) : ncsave;
   L.qcten = L.qiten = L.qrten = L.qsten = L.qgten = L.ngten = L.qbten = L.niten = L.nrten =
       L.ncten = R(0);
+  clear_mags(L);
 
   // thermo_vars runs after the initial checks and after each of the three stages
   // that follow (main:412, 524, 557, 585)
@@ -1120,8 +1148,19 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
   };
   [[maybe_unused]] const R odt_r = step_odt<R>(a);
   const bool p0 = part != 1, p1 = part != 0;
+  // decision trace of a test build: substep count j and top level 4 + j of species j
+  [[maybe_unused]] auto trace_col = [&](int j, int st, int kt) {
+#ifdef TEMPO_TRACE
+    if (a.trace) {
+      int* tc = a.trace + a.ncol * nz * kTracePoint + (long)a.act[s] * kTraceColumn;
+      if (j < 4) tc[j] = st;
+      tc[4 + j] = kt;
+    }
+#endif
+  };
   if (any_qr && p0) {
     fill(SR_VTR, SR_VTNR, true, false, steps, ktop);
+    trace_col(0, steps, ktop);
     if constexpr (SEMI) {
       steps = max((int)(steps / 10.0) + 1, 1);  // semi_sedi_factor (main:595, 599)
       sub[0] = steps;
@@ -1163,6 +1202,7 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
   }
   if (any_qg && p1) {
     fill(SR_VTG, SR_VTNG, false, false, steps, ktop);
+    trace_col(1, steps, ktop);
     if constexpr (SEMI) {
       const bool hail = a.flags & F_HAIL;
       steps = max((int)(steps / 10.0) + 1, 1);  // main:636, 640
@@ -1210,6 +1250,7 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
   }
   if (any_qs && p0) {
     fill(SR_VTSA, SR_VTSA, false, true, steps, ktop);
+    trace_col(2, steps, ktop);
     sub[2] = steps;
     const int fx[1] = {SD_XRS}, ft[1] = {SD_TQS}, fv[1] = {SR_VTSA};
     const double lim[1] = {r1};
@@ -1217,6 +1258,7 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
   }
   if (any_qi && p1) {
     fill(SR_VTI, SR_VTNI, false, false, steps, ktop);
+    trace_col(3, steps, ktop);
     sub[3] = steps;
     const int fx[2] = {SD_XRI, SD_XNI}, ft[2] = {SD_TQI, SD_TNI}, fv[2] = {SR_VTI, SR_VTNI};
     const double lim[2] = {r1, r2};
@@ -1235,6 +1277,7 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
       sr[SR_VTNC * fsd + (long)k * kSlotTile] = R(0);
     }
     sub[4] = 1;
+    trace_col(4, 1, kt);
     const int fx[2] = {SD_XRC, SD_XNC}, ft[2] = {SD_TQC, SD_TNC}, fv[2] = {SR_VTC, SR_VTNC};
     const double lim[2] = {r1, r2};
     sweep(Two{}, fx, ft, fv, lim, 1, kt, &prec_c);
@@ -1309,6 +1352,9 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
   Lev<R> L;
   L.cs = &cst;
   L.ci = &ci;
+#ifdef TEMPO_TRACE
+  L.tr = a.trace ? a.trace + ((long)a.act[s] * nz + k) * kTracePoint : nullptr;
+#endif
   L.t1d = (f & F_USE_T) ? io.template in<I>(a.t[e], C_T1D)
                         : io.template in<I>(a.th[e], C_T1D) * ldi<I>(a.pii + e);
   L.pres = R(a.p[e]);
@@ -1369,6 +1415,7 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
   else
     io.th(e, tnew / ldi<I>(a.pii + e));
   // final checks (main:750-781)
+  TG_TRACE_PASS(L, 4);
   cloud_check(L, L.qc1d, L.nc1d, has_nc, ncsave, dt, odt);
   rain_check(L, L.qr1d, L.nr1d, dt, odt);
   ice_check(L, L.qi1d, L.ni1d, dt, odt);

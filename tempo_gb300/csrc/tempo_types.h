@@ -30,6 +30,7 @@ struct Tables {
                       //   tcr_sacr1,tms_sacr1,tcr_sacr2,tms_sacr2,tnr_racs1,tnr_racs2,tnr_sacr1,tnr_sacr2
   const R* qrfz;      // [Fortran (i,j,k,m) flat][4]: tpi_qrfz,tni_qrfz,tpg_qrfz,tnr_qrfz
   const R* qcfz;      // [Fortran (i,j,k,m) flat][2]: tpi_qcfz,tni_qcfz
+  const double* edges;  // [kEdgesCount] least values of the log-index bins (tempo_consts.h)
 };
 
 enum : uint32_t {
@@ -117,7 +118,55 @@ struct StepArgs {
   // phase A's points in regime order: thread q takes level-major point ord[q] (point p
   // at level p / nact of slot p % nact); NULL = level-major order
   unsigned* ord;
+  // decision trace of a test build (TEMPO_TRACE): kTracePoint ints per (tile column,
+  // level) point, column c's level k at (c * nz + k) * kTracePoint, then kTraceColumn
+  // ints per tile column; NULL = off.  Product builds never write it.
+  int* trace;
 };
+
+// A multi-domain batch (tempo_run_batch_dev_f32_c): nd tiles, each with its own step
+// arguments (levels, dt, arrays, scratch), stepped by one sequence of launches.  Work
+// items are numbered across the batch: tile columns domain after domain (col_start), and,
+// after prep, active slots (slot_start) and level-major points (pt_start).
+constexpr int kMaxDomains = 256;
+template <class S>
+struct BatchArgs {
+  const StepArgs<S>* dom;  // [nd] each domain's step arguments (device copy)
+  const long* col_start;   // [nd + 1] first batch column of each domain
+  unsigned* slot_start;    // [nd + 1] first batch slot of each domain (written after prep)
+  unsigned* pt_start;      // [nd + 1] first batch point of each domain (written after prep)
+  unsigned* queue;         // work queue of the persistent points kernel (zeroed after prep)
+  unsigned* ord;           // batch points in regime order (NULL: domain by domain, level-major)
+  int nd;
+  long ncol;               // sum of the domains' tile columns
+  long npts_max;           // sum of the domains' columns x levels (grid bound of the point kernels)
+};
+
+// Layout of the decision trace (test builds compiled with TEMPO_TRACE).  The oracle
+// records the same layout, so a test compares every table index and branch decision
+// of a step with the oracle's.  Per point: the existence and limit bits of each pass of
+// the check routines (0 initial checks, 1 checks on temporaries after the rates, 2 the
+// cloud check after condensation, 3 the rain check after evaporation, 4 the final
+// checks), the table indices of each rate routine, the over-depletion limiter's
+// branches.  Per column: substep counts and top levels of the sedimentation.
+enum TraceSlot : int {
+  TR_CHECK = 0,   // + pass (0..4): TraceCheckBit | idx_bg << 12 | nu_c << 16
+  TR_RW = 5,      // warm_rain: efrw rain bin | int(mvd_c 1e6) << 8 | branch bits << 16
+  TR_RS = 6,      // rain-snow: idx_s | idx_t << 6 | idx_r1 << 12 | idx_r << 18 | taken << 24
+  TR_RG = 7,      // rain-graupel: idx_g1 | idx_g << 6 | idx_r1 << 12 | idx_r << 18 | taken << 24
+  TR_FZR = 8,     // rain freezing: idx_r | idx_r1 << 6 | idx_tc << 12 | idx_in << 18 | taken << 24
+  TR_FZC = 9,     // cloud freezing: idx_c | idx_n << 8 | taken << 16
+  TR_ICE = 10,    // ice_processes: idx_i | idx_i1 << 8 | taken << 16
+  TR_RIME = 11,   // riming: efsw snow bin | int(mvd_c 1e6) << 8 | taken << 16
+  TR_EVAP = 12,   // droplet evaporation: idx_d | idx_c << 8 | idx_n << 16 | taken << 24
+  TR_LIMIT = 13,  // check_over_depletion: one bit per rescaled group
+  kTracePoint = 16
+};
+enum TraceCheckBit : int {
+  TB_QC = 1, TB_QC_HIT = 2, TB_QR = 4, TB_QR_HIT = 8, TB_QI = 16, TB_QI_HIT = 32,
+  TB_QS = 64, TB_QG = 128, TB_QG_HIT = 256
+};
+constexpr int kTraceColumn = 10;  // substeps rain, graupel, snow, ice; ktop rain, graupel, snow, ice, cloud; spare
 // regimes of a point (tempo_step.cuh: point_regime)
 constexpr int kRegimes = 64;
 // size of the cloud-number network: scaler means and variances (7 + 7), weights00
