@@ -415,8 +415,13 @@ def precision_study(tg, W, torch, device, ncol_side=512):
             a, b = A[k][np.broadcast_to(m, A[k].shape)], B[k][np.broadcast_to(m, B[k].shape)]
             d = np.abs(a - b)
             e = d / np.maximum(np.abs(b), fl)
+            # the same with the floor at 1e-7 of the field's largest value (the FP32
+            # resolution of the field's scale)
+            es = d / np.maximum(np.abs(b), 1e-7 * max(np.abs(b).max(), 1e-300))
             out[k] = {"max": float(e.max()), "rms": float(np.sqrt((e * e).mean())),
                       "frac_gt_1e-5": float((e > 1e-5).mean()),
+                      "max_scaled_floor": float(es.max()),
+                      "frac_scaled_floor_gt_1e-5": float((es > 1e-5).mean()),
                       "normwise": float(d.max() / max(np.abs(b).max(), 1e-300)),
                       "rel_rms": float(np.sqrt((d * d).sum() / max((b * b).sum(), 1e-300)))}
         a, b = A["refl10cm"], B["refl10cm"]
