@@ -50,6 +50,22 @@ constexpr long QCFZ_COUNT = (long)ntb_c * nbc * ntb_t1 * ntb_in;
 constexpr long QRFZ_COUNT = (long)ntb_r * ntb_r1 * ntb_t1 * ntb_in;
 constexpr long CCN_COUNT = (long)ntb_arc * ntb_arw * ntb_art * ntb_arr * ntb_ark;
 
+// real ** integer as the reference's compiled code evaluates it (binary powering, a
+// reciprocal for negative exponents); host and device share it
+template <class T>
+TG_HD inline T ipow_binary(T x, int m) {
+  unsigned n = m < 0 ? -(unsigned)m : (unsigned)m;
+  T y = (n % 2) ? x : T(1);
+  while (n >>= 1) {
+    x = x * x;
+    if (n % 2) y = y * x;
+  }
+  return m < 0 ? T(1) / y : y;
+}
+// 10**m for the decade searches of the table indices, every m a finite positive float's
+// decade can take; other m fall back to the powering
+constexpr int kP10Min = -46, kP10Max = 39, kP10Count = kP10Max - kP10Min + 1;
+
 // ---- run-time derived values (params:411-658, utils) ----
 template <class R>
 struct TempoConsts {
@@ -73,6 +89,14 @@ struct TempoConsts {
   R hbins[nhbins], dhbins[nhbins];
   R ta_na[ntb_arc], ta_ww[ntb_arw], ta_tk[ntb_art];
   R sa[10], sb[10];
+  // powers of constants that the reference evaluates at every use, computed once here
+  // with the same expression (host libm): (crg(3) org2 org1)**bm_r (main:2546),
+  // (cgg(3,1) ogg2 ogg1)**bm_g (main:2579) and **obmg (main:1207),
+  // (ccg(3,nu) ocg2(nu))**obmr (main:2318), and the Cunningham slip correction of the
+  // two aerosol diameters (aerosols:106; 0 = 0.04 um, 1 = 0.8 um)
+  R rain_n0_k, graupel_n0_k, graupel_lam_k, dc_g_k[15], aer_cc[2];
+  // ipow_binary(R(10), m) in R's own arithmetic, m = kP10Min..kP10Max
+  R p10[kP10Count];
 };
 
 // Fills a double-precision constant set exactly as tempo_init does for the given

@@ -9,8 +9,10 @@
 // the FP32 pipes.  The algorithms are the classical error-free transformations:
 // Knuth's TwoSum, Dekker's Fast2Sum, and the FMA form of Dekker's TwoProduct, combined
 // as in the double-double arithmetic of Hida, Li and Bailey (QD library, 2001) with
-// accurate (cancellation-safe) addition.  Relative error of + - * / is a few units
-// of 2^-48.
+// accurate (cancellation-safe) addition, and the division algorithms of Joldes, Muller
+// and Popescu ("Tight and rigorous error bounds for basic building blocks of
+// double-word arithmetic", ACM TOMS 44(2), 2017).  Relative error of + - * is a few
+// units of 2^-48 (u^2, u = 2^-24), of / at most 15 u^2.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -96,18 +98,33 @@ __host__ __device__ __forceinline__ df operator*(df a, float b) {
 }
 __host__ __device__ __forceinline__ df operator*(float a, df b) { return b * a; }
 
-// long division with two correction steps (QD's accurate division)
-__host__ __device__ __forceinline__ df operator/(df a, df b) {
-  float q1 = a.hi / b.hi;
-  df r = a - b * q1;
-  float q2 = r.hi / b.hi;
-  r = r - b * q2;
-  float q3 = r.hi / b.hi;
+// Division, DWDivDW2 of Joldes, Muller and Popescu (2017): one float quotient th, the
+// remainder x - y th (y th as a double-word by DWTimesFP3; xh - rh is exact), one
+// correction tl = remainder / yh.  Relative error at most 15 u^2 + 56 u^3.
+__host__ __device__ __forceinline__ df operator/(df x, df y) {
+  const float th = x.hi / y.hi;
+  float rh, rl;
+  dfo::two_prod(y.hi, th, rh, rl);
+  rl = fmaf(y.lo, th, rl);
+  dfo::fast_two_sum(rh, rl, rh, rl);
+  const float ph = x.hi - rh;
+  const float dl = x.lo - rl;
+  const float tl = (ph + dl) / y.hi;
   float h, l;
-  dfo::fast_two_sum(q1, q2, h, l);
-  return df(h, l) + q3;
+  dfo::fast_two_sum(th, tl, h, l);
+  return df(h, l);
 }
-__host__ __device__ __forceinline__ df operator/(df a, float b) { return a / df(b); }
+// double-word by float, DWDivFP3 of the same paper: relative error at most 3 u^2
+__host__ __device__ __forceinline__ df operator/(df x, float y) {
+  const float th = x.hi / y;
+  float ph, pl;
+  dfo::two_prod(th, y, ph, pl);
+  const float d = ((x.hi - ph) - pl) + x.lo;
+  const float tl = d / y;
+  float h, l;
+  dfo::fast_two_sum(th, tl, h, l);
+  return df(h, l);
+}
 __host__ __device__ __forceinline__ df operator/(float a, df b) { return df(a) / b; }
 
 // double operands (constants): converted to df, never narrowed to float
@@ -122,6 +139,21 @@ __host__ __device__ __forceinline__ df operator/(double a, df b) { return df(a) 
 
 __host__ __device__ __forceinline__ df& operator+=(df& a, df b) { return a = a + b; }
 __host__ __device__ __forceinline__ df& operator-=(df& a, df b) { return a = a - b; }
+
+// c + x s for one Horner step of a polynomial: the sum by the sloppy double-word
+// addition (QD's sloppy_add; SloppyDWPlusDW of Joldes, Muller and Popescu), whose
+// absolute error is a few u^2 (|c| + |x s|).  Horner's own error is of that form
+// (u^2 times the sum of the terms' magnitudes) whatever the addition, so the accurate
+// addition buys nothing here.
+__host__ __device__ __forceinline__ df horner_step(df x, df s, double c) {
+  const df p = x * s, a(c);
+  float sh, sl;
+  dfo::two_sum(a.hi, p.hi, sh, sl);
+  const float w = sl + (a.lo + p.lo);
+  float h, l;
+  dfo::fast_two_sum(sh, w, h, l);
+  return df(h, l);
+}
 
 // comparisons on the represented value (hi and lo are normalised: |lo| <= ulp(hi)/2)
 __host__ __device__ __forceinline__ bool operator<(df a, df b) {

@@ -246,6 +246,15 @@ void make_consts(TempoConsts<double>* c, bool hailaware) {
                          0.060366, 0.000079,  0.000594, 0.,       -0.003577};
   std::memcpy(c->sa, sa, sizeof sa);
   std::memcpy(c->sb, sb, sizeof sb);
+  c->rain_n0_k = std::pow(c->crg[2] * c->org2 * c->org1, bm_r);
+  c->graupel_n0_k = std::pow(c->cgg[0][2] * c->ogg2 * c->ogg1, bm_g);
+  c->graupel_lam_k = std::pow(c->cgg[0][2] * c->ogg2 * c->ogg1, c->obmg);
+  for (int nu = 1; nu <= 15; nu++)
+    c->dc_g_k[nu - 1] = std::pow(c->ccg[nu - 1][2] * c->ocg2[nu - 1], c->obmr);
+  const double meanpath = 0.0256e-6, da[2] = {0.04e-6, 0.8e-6};
+  for (int i = 0; i < 2; i++)
+    c->aer_cc[i] = 1.0 + 2.0 * meanpath / da[i] * (1.257 + 0.4 * std::exp(-(0.55 * da[i] / meanpath)));
+  for (int m = kP10Min; m <= kP10Max; m++) c->p10[m - kP10Min] = ipow_binary(10.0, m);
 }
 
 void narrow_consts(const TempoConsts<double>& d, TempoConsts<float>* f) {
@@ -268,8 +277,12 @@ void narrow_consts(const TempoConsts<double>& d, TempoConsts<float>* f) {
   NAR(t2_qr_ev); NAR(t1_qs_sd); NAR(t2_qs_sd); NAR(t1_qs_me); NAR(t2_qs_me); NAR(t1_qg_sd);
   NAR(t1_qg_me); NAR(nic1);
   NAR(dr1); NAR(drn); NAR(ds1); NAR(dsn); NAR(t_nc1); NAR(r_c1); NAR(r_r1); NAR(r_s1);
-  NAR(r_g1); NAR(nt_in1); NARA(hbins); NARA(dhbins); NARA(ta_na); NARA(ta_ww); NARA(ta_tk);
+  NAR(r_g1); NAR(nt_in1); NAR(rain_n0_k); NAR(graupel_n0_k); NAR(graupel_lam_k);
+  NARA(dc_g_k); NARA(aer_cc); NARA(hbins); NARA(dhbins); NARA(ta_na); NARA(ta_ww); NARA(ta_tk);
   NARA(sa); NARA(sb);
+  // powers of ten in float arithmetic (not narrowed doubles): the mixed form's decade
+  // searches divide by exactly what the float powering gives
+  for (int m = kP10Min; m <= kP10Max; m++) f->p10[m - kP10Min] = ipow_binary(10.0f, m);
 #undef NAR
 #undef NARA
 #undef NAR2

@@ -55,6 +55,10 @@ __device__ __forceinline__ double Fabs(double x) { return fabs(x); }
 __device__ __forceinline__ float Fabs(float x) { return fabsf(x); }
 __device__ __forceinline__ double Copysign(double a, double b) { return copysign(a, b); }
 __device__ __forceinline__ float Copysign(float a, float b) { return copysignf(a, b); }
+// 10**x: the FP64 drop-in keeps the reference's pow(10, x); the mixed form calls the
+// library's exp10f (its documented error bound is below powf's)
+__device__ __forceinline__ double Pow10(double x) { return pow(10.0, x); }
+__device__ __forceinline__ float Pow10(float x) { return exp10f(x); }
 
 // the same functions on dual numbers: values through the scalar functions above (so
 // the value part matches the plain kernels), derivatives by the chain rule
@@ -78,6 +82,9 @@ template <class T, int N, class U, class = typename std::enable_if<std::is_arith
 __device__ __forceinline__ Dual<T, N> Pow(U a, const Dual<T, N>& b) {
   const T r = Pow(T(a), b.v);
   return dual_chain(b, r, (T(a) > T(0)) ? r * Log(T(a)) : T(0));
+}
+template <class T, int N> __device__ __forceinline__ Dual<T, N> Pow10(const Dual<T, N>& b) {
+  return Pow(T(10.0), b);
 }
 template <class T, int N> __device__ __forceinline__ Dual<T, N> Exp(const Dual<T, N>& a) {
   const T r = Exp(a.v);
@@ -116,15 +123,7 @@ template <class T> __device__ __forceinline__ int Int(T x) { return (int)x; }
 template <class T, int N> __device__ __forceinline__ int Nint(const Dual<T, N>& x) { return Nint(x.v); }
 template <class T, int N> __device__ __forceinline__ int Int(const Dual<T, N>& x) { return Int(x.v); }
 // real ** integer: binary powering with a reciprocal for negative exponents
-template <class T> __device__ __forceinline__ T Ipow(T x, int m) {
-  unsigned n = m < 0 ? -(unsigned)m : (unsigned)m;
-  T y = (n % 2) ? x : T(1);
-  while (n >>= 1) {
-    x = x * x;
-    if (n % 2) y = y * x;
-  }
-  return m < 0 ? T(1) / y : y;
-}
+template <class T> __device__ __forceinline__ T Ipow(T x, int m) { return ipow_binary(x, m); }
 
 // ---------------------------------------------------------------------------------
 // constants and tables
@@ -149,6 +148,16 @@ struct Lev {
   R rc, nc, rr, nr, ri, ni, rs, rg, ng, rb, nwfa, nifa;
   R ilamc, ilami, ilamr, ilamg, mvd_c, mvd_r, mvd_g;
   R smob, smoc, smo0, smo1, smo2, smoe, smof, smog, smoz;
+  // rain table indices of the process rates (get_rain_table_index, main:2526-2555),
+  // which three rate routines use with the same rain state: formed at the first use
+  // (0 = not yet)
+  mutable int rain_idx = 0, rain_idx1 = 0;
+  // size-distribution powers that several rate routines form from the same rain and
+  // graupel state (graupel intercept and the 9th collection power, rain intercept and
+  // the 9th collection power): formed at the first use (bits of psd_have); the rate
+  // stage drops them and the rain indices when it ends, before the state changes
+  mutable R psd_n0g, psd_pg9, psd_n0r, psd_pf9;
+  mutable int psd_have = 0;
   // thermodynamic island
   I t1d, qv1d, temp, qv, rho, qvs, qvsi, delqvs, ssatw, ssati, tten, qvten;
   I qvs_t0;  // calc_rslf(p, t0): pressure is fixed through the step, so once per level
@@ -173,11 +182,21 @@ struct Lev {
     if ((L).tr) (L).tr[(slot)] |= (int)(bits);     \
   } while (0)
 #define TG_TRACE_PASS(L, p) ((L).tpass = (p))
+// index v of a table read must lie in [lo, hi]: outside, the site's bit goes to the
+// point's TR_RANGE slot and v is clamped, so the read stays inside the table
+#define TG_RANGE(L, site, v, lo, hi)                 \
+  do {                                               \
+    if ((v) < (lo) || (v) > (hi)) {                  \
+      if ((L).tr) (L).tr[TR_RANGE] |= (int)(site);   \
+      (v) = (v) < (lo) ? (lo) : (hi);                \
+    }                                                \
+  } while (0)
 #else
 #define TG_TRACE(L, slot, bits) \
   do {                          \
   } while (0)
 #define TG_TRACE_PASS(L, p) ((void)0)
+#define TG_RANGE(L, site, v, lo, hi) ((void)0)
 #endif
 
 // process rates (ty_tend, main:47-64)
@@ -209,28 +228,28 @@ template <class R> __device__ __forceinline__ R rho_g(int m) { return R(rho_gd(m
 // ---------------------------------------------------------------------------------
 // utils.F90
 // ---------------------------------------------------------------------------------
+// One Horner step c + x s in the island type (the double-float form has its own,
+// tempo_dfloat.cuh), and the nested polynomial c0 + x (c1 + x (c2 + ...)) in the
+// reference's order.
+template <class I> __device__ __forceinline__ I horner_step(I x, I s, double c) { return c + x * s; }
+template <class I> __device__ __forceinline__ I horner(I, double c) { return I(c); }
+template <class I, class... Cs>
+__device__ __forceinline__ I horner(I x, double c, Cs... cs) {
+  return horner_step(x, horner(x, cs...), c);
+}
+
 // calc_rslf / calc_rsif (utils:285-331) in the island type
 template <class I> __device__ __forceinline__ I calc_rslf(I p, I t) {
   I x = Max(I(-80.0), t - 273.16);
-  I esl = .611583699E03 +
-          x * (.444606896E02 +
-               x * (.143177157e01 +
-                    x * (.264224321e-1 +
-                         x * (.299291081e-3 +
-                              x * (.203154182e-5 +
-                                   x * (.702620698e-8 + x * (.379534310e-11 + x * -.321582393e-13)))))));
+  I esl = horner(x, .611583699E03, .444606896E02, .143177157e01, .264224321e-1, .299291081e-3,
+                 .203154182e-5, .702620698e-8, .379534310e-11, -.321582393e-13);
   esl = Min(esl, p * 0.15);
   return .622 * esl / (p - esl);
 }
 template <class I> __device__ __forceinline__ I calc_rsif(I p, I t) {
   I x = Max(I(-80.0), t - 273.16);
-  I esi = .609868993e03 +
-          x * (.499320233e02 +
-               x * (.184672631e01 +
-                    x * (.402737184e-1 +
-                         x * (.565392987e-3 +
-                              x * (.521693933e-5 +
-                                   x * (.307839583e-7 + x * (.105785160e-9 + x * .161444444e-12)))))));
+  I esi = horner(x, .609868993e03, .499320233e02, .184672631e01, .402737184e-1, .565392987e-3,
+                 .521693933e-5, .307839583e-7, .105785160e-9, .161444444e-12);
   esi = Min(esi, p * 0.15);
   return .622 * esi / Max(I(1.e-4), (p - esi));
 }
@@ -256,42 +275,42 @@ __device__ void snow_moments(Lev<R>& L, R tc, int which) {
   R loga_, a_, b_, smo2_;
   L.smob = L.rs * c.oams;
   loga_ = poly_a(c.sa, tc, R(bm_s));
-  a_ = Pow(R(10.0), loga_);
+  a_ = Pow10(loga_);
   b_ = poly_a(c.sb, tc, R(bm_s));
   smo2_ = Pow(L.smob / a_, R(1.0) / b_);
   L.smo2 = smo2_;
   loga_ = poly_a(c.sa, tc, c.cse[0]);
-  a_ = Pow(R(10.0), loga_);
+  a_ = Pow10(loga_);
   b_ = poly_a(c.sb, tc, c.cse[0]);
   L.smoc = a_ * Pow(smo2_, b_);
   if (which == 1) {
     const auto* sa = c.sa;
     const auto* sb = c.sb;
     loga_ = sa[0] + sa[1] * tc + sa[4] * tc * tc + sa[8] * tc * tc * tc;
-    a_ = Pow(R(10.0), loga_);
+    a_ = Pow10(loga_);
     b_ = sb[0] + sb[1] * tc + sb[4] * tc * tc + sb[8] * tc * tc * tc;
     L.smo0 = a_ * Pow(smo2_, b_);
     loga_ = sa[0] + sa[1] * tc + sa[2] + sa[3] * tc + sa[4] * tc * tc + sa[5] + sa[6] * tc * tc +
             sa[7] * tc + sa[8] * tc * tc * tc + sa[9];
-    a_ = Pow(R(10.0), loga_);
+    a_ = Pow10(loga_);
     b_ = sb[0] + sb[1] * tc + sb[2] + sb[3] * tc + sb[4] * tc * tc + sb[5] + sb[6] * tc * tc +
          sb[7] * tc + sb[8] * tc * tc * tc + sb[9];
     L.smo1 = a_ * Pow(smo2_, b_);
     loga_ = poly_a(sa, tc, c.cse[12]);
-    a_ = Pow(R(10.0), loga_);
+    a_ = Pow10(loga_);
     b_ = poly_a(sb, tc, c.cse[12]);
     L.smoe = a_ * Pow(smo2_, b_);
     loga_ = poly_a(sa, tc, c.cse[15]);
-    a_ = Pow(R(10.0), loga_);
+    a_ = Pow10(loga_);
     b_ = poly_a(sb, tc, c.cse[15]);
     L.smof = a_ * Pow(smo2_, b_);
     loga_ = poly_a(sa, tc, c.cse[16]);
-    a_ = Pow(R(10.0), loga_);
+    a_ = Pow10(loga_);
     b_ = poly_a(sb, tc, c.cse[16]);
     L.smog = a_ * Pow(smo2_, b_);
   } else if (which == 2) {
     loga_ = poly_a(c.sa, tc, c.cse[2]);
-    a_ = Pow(R(10.0), loga_);
+    a_ = Pow10(loga_);
     b_ = poly_a(c.sb, tc, c.cse[2]);
     L.smoz = a_ * Pow(smo2_, b_);
   }
@@ -591,9 +610,9 @@ __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R od
       L.idx_bg = idx_bg1;
       R ygra1 = Log10(Max(R(1.e-9), L.rg));
       R zans1 = R(3.4) + R(2.0 / 7.0) * (ygra1 + R(8.0));
-      R n0_exp = Max(R(gonv_min), Min(Pow(R(10.0), zans1), R(gonv_max)));
+      R n0_exp = Max(R(gonv_min), Min(Pow10(zans1), R(gonv_max)));
       R lam_exp = Pow(n0_exp * c.am_g[idx_bg1 - 1] * c.cgg[0][0] / L.rg, c.oge1);
-      lamg = lam_exp * Pow(c.cgg[0][2] * c.ogg2 * c.ogg1, c.obmg);
+      lamg = lam_exp * c.graupel_lam_k;
       L.ng = c.cgg[0][1] * c.ogg3 * L.rg * Pow(lamg, R(bm_g)) / c.am_g[idx_bg1 - 1];
       L.rb = R(meters3_to_liters) * L.rg / rho_g<R>(idx_bg1);
     }

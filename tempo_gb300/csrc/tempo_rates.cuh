@@ -12,16 +12,22 @@ namespace tg {
 // table indices
 // ---------------------------------------------------------------------------------
 // decade search shared by get_*_table_index: find n with 1 <= x/10**n < 10 among
-// nint(log10(x)) + {-1, 0, +1}, then the linear bin index (main:2501-2507)
-template <class R>
-__device__ __forceinline__ int decade_index(R x, int n2, int nmax) {
+// nint(log10(x)) + {-1, 0, +1}, then the linear bin index (main:2501-2507); 10**n from
+// the constant set's table (the same values as the powering)
+template <class C, class R>
+__device__ __forceinline__ R pow10_of(const TempoConsts<C>& c, int m) {
+  return (m >= kP10Min && m <= kP10Max) ? R(c.p10[m - kP10Min]) : Ipow(R(10.0), m);
+}
+template <class C, class R>
+__device__ __forceinline__ int decade_index(const TempoConsts<C>& c, R x, int n2, int nmax) {
   int nx = Nint(Log10(x)), n = 0;
+  R q = R(0.0);
   for (int nn = nx - 1; nn <= nx + 1; nn++) {
     n = nn;
-    R q = x / Ipow(R(10.0), nn);
+    q = x / pow10_of<C, R>(c, nn);
     if (q >= R(1.0) && q < R(10.0)) break;
   }
-  int idx = Int(x / Ipow(R(10.0), n)) + 10 * (n - n2) - (n - n2);
+  int idx = Int(q) + 10 * (n - n2) - (n - n2);
   return max(1, min(idx, nmax));
 }
 template <class R> __device__ __forceinline__ int temperature_index(Isl<R> tempk) {  // main:2511-2523
@@ -32,19 +38,58 @@ template <class R> __device__ __forceinline__ int temperature_index(Isl<R> tempk
 }
 template <class C, class R>
 __device__ __forceinline__ void rain_index(const TempoConsts<C>& c, R rr, R ilamr, int& idx_r, int& idx_r1) {  // :2526-2555
-  idx_r = decade_index(rr, c.nir2, ntb_r);
+  idx_r = decade_index(c, rr, c.nir2, ntb_r);
   R lamr = R(1.) / ilamr;
-  R lam_exp = lamr * Pow(c.crg[2] * c.org2 * c.org1, R(bm_r));
+  R lam_exp = lamr * c.rain_n0_k;
   R n0_exp = c.org1 * rr / c.am_r * Pow(lam_exp, c.cre[0]);
-  idx_r1 = decade_index(n0_exp, c.nir3, ntb_r1);
+  idx_r1 = decade_index(c, n0_exp, c.nir3, ntb_r1);
+}
+// graupel intercept ng ogg2 lamg**cge(2,1) and ilamg**cge(9,idx_bg) (main:2458-2462,
+// 3002, 3074, 3180-3188), and rain intercept nr org2 lamr**cre(2) and
+// (lamr + fv_r)**(-cre(9)) with lamr = 1/ilamr (main:2970-2975, 3148-3156), once per
+// level and rate stage
+template <class R>
+__device__ __forceinline__ R graupel_n0(const Lev<R>& L) {
+  if (!(L.psd_have & 1)) {
+    L.psd_n0g = L.ng * L.cs->ogg2 * Pow(R(1.0) / L.ilamg, L.cs->cge[0][1]);
+    L.psd_have |= 1;
+  }
+  return L.psd_n0g;
+}
+template <class R>
+__device__ __forceinline__ R graupel_pg9(const Lev<R>& L) {
+  if (!(L.psd_have & 2)) {
+    L.psd_pg9 = Pow(L.ilamg, L.cs->cge[L.idx_bg - 1][8]);
+    L.psd_have |= 2;
+  }
+  return L.psd_pg9;
+}
+template <class R>
+__device__ __forceinline__ void rain_n0_pf9(const Lev<R>& L, R& n0_r, R& pf9) {
+  if (!(L.psd_have & 4)) {
+    const R lamr = R(1.0) / L.ilamr;
+    L.psd_n0r = L.nr * L.cs->org2 * Pow(lamr, L.cs->cre[1]);
+    L.psd_pf9 = Pow(lamr + R(fv_r), -L.cs->cre[8]);
+    L.psd_have |= 4;
+  }
+  n0_r = L.psd_n0r;
+  pf9 = L.psd_pf9;
+}
+
+// rain_index of the level's rain state (L.rr, L.ilamr), formed once per level
+template <class R>
+__device__ __forceinline__ void level_rain_index(const Lev<R>& L, int& idx_r, int& idx_r1) {
+  if (L.rain_idx == 0) rain_index(*L.cs, L.rr, L.ilamr, L.rain_idx, L.rain_idx1);
+  idx_r = L.rain_idx;
+  idx_r1 = L.rain_idx1;
 }
 template <class C, class R>
 __device__ __forceinline__ void graupel_index(const TempoConsts<C>& c, R rg, R ilamg, int idx, int& idx_g, int& idx_g1) {  // main:2558-2588
-  idx_g = decade_index(rg, c.nig2, ntb_g);
+  idx_g = decade_index(c, rg, c.nig2, ntb_g);
   R lamg = R(1.) / ilamg;
-  R lam_exp = lamg * Pow(c.cgg[0][2] * c.ogg2 * c.ogg1, R(bm_g));
+  R lam_exp = lamg * c.graupel_n0_k;
   R n0_exp = c.ogg1 * rg / c.am_g[idx - 1] * Pow(lam_exp, c.cge[0][0]);
-  idx_g1 = decade_index(n0_exp, c.nig3, ntb_g1);
+  idx_g1 = decade_index(c, n0_exp, c.nig3, ntb_g1);
 }
 // The bin of a value whose reference index is a non-decreasing function of it built on
 // libm's log (main:2341, 2391, 2607).  `guess` is that function in this device's
@@ -64,7 +109,7 @@ __device__ __forceinline__ int edge_index(const double* e, int n, double x, int 
 template <class C, class R>
 __device__ __forceinline__ void cloud_index(const TempoConsts<C>& c, const double* edges, R rc, R nc,
                                             int& idx_c, int& idx_n) {  // :2591-2609
-  idx_c = decade_index(rc, c.nic2, ntb_c);
+  idx_c = decade_index(c, rc, c.nic2, ntb_c);
   int in = Nint(R(1.0) + R(nbc) * Log(nc / c.t_nc1) / c.nic1);
   idx_n = edge_index(edges + kEdgesN, nbc, edge_arg(nc), in);
 }
@@ -89,7 +134,7 @@ __device__ void warm_rain(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, 
       int nu_c = get_nuc(L.nc);
       R lamc = R(1.0) / L.ilamc;
       R xdc = Max(R(d0c) * R(1.e6), (Pow(L.rc / (c.am_r * L.nc), c.obmr)) * R(1.e6));
-      R dc_g = (Pow(c.ccg[nu_c - 1][2] * c.ocg2[nu_c - 1], c.obmr) / lamc) * R(1.e6);
+      R dc_g = (c.dc_g_k[nu_c - 1] / lamc) * R(1.e6);
       R dc_b = Pow(xdc * xdc * xdc * dc_g * dc_g * dc_g - xdc * xdc * xdc * xdc * xdc * xdc,
                    R(1.0) / R(6.0));
       R zeta1 = R(0.5) * ((R(6.25e-6) * xdc * dc_b * dc_b * dc_b - R(0.4)) +
@@ -108,8 +153,11 @@ __device__ void warm_rain(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, 
       R lamr = (R(3.0) + R(mu_r) + R(0.672)) / L.mvd_r;
       int idx = 1 + Int(R(nbr) * Log(L.mvd_r / c.dr1) / Log(c.drn / c.dr1));
       idx = edge_index(T.edges + kEdgesR, nbr, edge_arg(L.mvd_r), idx);
-      TG_TRACE(L, TR_RW, idx | (Int(L.mvd_c * R(1.e6)) << 8) | (1 << 18));
-      R ef_rw = ld(T.t_efrw + (idx - 1) + (long)(Int(L.mvd_c * R(1.e6)) - 1) * nbr);
+      int mc = Int(L.mvd_c * R(1.e6));
+      TG_TRACE(L, TR_RW, idx | (mc << 8) | (1 << 18));
+      TG_RANGE(L, RG_EFRW, idx, 1, nbr);
+      TG_RANGE(L, RG_EFRW, mc, 1, nbc);
+      R ef_rw = ld(T.t_efrw + (idx - 1) + (long)(mc - 1) * nbr);
       R n0_r = L.nr * c.org2 * Pow(lamr, c.cre[1]);
       t.prr_rcw = L.rhof * c.t1_qr_qc * ef_rw * L.rc * n0_r * Pow(lamr + R(fv_r), -c.cre[8]);
       t.prr_rcw = Min(L.rc * odt, t.prr_rcw);
@@ -126,9 +174,13 @@ __device__ void rain_snow_rain_graupel(const Lev<R>& L, Tend<R>& t, const Tables
   if (L.l_qr && L.l_qs) {
     if (L.rr >= c.r_r1 && L.rs >= c.r_s1) {
       int idx_t = temperature_index<R>(L.temp), idx_r, idx_r1;
-      rain_index(c, L.rr, L.ilamr, idx_r, idx_r1);
-      int idx_s = decade_index(L.rs, c.nis2, ntb_s);
+      level_rain_index(L, idx_r, idx_r1);
+      int idx_s = decade_index(c, L.rs, c.nis2, ntb_s);
       TG_TRACE(L, TR_RS, idx_s | (idx_t << 6) | (idx_r1 << 12) | (idx_r << 18) | (1 << 24));
+      TG_RANGE(L, RG_QS, idx_s, 1, ntb_s);
+      TG_RANGE(L, RG_QS, idx_t, 1, ntb_t);
+      TG_RANGE(L, RG_QS, idx_r1, 1, ntb_r1);
+      TG_RANGE(L, RG_QS, idx_r, 1, ntb_r);
       const Cst<R>* e = T.qs + 12L * ((idx_s - 1) + (long)(idx_t - 1) * ntb_s +
                                  (long)(idx_r1 - 1) * ntb_s * ntb_t +
                                  (long)(idx_r - 1) * ntb_s * ntb_t * ntb_r1);
@@ -155,11 +207,16 @@ __device__ void rain_snow_rain_graupel(const Lev<R>& L, Tend<R>& t, const Tables
   }
   if (L.l_qr && L.l_qg) {
     if (L.rr >= c.r_r1 && L.rg >= c.r_g1) {
-      const int ig = L.idx_bg;
+      int ig = L.idx_bg;
       int idx_r, idx_r1, idx_g, idx_g1;
-      rain_index(c, L.rr, L.ilamr, idx_r, idx_r1);
+      level_rain_index(L, idx_r, idx_r1);
       graupel_index(c, L.rg, L.ilamg, ig, idx_g, idx_g1);
       TG_TRACE(L, TR_RG, idx_g1 | (idx_g << 6) | (idx_r1 << 12) | (idx_r << 18) | (1 << 24));
+      TG_RANGE(L, RG_QG, idx_g1, 1, ntb_g1);
+      TG_RANGE(L, RG_QG, idx_g, 1, ntb_g);
+      TG_RANGE(L, RG_QG, ig, 1, nrhg);
+      TG_RANGE(L, RG_QG, idx_r1, 1, ntb_r1);
+      TG_RANGE(L, RG_QG, idx_r, 1, ntb_r);
       const Cst<R>* e = T.qg + 5L * ((idx_g1 - 1) + (long)(idx_g - 1) * ntb_g1 +
                                 (long)(ig - 1) * ntb_g1 * ntb_g +
                                 (long)(idx_r1 - 1) * ntb_g1 * ntb_g * nrhg +
@@ -203,7 +260,7 @@ __device__ __forceinline__ R koop_nucleation(const TempoConsts<C>& c, R temp, R 
   R log_j_rate = R(-906.7) + (R(8502.0) * delta_aw) - (R(26924.0) * delta_aw * delta_aw) +
                  (R(29180.0) * delta_aw * delta_aw * delta_aw);
   log_j_rate = Min(R(20.0), log_j_rate);
-  R j_rate = Pow(R(10.0), log_j_rate);
+  R j_rate = Pow10(log_j_rate);
   R prob_h = Min(R(1.0) - Exp(-j_rate * c.ar_volume * dt), R(1.0));
   if (prob_h > R(0.0)) xni = Min(prob_h * naero, R(1000.e3));
   return Max(R(0.0), xni);
@@ -220,15 +277,21 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
   R rate_max = R((L.qv - L.qvsi) * L.rho) * odt * R(0.999);
   R rho = R(L.rho);
   R xni, xnc;
+  // DeMott's number (main:2754 and :2798, the same arguments): evaluated once
+  const R xni_demott = (f & F_NIFA) ? demott_nucleation(c, tempc, rho, L.nifa) : R(0.0);
   if (f & F_NIFA)
-    xni = demott_nucleation(c, tempc, rho, L.nifa);
+    xni = xni_demott;
   else
     xni = R(1.0) * R(1000.0);
-  int idx_in = (xni > c.nt_in1) ? decade_index(xni, c.niin2, ntb_in) : 1;
+  int idx_in = (xni > c.nt_in1) ? decade_index(c, xni, c.niin2, ntb_in) : 1;
   if (L.rr > c.r_r1) {
     int idx_r, idx_r1;
-    rain_index(c, L.rr, L.ilamr, idx_r, idx_r1);
+    level_rain_index(L, idx_r, idx_r1);
     TG_TRACE(L, TR_FZR, idx_r | (idx_r1 << 6) | (idx_tc << 12) | (idx_in << 18) | (1 << 24));
+    TG_RANGE(L, RG_QRFZ, idx_r, 1, ntb_r);
+    TG_RANGE(L, RG_QRFZ, idx_r1, 1, ntb_r1);
+    TG_RANGE(L, RG_QRFZ, idx_tc, 1, ntb_t1);
+    TG_RANGE(L, RG_QRFZ, idx_in, 1, ntb_in);
     const Cst<R>* e = T.qrfz + 4L * ((idx_r - 1) + (long)(idx_r1 - 1) * ntb_r +
                                 (long)(idx_tc - 1) * ntb_r * ntb_r1 +
                                 (long)(idx_in - 1) * ntb_r * ntb_r1 * ntb_t1);
@@ -238,7 +301,7 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
     t.pnr_rfz = ld(e + 3) * odt;
     t.prg_rfz = Min(L.rr * odt, t.prg_rfz);
     t.pnr_rfz = Min(L.nr * odt, t.pnr_rfz);
-    t.png_rfz = t.pnr_rfz * Max(Min((Pow(R(10.0), -(R(0.1) * w)) + R(0.1)), R(1.0)), R(0.1));
+    t.png_rfz = t.pnr_rfz * Max(Min((Pow10(-(R(0.1) * w)) + R(0.1)), R(1.0)), R(0.1));
   } else if (L.rr > R(r1) && L.temp < hgfrz) {
     TG_TRACE(L, TR_FZR, 1 << 25);
     t.pri_rfz = L.rr * odt;
@@ -249,6 +312,10 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
     int idx_c, idx_n;
     cloud_index(c, T.edges, L.rc, L.nc, idx_c, idx_n);
     TG_TRACE(L, TR_FZC, idx_c | (idx_n << 8) | (1 << 16));
+    TG_RANGE(L, RG_QCFZ, idx_c, 1, ntb_c);
+    TG_RANGE(L, RG_QCFZ, idx_n, 1, nbc);
+    TG_RANGE(L, RG_QCFZ, idx_tc, 1, ntb_t1);
+    TG_RANGE(L, RG_QCFZ, idx_in, 1, ntb_in);
     const Cst<R>* e = T.qcfz + 2L * ((idx_c - 1) + (long)(idx_n - 1) * ntb_c +
                                 (long)(idx_tc - 1) * ntb_c * nbc +
                                 (long)(idx_in - 1) * ntb_c * nbc * ntb_t1);
@@ -263,7 +330,7 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
   }
   if ((L.ssati >= demott_nuc_ssati) || (L.ssatw > eps && tempc < R(demott_nuc_tempc))) {
     if (f & F_NIFA)
-      xnc = demott_nucleation(c, tempc, rho, L.nifa);
+      xnc = xni_demott;
     else
       xnc = Min(R(icenuc_max), R(tno) * Exp(R(ato) * R(t0 - L.temp)));
     xni = L.ni + (t.pni_rfz + t.pni_wfz) * dt;
@@ -312,8 +379,10 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>&
   R rate_max = R((L.qv - L.qvsi) * L.rho) * odt * R(0.999);
   R ssati = R(L.ssati);
   if (L.l_qi) {
-    int idx_i = decade_index(L.ri, c.nii2, ntb_i), idx_i1 = decade_index(L.ni, c.nii3, ntb_i1);
+    int idx_i = decade_index(c, L.ri, c.nii2, ntb_i), idx_i1 = decade_index(c, L.ni, c.nii3, ntb_i1);
     TG_TRACE(L, TR_ICE, idx_i | (idx_i1 << 8) | (1 << 16));
+    TG_RANGE(L, RG_ICE, idx_i, 1, ntb_i);
+    TG_RANGE(L, RG_ICE, idx_i1, 1, ntb_i1);
     R xdi = Max(R(c.d0i), (R(bm_i) + R(mu_i) + R(1.)) * L.ilami);
     R xmi = c.am_i * Pow(xdi, R(bm_i));
     R oxmi = R(1.0) / xmi;
@@ -351,12 +420,12 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>&
     }
     if (L.rr >= c.r_r1 && L.mvd_r > R(4.0) * xdi) {
       R lamr = R(1.0) / L.ilamr;
-      R n0_r = L.nr * c.org2 * Pow(lamr, c.cre[1]);
-      R pf9 = Pow(lamr + R(fv_r), -c.cre[8]);
+      R n0_r, pf9;
+      rain_n0_pf9(L, n0_r, pf9);
       t.pri_rci = L.rhof * c.t1_qr_qi * R(ef_ri) * L.ri * n0_r * pf9;
       t.pnr_rci = L.rhof * c.t1_qr_qi * R(ef_ri) * L.ni * n0_r * pf9;
       t.pnr_rci = Min(L.nr * odt, t.pnr_rci);
-      t.png_rci = t.pnr_rci * Max(Min((Pow(R(10.0), -(R(0.1) * w)) + R(0.1)), R(1.0)), R(0.1));
+      t.png_rci = t.pnr_rci * Max(Min((Pow10(-(R(0.1) * w)) + R(0.1)), R(1.0)), R(0.1));
       t.pni_rci = t.pri_rci * oxmi;
       t.prr_rci = L.rhof * c.t2_qr_qi * R(ef_ri) * L.ni * n0_r * Pow(lamr + R(fv_r), -c.cre[7]);
       t.prr_rci = Min(L.rr * odt, t.prr_rci);
@@ -377,7 +446,7 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>&
   if (L.l_qg) {
     if (L.ssati < -eps) {
       const int ig = L.idx_bg;
-      R n0_g = L.ng * c.ogg2 * Pow(R(1.0) / L.ilamg, c.cge[0][1]);
+      R n0_g = graupel_n0(L);
       R t2_qg_sd = R(0.28) * c.sc3 * Sqrt(c.av_g[ig - 1]) * c.cgg[ig - 1][10];
       t.prg_gde = R(c_cube) * t1_subl * L.diffu * ssati * rvs * n0_g *
                   (c.t1_qg_sd * Pow(L.ilamg, c.cge[0][9]) +
@@ -403,8 +472,11 @@ __device__ void riming(Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, R odt) {
     if ((L.mvd_c > R(d0c)) && (xds > R(d0s))) {
       int idxs = 1 + Int(R(nbs) * Log(xds / c.ds1) / Log(c.dsn / c.ds1));
       idxs = edge_index(T.edges + kEdgesS, nbs, edge_arg(xds), idxs);
-      TG_TRACE(L, TR_RIME, idxs | (Int(L.mvd_c * R(1.e6)) << 8) | (1 << 16));
-      R ef_sw = ld(T.t_efsw + (idxs - 1) + (long)(Int(L.mvd_c * R(1.e6)) - 1) * nbs);
+      int mc = Int(L.mvd_c * R(1.e6));
+      TG_TRACE(L, TR_RIME, idxs | (mc << 8) | (1 << 16));
+      TG_RANGE(L, RG_EFSW, idxs, 1, nbs);
+      TG_RANGE(L, RG_EFSW, mc, 1, nbc);
+      R ef_sw = ld(T.t_efsw + (idxs - 1) + (long)(mc - 1) * nbs);
       t.prs_scw = L.rhof * c.t1_qs_qc * ef_sw * L.rc * L.smoe;
       t.prs_scw = Min(L.rc * odt, t.prs_scw);
       t.pnc_scw = L.rhof * c.t1_qs_qc * ef_sw * L.nc * L.smoe;
@@ -452,8 +524,8 @@ __device__ void riming(Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, R odt) {
           ef_gw = R(0.77);
         if (L.temp > t0) ef_gw = ef_gw * R(0.1);
         R t1_qg_qc = R(pi) * R(.25) * c.av_g[ig - 1] * c.cgg[ig - 1][8];
-        R n0_g = L.ng * c.ogg2 * Pow(R(1.0) / L.ilamg, c.cge[0][1]);
-        R pg9 = Pow(L.ilamg, c.cge[ig - 1][8]);
+        R n0_g = graupel_n0(L);
+        R pg9 = graupel_pg9(L);
         t.prg_gcw = L.rhof * t1_qg_qc * ef_gw * L.rc * n0_g * pg9;
         t.pnc_gcw = L.rhof * t1_qg_qc * ef_gw * L.nc * n0_g * pg9;
         t.pnc_gcw = Min(L.nc * odt, t.pnc_gcw);
@@ -491,7 +563,7 @@ __device__ void melting(const Lev<R>& L, Tend<R>& t, R t1_subl, uint32_t f, R dt
     if (t.prr_sml > R(0.0)) {
       t.prr_sml = t.prr_sml + R(4218.0) * c.olfus * tempc * (t.prr_rcs + t.prs_scw);
       t.prr_sml = Min(L.rs * odt, Max(R(0.0), t.prr_sml));
-      t.pnr_sml = L.smo0 / L.rs * t.prr_sml * Pow(R(10.0), -(R(0.25) * tempc));
+      t.pnr_sml = L.smo0 / L.rs * t.prr_sml * Pow10(-(R(0.25) * tempc));
       t.pnr_sml = Min(L.smo0 * odt, t.pnr_sml);
     } else {
       t.prr_sml = R(0.0);
@@ -505,7 +577,7 @@ __device__ void melting(const Lev<R>& L, Tend<R>& t, R t1_subl, uint32_t f, R dt
   }
   if (L.l_qg) {
     const int ig = L.idx_bg;
-    R n0_g = L.ng * c.ogg2 * Pow(R(1.0) / L.ilamg, c.cge[0][1]);
+    R n0_g = graupel_n0(L);
     R n0_melt = n0_g;
     if ((L.rg * L.ng) < R(1.e-4)) {
       R lamg = R(1.) / L.ilamg;
@@ -521,7 +593,7 @@ __device__ void melting(const Lev<R>& L, Tend<R>& t, R t1_subl, uint32_t f, R dt
     if (t.prr_gml > R(0.0)) {
       R melt_f = Max(R(0.05), Min(t.prr_gml * dt / L.rg, R(1.0)));
       t.pbg_gml = R(meters3_to_liters) * t.prr_gml / Max(Min(melt_f * rho_g<R>(ig), R(rho_w)), R(50.0));
-      t.pnr_gml = t.prr_gml * L.ng / L.rg * Pow(R(10.0), -(R(0.33) * tempc));
+      t.pnr_gml = t.prr_gml * L.ng / L.rg * Pow10(-(R(0.33) * tempc));
     } else {
       t.prr_gml = R(0.0);
       t.pnr_gml = R(0.0);
@@ -542,10 +614,13 @@ __device__ void melting(const Lev<R>& L, Tend<R>& t, R t1_subl, uint32_t f, R dt
   }
 }
 
-// aerosol_collection_efficiency (src/module_mp_tempo_aerosols.F90:76-118)
+// aerosol_collection_efficiency (src/module_mp_tempo_aerosols.F90:76-118) of one
+// collector for the two aerosol diameters the step uses (0.04 and 0.8 um): the terms
+// that depend only on the collector (fall speed, Reynolds number) are formed once.
 template <class C, class R>
-__device__ R aerosol_eff(const TempoConsts<C>& c, R d, R da, R visc, R rhoa, R temp, int species) {
-  const R boltzman = R(1.3806503e-23), meanpath = R(0.0256e-6);
+__device__ void aerosol_eff(const TempoConsts<C>& c, R d, R visc, R rhoa, R temp, int species,
+                            R& eff_wf, R& eff_if) {
+  const R boltzman = R(1.3806503e-23);
   R vt = R(1.0), rho_p = R(rho_w);
   if (species == 0) {  // rain
     vt = R(-0.1021) + R(4.932e3) * d - R(0.9551e6) * d * d + R(0.07934e9) * d * d * d -
@@ -558,57 +633,57 @@ __device__ R aerosol_eff(const TempoConsts<C>& c, R d, R da, R visc, R rhoa, R t
     vt = c.av_g[idx_bg1 - 1] * Pow(d, c.bv_g[idx_bg1 - 1]);
     rho_p = rho_g<R>(idx_bg1);
   }
-  R cc = R(1.0) + R(2.0) * meanpath / da * (R(1.257) + R(0.4) * Exp(-(R(0.55) * da / meanpath)));
-  R diff = boltzman * temp * cc / (R(3.0) * R(pi) * visc * da);
   R re = R(0.5) * rhoa * d * vt / visc;
-  R scn = visc / (rhoa * diff);
-  R st = (rho_p - rhoa) * da * da * vt * cc / (R(9.0) * visc * d);
   R aval = Log(R(1.0) + re);
   R st2 = (R(1.2) + R(1.0 / 12.0) * aval) / (R(1.0) + aval);
   R sre = Sqrt(re);
-  R eff = R(4.0) / (re * scn) * (R(1.0) + R(0.4) * sre * Pow(scn, R(0.3333)) + R(0.16) * sre * Sqrt(scn)) +
-          R(4.0) * da / d * (R(0.02) + da / d * (R(1.0) + R(2.0) * sre));
-  if (st > st2) eff = eff + Pow((st - st2) / (st - st2 + R(0.666667)), R(1.5));
-  return Max(R(1.e-5), Min(eff, R(1.0)));
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    const R da = i == 0 ? R(0.04e-6) : R(0.8e-6);
+    R cc = c.aer_cc[i];
+    R diff = boltzman * temp * cc / (R(3.0) * R(pi) * visc * da);
+    R scn = visc / (rhoa * diff);
+    R st = (rho_p - rhoa) * da * da * vt * cc / (R(9.0) * visc * d);
+    R eff = R(4.0) / (re * scn) * (R(1.0) + R(0.4) * sre * Pow(scn, R(0.3333)) + R(0.16) * sre * Sqrt(scn)) +
+            R(4.0) * da / d * (R(0.02) + da / d * (R(1.0) + R(2.0) * sre));
+    if (st > st2) eff = eff + Pow((st - st2) / (st - st2 + R(0.666667)), R(1.5));
+    (i == 0 ? eff_wf : eff_if) = Max(R(1.e-5), Min(eff, R(1.0)));
+  }
 }
 
 // aerosol_scavenging (main:3122-3193)
 template <class R>
 __device__ void aerosol_scavenging(const Lev<R>& L, Tend<R>& t, R odt) {
   const TempoConsts<Cst<R>>& c = *L.cs;
-  const R wf = R(0.04e-6), iff = R(0.8e-6);
   R temp = R(L.temp), rho = R(L.rho);
+  R ef_wf, ef_if;
   if (L.l_qr && L.mvd_r > R(d0r)) {
-    R ef_ra = aerosol_eff(c, L.mvd_r, wf, L.visco, rho, temp, 0);
-    R lamr = R(1.0) / L.ilamr;
-    R n0_r = L.nr * c.org2 * Pow(lamr, c.cre[1]);
-    R pf9 = Pow(lamr + R(fv_r), -c.cre[8]);
-    t.pna_rca = L.rhof * c.t1_qr_qc * ef_ra * L.nwfa * n0_r * pf9;
+    aerosol_eff(c, L.mvd_r, L.visco, rho, temp, 0, ef_wf, ef_if);
+    R n0_r, pf9;
+    rain_n0_pf9(L, n0_r, pf9);
+    t.pna_rca = L.rhof * c.t1_qr_qc * ef_wf * L.nwfa * n0_r * pf9;
     t.pna_rca = Min(L.nwfa * odt, t.pna_rca);
-    ef_ra = aerosol_eff(c, L.mvd_r, iff, L.visco, rho, temp, 0);
-    t.pnd_rcd = L.rhof * c.t1_qr_qc * ef_ra * L.nifa * n0_r * pf9;
+    t.pnd_rcd = L.rhof * c.t1_qr_qc * ef_if * L.nifa * n0_r * pf9;
     t.pnd_rcd = Min(L.nifa * odt, t.pnd_rcd);
   }
   if (L.l_qs && L.rs > c.r_s1) {
     R xds = L.smoc / L.smob;
-    R ef_sa = aerosol_eff(c, xds, wf, L.visco, rho, temp, 1);
-    t.pna_sca = L.rhof * c.t1_qs_qc * ef_sa * L.nwfa * L.smoe;
+    aerosol_eff(c, xds, L.visco, rho, temp, 1, ef_wf, ef_if);
+    t.pna_sca = L.rhof * c.t1_qs_qc * ef_wf * L.nwfa * L.smoe;
     t.pna_sca = Min(L.nwfa * odt, t.pna_sca);
-    ef_sa = aerosol_eff(c, xds, iff, L.visco, rho, temp, 1);
-    t.pnd_scd = L.rhof * c.t1_qs_qc * ef_sa * L.nifa * L.smoe;
+    t.pnd_scd = L.rhof * c.t1_qs_qc * ef_if * L.nifa * L.smoe;
     t.pnd_scd = Min(L.nifa * odt, t.pnd_scd);
   }
   if (L.l_qg && L.rg > c.r_g1) {
     const int ig = L.idx_bg;
     R xdg = (R(bm_g) + R(mu_g) + R(1.0)) * L.ilamg;
-    R ef_ga = aerosol_eff(c, xdg, wf, L.visco, rho, temp, 2);
+    aerosol_eff(c, xdg, L.visco, rho, temp, 2, ef_wf, ef_if);
     R t1_qg_qc = R(pi) * R(.25) * c.av_g[ig - 1] * c.cgg[ig - 1][8];
-    R n0_g = L.ng * c.ogg2 * Pow(R(1.0) / L.ilamg, c.cge[0][1]);
-    R pg9 = Pow(L.ilamg, c.cge[ig - 1][8]);
-    t.pna_gca = L.rhof * t1_qg_qc * ef_ga * L.nwfa * n0_g * pg9;
+    R n0_g = graupel_n0(L);
+    R pg9 = graupel_pg9(L);
+    t.pna_gca = L.rhof * t1_qg_qc * ef_wf * L.nwfa * n0_g * pg9;
     t.pna_gca = Min(L.nwfa * odt, t.pna_gca);
-    ef_ga = aerosol_eff(c, xdg, iff, L.visco, rho, temp, 2);
-    t.pnd_gcd = L.rhof * t1_qg_qc * ef_ga * L.nifa * n0_g * pg9;
+    t.pnd_gcd = L.rhof * t1_qg_qc * ef_if * L.nifa * n0_g * pg9;
     t.pnd_gcd = Min(L.nifa * odt, t.pnd_gcd);
   }
 }
@@ -861,6 +936,9 @@ __device__ void cloud_condensation(const Lev<R>& L, Tend<R>& t, const Tables<Cst
       int idx_c, idx_n;
       cloud_index(c, T.edges, L.rc, L.nc, idx_c, idx_n);
       TG_TRACE(L, TR_EVAP, idx_d | (idx_c << 8) | (idx_n << 16) | (1 << 24));
+      TG_RANGE(L, RG_EVAP, idx_d, 1, nbc);
+      TG_RANGE(L, RG_EVAP, idx_c, 1, ntb_c);
+      TG_RANGE(L, RG_EVAP, idx_n, 1, nbc);
       R tnc = ld(T.tnc_wev + (idx_d - 1) + (long)(idx_c - 1) * nbc + (long)(idx_n - 1) * nbc * ntb_c);
       t.prw_vcd = Max(-(L.rc * R(0.99) * orho * odt), t.prw_vcd);
       t.pnc_wcd = Max(-(L.nc * R(0.99) * orho * odt), -(tnc * orho * odt));

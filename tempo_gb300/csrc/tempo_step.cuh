@@ -174,7 +174,7 @@ TG_UNROLL
     corr = R(-0.2704) * (pe * p4) + R(1.838) * p4 - R(5.127) * (pe * p2) + R(8.547) * p2 -
            R(8.439) * pe + R(4.297);
   }
-  return corr * Pow(R(10.0), pe);
+  return corr * Pow10(pe);
 }
 
 // The initial checks of the level (main:346-396).  With F_MLNC the single-moment cloud
@@ -467,6 +467,8 @@ __device__ __forceinline__ void points_stage(int stage, Lev<R>& L, Tend<R>& td, 
       melting(L, td, t1s, f, dt, odt);
       if (has_nwfa || has_nifa) aerosol_scavenging(L, td, odt);
       block_sync<kSync>(go);
+      L.psd_have = 0;
+      L.rain_idx = 0;
     }
     check_over_depletion(L, td, odt);
     sum_tendencies(L, td);

@@ -160,7 +160,14 @@ enum TraceSlot : int {
   TR_RIME = 11,   // riming: efsw snow bin | int(mvd_c 1e6) << 8 | taken << 16
   TR_EVAP = 12,   // droplet evaporation: idx_d | idx_c << 8 | idx_n << 16 | taken << 24
   TR_LIMIT = 13,  // check_over_depletion: one bit per rescaled group
+  TR_RANGE = 14,  // table indices found out of their table's range (RangeSite bits; the
+                  // index is clamped before the read).  The oracle never sets it.
   kTracePoint = 16
+};
+// table-read sites whose indices the test build checks against the table's bounds
+enum RangeSite : int {
+  RG_EFRW = 1, RG_EFSW = 2, RG_QS = 4, RG_QG = 8, RG_QRFZ = 16, RG_QCFZ = 32, RG_ICE = 64,
+  RG_EVAP = 128
 };
 enum TraceCheckBit : int {
   TB_QC = 1, TB_QC_HIT = 2, TB_QR = 4, TB_QR_HIT = 8, TB_QI = 16, TB_QI_HIT = 32,

@@ -14,7 +14,11 @@ main:1171/1200, or a substep count int(dt vt / dz + 1)) are excluded: there the
 result of the reference itself depends on the last bit of a libm result.
 
 The mixed form's decisions are counted against the oracle's (the precision study):
-its FP32 values can land on the other side of a bin edge or threshold."""
+its FP32 values can land on the other side of a bin edge or threshold.
+
+The same build checks every table index against its table's bounds before the read
+(TR_RANGE): a bad index sets its site's bit and is clamped.  No point of any case, in
+either form, may set one."""
 import numpy as np
 import pytest
 
@@ -25,6 +29,7 @@ pytestmark = pytest.mark.gpu
 
 # mixed form: decisions that differ from the oracle's, per point and over all slots
 MIXED_FLIP_BOUND = 5e-4
+TR_RANGE = 14  # TraceSlot::TR_RANGE
 
 
 def _oracle_trace(oracle_mod, wl, over, hail):
@@ -103,6 +108,14 @@ def test_fp64_decisions_equal_the_oracle(tg, oracle_mod, oracle_tables, case):
     bad = {k: v for k, v in mismatches(got, ref, ncol, nz, clean).items() if v}
     print(name, "decisions recorded", ncheck, "tie columns", int((~clean).sum()), "mismatches", bad)
     assert not bad, (name, bad)
+    _assert_indices_in_range(got, ncol, nz)
+
+
+def _assert_indices_in_range(got, ncol, nz):
+    pts = got[: ncol * nz * TRACE_POINT].reshape(ncol, nz, TRACE_POINT)
+    rng = pts[:, :, TR_RANGE]
+    sites = int(np.bitwise_or.reduce(rng.ravel()))
+    assert not rng.any(), ("table index out of range", int(np.count_nonzero(rng)), hex(sites))
 
 
 @pytest.mark.parametrize("case", [1, 2], ids=["config1", "config2"])
@@ -116,3 +129,4 @@ def test_mixed_decision_census(tg, oracle_mod, oracle_tables, case):
     frac = {k: v / npts for k, v in mm.items() if v}
     print(name, "points", npts, "mixed-form decision flips per point", frac)
     assert sum(mm.values()) / npts < MIXED_FLIP_BOUND, frac
+    _assert_indices_in_range(got, ncol, nz)

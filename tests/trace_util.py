@@ -13,7 +13,7 @@ TRACE_POINT, TRACE_COLUMN = 16, 10
 SLOTS = {0: "check_initial", 1: "check_rates", 2: "check_condensation", 3: "check_evaporation",
          4: "check_final", 5: "warm_rain", 6: "rain_snow", 7: "rain_graupel",
          8: "rain_freezing", 9: "cloud_freezing", 10: "ice_processes", 11: "riming",
-         12: "droplet_evaporation", 13: "limiter", 14: "unused14", 15: "unused15"}
+         12: "droplet_evaporation", 13: "limiter", 14: "index_range", 15: "unused15"}
 COLUMN_SLOTS = ("substeps_rain", "substeps_graupel", "substeps_snow", "substeps_ice",
                 "ktop_rain", "ktop_graupel", "ktop_snow", "ktop_ice", "ktop_cloud", "unused")
 
