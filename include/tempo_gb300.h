@@ -302,8 +302,8 @@ int tempo_kernel_times_c(tempo_ctx_t *ctx, float ms[5]);
  * median step time.  Candidates 0-15: every variant of the per-level kernel (block
  * shape, barriers, register budget) in each order of the points (candidate v: variant
  * v % 8, order v / 8, as tempo_set_points_variant and tempo_set_points_order take
- * them), timed over the regime-order and per-level kernels; candidates 16-21: the
- * sedimentation variants 0-5 (tempo_set_sedim_variant) with the best of 0-15, timed
+ * them), timed over the regime-order and per-level kernels; candidates 16-27: the
+ * sedimentation variants 0-11 (tempo_set_sedim_variant) with the best of 0-15, timed
  * over the sedimentation kernel.  The best of each group is kept for later runs (all
  * precisions).  Tune on a state like the ones the runs will see: the work of a step
  * depends on the state it starts from.  Arguments as tempo_run_dev_f32_c; times_ms
@@ -366,9 +366,11 @@ int tempo_set_points_variant(tempo_ctx_t *ctx, int variant);
  * tempo_run_dev_f32_noalloc_c always runs level-major. */
 int tempo_set_points_order(tempo_ctx_t *ctx, int order);
 
-/* No reference counterpart.  Selects the sedimentation kernel variant directly (0..5):
- * variant % 3 + 1 levels whose loads a sweep issues together, and for variants 3-5 a
- * column's species split over two threads (rain and snow; graupel, ice and cloud).
+/* No reference counterpart.  Selects the sedimentation kernel variant directly (0..11):
+ * variant % 3 + 1 levels whose loads a substep's sweep issues together; for variants
+ * 3-5 and 9-11 a column's species split over two threads (rain and snow; graupel, ice
+ * and cloud); variants 0-5 run a species' substeps level by level (one pass over the
+ * column) when a warp's substep counts are at most 8, variants 6-11 substep by substep.
  * Variant 0 is the default.  Every variant computes the same values. */
 int tempo_set_sedim_variant(tempo_ctx_t *ctx, int variant);
 

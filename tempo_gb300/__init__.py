@@ -379,12 +379,12 @@ class TempoContext:
             if a is not None:
                 setattr(d, n, a.data_ptr())
         s = stream if stream is not None else torch.cuda.current_stream(p.device)
-        times = (ctypes.c_float * 22)()
+        times = (ctypes.c_float * 28)()
         chosen = ctypes.c_int(-1)
         _check(lib.tempo_autotune_dev_f32_c(
             self._h, ctypes.byref(cfg), float(dt), int(itimestep), *ptrs,
             land.data_ptr() if land is not None else None, *b[6:], ctypes.byref(d),
-            ctypes.c_void_p(s.cuda_stream), int(reps), times, 22, ctypes.byref(chosen)))
+            ctypes.c_void_p(s.cuda_stream), int(reps), times, 28, ctypes.byref(chosen)))
         return chosen.value, [float(x) for x in times]
 
     # ---- derivatives ----------------------------------------------------------------
@@ -454,8 +454,10 @@ class TempoContext:
         _check(load_library().tempo_set_points_order(self._h, int(order)))
 
     def set_sedim_variant(self, v: int):
-        """Sedimentation kernel variant 0..5: v % 3 + 1 levels loaded together per
-        sweep; v >= 3 splits a column's species over two threads."""
+        """Sedimentation kernel variant 0..11: v % 3 + 1 levels loaded together per
+        substep sweep; (v // 3) % 2 splits a column's species over two threads; v < 6
+        runs a species' substeps level by level where they fit, v >= 6 substep by
+        substep."""
         _check(load_library().tempo_set_sedim_variant(self._h, int(v)))
 
     def set_host_slabs(self, n: int):

@@ -108,12 +108,12 @@ __global__ void __launch_bounds__(points_block(V), points_min_blocks(V)) tempo_p
   }
 }
 
-template <class R, class S, int G, bool SPLIT>
+template <class R, class S, int G, bool SPLIT, bool BLOCK>
 __global__ void __launch_bounds__(128, sedim_min_blocks<R>()) tempo_sedim_batch_kernel(const __grid_constant__ BatchArgs<S> b) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)b.slot_start[b.nd]) return;
   const int d = domain_of(b.slot_start, b.nd, t);
-  sedim_column<R, S, false, G>(b.dom[d], nullptr, nullptr, t - (long)b.slot_start[d],
+  sedim_column<R, S, false, G, BLOCK>(b.dom[d], nullptr, nullptr, t - (long)b.slot_start[d],
                                SPLIT ? (int)blockIdx.y : -1);
 }
 
@@ -134,7 +134,7 @@ template <class R, class S, int V = 0>
 void launch_sedim_batch(const BatchArgs<S>& b, int sv, unsigned gcol, cudaStream_t s) {
   if constexpr (V + 1 < kSedimVariants)
     if (sv != V) return launch_sedim_batch<R, S, V + 1>(b, sv, gcol, s);
-  tempo_sedim_batch_kernel<R, S, sedim_group(V), sedim_split(V)>
+  tempo_sedim_batch_kernel<R, S, sedim_group(V), sedim_split(V), sedim_blocked(V)>
       <<<dim3(gcol, sedim_split(V) ? 2 : 1), kBlock, 0, s>>>(b);
 }
 

@@ -97,6 +97,9 @@ struct TempoConsts {
   R rain_n0_k, graupel_n0_k, graupel_lam_k, dc_g_k[15], aer_cc[2];
   // ipow_binary(R(10), m) in R's own arithmetic, m = kP10Min..kP10Max
   R p10[kP10Count];
+  // logarithms of the CCN activation table's aerosol-number and vertical-velocity
+  // grid values (main:2222-2223, 2236-2237)
+  R ln_ta_na[ntb_arc], ln_ta_ww[ntb_arw];
 };
 
 // Fills a double-precision constant set exactly as tempo_init does for the given

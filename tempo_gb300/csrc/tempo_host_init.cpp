@@ -255,6 +255,8 @@ void make_consts(TempoConsts<double>* c, bool hailaware) {
   for (int i = 0; i < 2; i++)
     c->aer_cc[i] = 1.0 + 2.0 * meanpath / da[i] * (1.257 + 0.4 * std::exp(-(0.55 * da[i] / meanpath)));
   for (int m = kP10Min; m <= kP10Max; m++) c->p10[m - kP10Min] = ipow_binary(10.0, m);
+  for (int i = 0; i < ntb_arc; i++) c->ln_ta_na[i] = std::log(c->ta_na[i]);
+  for (int i = 0; i < ntb_arw; i++) c->ln_ta_ww[i] = std::log(c->ta_ww[i]);
 }
 
 void narrow_consts(const TempoConsts<double>& d, TempoConsts<float>* f) {
@@ -278,7 +280,7 @@ void narrow_consts(const TempoConsts<double>& d, TempoConsts<float>* f) {
   NAR(t1_qg_me); NAR(nic1);
   NAR(dr1); NAR(drn); NAR(ds1); NAR(dsn); NAR(t_nc1); NAR(r_c1); NAR(r_r1); NAR(r_s1);
   NAR(r_g1); NAR(nt_in1); NAR(rain_n0_k); NAR(graupel_n0_k); NAR(graupel_lam_k);
-  NARA(dc_g_k); NARA(aer_cc); NARA(hbins); NARA(dhbins); NARA(ta_na); NARA(ta_ww); NARA(ta_tk);
+  NARA(dc_g_k); NARA(aer_cc); NARA(ln_ta_na); NARA(ln_ta_ww); NARA(hbins); NARA(dhbins); NARA(ta_na); NARA(ta_ww); NARA(ta_tk);
   NARA(sa); NARA(sb);
   // powers of ten in float arithmetic (not narrowed doubles): the mixed form's decade
   // searches divide by exactly what the float powering gives

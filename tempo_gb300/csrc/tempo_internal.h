@@ -102,8 +102,9 @@ cudaError_t launch_melt_refl(const StepArgs<S>& a, const TempoConsts<double>& c,
 // autotuner's candidates (each variant in level-major and in regime order)
 constexpr int kPointsVariants = 8;
 constexpr int kPointsCandidates = 2 * kPointsVariants;
-// number of sedimentation-kernel variants (tempo_step.cuh: sedim_group, sedim_split)
-constexpr int kSedimCandidates = 6;
+// number of sedimentation-kernel variants (tempo_step.cuh: sedim_group, sedim_split,
+// sedim_blocked)
+constexpr int kSedimCandidates = 12;
 // kernels launched per step (prep, points, sedim, final), and one more when phase A's
 // points run in regime order
 constexpr int kStepLaunches = 4;

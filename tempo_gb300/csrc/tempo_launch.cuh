@@ -48,12 +48,12 @@ cudaError_t launch_points(const StepArgs<S>& a, const Tables<Cst<R>>& T, const T
 }
 
 // the explicit sedimentation kernel, variant sv (tempo_step.cuh: sedim_group,
-// sedim_split)
+// sedim_split, sedim_blocked)
 template <class R, class S, int V = 0>
 void launch_sedim(const StepArgs<S>& a, int sv, unsigned gcol, cudaStream_t s) {
   if constexpr (V + 1 < kSedimVariants)
     if (sv != V) return launch_sedim<R, S, V + 1>(a, sv, gcol, s);
-  tempo_sedim_kernel<R, S, sedim_group(V), sedim_split(V)>
+  tempo_sedim_kernel<R, S, sedim_group(V), sedim_split(V), sedim_blocked(V)>
       <<<dim3(gcol, sedim_split(V) ? 2 : 1), kBlock, 0, s>>>(a);
 }
 

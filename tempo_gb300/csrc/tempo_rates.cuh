@@ -847,7 +847,7 @@ __device__ R activate_cloud_number(const TempoConsts<C>& c, R temp, R w1d, R nwf
     if (n_local >= c.ta_na[n - 2] && n_local < c.ta_na[n - 1]) break;
   n = min(n, ntb_arc);
   const int i = n;
-  R x1 = Log(c.ta_na[i - 2]), x2 = Log(c.ta_na[i - 1]);
+  R x1 = c.ln_ta_na[i - 2], x2 = c.ln_ta_na[i - 1];
   R w_local = w1d;
   if (w_local >= c.ta_ww[ntb_arw - 1])
     w_local = c.ta_ww[ntb_arw - 1] - R(1.0);
@@ -857,7 +857,7 @@ __device__ R activate_cloud_number(const TempoConsts<C>& c, R temp, R w1d, R nwf
     if (w_local >= c.ta_ww[n - 2] && w_local < c.ta_ww[n - 1]) break;
   n = min(n, ntb_arw);
   const int j = n;
-  R y1 = Log(c.ta_ww[j - 2]), y2 = Log(c.ta_ww[j - 1]);
+  R y1 = c.ln_ta_ww[j - 2], y2 = c.ln_ta_ww[j - 1];
   int k = max(1, min(Nint((temp - c.ta_tk[0]) * R(0.1)) + 1, ntb_art));
   const int l = 3, m = 2;
   auto TN = [&](int a, int b) -> R {

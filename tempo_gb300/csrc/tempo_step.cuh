@@ -935,19 +935,22 @@ __device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dz
 // semi-Lagrangian scheme (semi_sedi_flag, main:599-613, 640-671), which rechecks the
 // species and recomputes their fall speeds after every substep (needs cst and ci).
 // Variants of the sedimentation kernel (picked per context by the autotuner): v % 3
-// selects the number of levels whose loads a sweep issues together, 1, 2 or 3 (more
-// loads in flight per thread against more registers per thread; 4 and 8 were measured
-// slower still); v / 3 = 1 splits a column's species over two threads (rain and snow
-// -- snow's fall speed reads rain's state after rain sedimentation -- and graupel, ice
-// and cloud), twice the threads for the same serial chains.
-constexpr int kSedimVariants = 6;
+// selects the number of levels whose loads a substep's sweep issues together, 1, 2 or
+// 3 (more loads in flight per thread against more registers per thread; 4 and 8 were
+// measured slower still); (v / 3) % 2 = 1 splits a column's species over two threads
+// (rain and snow -- snow's fall speed reads rain's state after rain sedimentation --
+// and graupel, ice and cloud), twice the threads for the same serial chains; v < 6
+// runs a species' substeps level by level (sweep_all) where the warp's substep counts
+// fit its register history, v >= 6 always substep by substep.
+constexpr int kSedimVariants = 12;
 __host__ __device__ constexpr int sedim_group(int v) { return v % 3 + 1; }
-__host__ __device__ constexpr bool sedim_split(int v) { return v >= 3; }
+__host__ __device__ constexpr bool sedim_split(int v) { return (v / 3) % 2 == 1; }
+__host__ __device__ constexpr bool sedim_blocked(int v) { return v < 6; }
 
 // Phase B of active slot s; part < 0: every species, 0: rain and snow, 1: graupel, ice
 // and cloud (each part writes the precipitation sums and substep counts of its own
 // species).
-template <class R, class S, bool SEMI, int G = 1>
+template <class R, class S, bool SEMI, int G = 1, bool BLOCK = true>
 __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoConsts<Cst<R>>* cst,
                                              const IslandConsts<Isl<R>>* ci, long s, int part = -1) {
   using I = Isl<R>;
@@ -1124,6 +1127,131 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
     }
     if (precip && x[0][0] > low_limit_mass_for_precip) *precip = *precip + s0[0] * dti * osteps;
   };
+  // All substeps of NF fields, level by level (temporal blocking).  In the upwind
+  // scheme level k's substep n reads only level k's state and the flux of level k + 1
+  // at substep n, so the column is walked once, top down: each level runs its substeps
+  // in order while hist[f][n] carries the flux of the level above at substep n.  Every
+  // level update, and every addition to the precipitation sum, is the arithmetic of
+  // the substep-by-substep sweep above in the same order; a level's fields are read
+  // and written once for all substeps instead of once per substep.  SM bounds the
+  // substeps (hist lives in registers).
+  auto sweep_all = [&](auto nf, auto smax, const int* fx, const int* ften, const int* fv,
+                       const double* limit, int steps, int ktop, I* precip) {
+    constexpr int NF = decltype(nf)::value;
+    constexpr int SM = decltype(smax)::value;
+    constexpr bool kMixed = std::is_same<I, df>::value;
+    I* x[NF];
+    I* ten[NF];
+    const R* vt[NF];
+    I lim[NF], hist[NF][SM];
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+      x[f] = sd + fx[f] * fsd;
+      ten[f] = sd + ften[f] * fsd;
+      vt[f] = sr + fv[f] * fsd;
+      lim[f] = I(limit[f]);
+    }
+    const I osteps = 1.0 / I(steps);
+    const I* odz = sd + SD_ODZ * fsd;
+    const I* ozr = sd + SD_OZR * fsd;
+    const I cx = dti * osteps;
+    {
+      const int k = nz - 1;
+      const long o = (long)k * kSlotTile;
+      I fo, fr;
+      if constexpr (kMixed) {
+        fo = odz[o];
+        fr = ozr[o];
+      } else {
+        fo = 1.0 / ldi<I>(dzp + k * NI);
+        fr = 1.0 / rho[o];
+      }
+#pragma unroll
+      for (int f = 0; f < NF; f++) {
+        I xk = x[f][o], tk = ten[f][o];
+        const I v = I(vt[f][o]);
+#pragma unroll
+        for (int n = 0; n < SM; n++)
+          if (n < steps) {
+            const I s_top = v * xk;
+            if constexpr (kMixed) {
+              tk = tk - s_top * fr * osteps;
+              xk = Max(lim[f], xk - s_top * fo * cx);
+            } else {
+              tk = tk - s_top * fo * osteps * fr;
+              xk = Max(lim[f], xk - s_top * fo * dti * osteps);
+            }
+            hist[f][n] = s_top;
+            if (k == 0 && f == 0 && precip && xk > low_limit_mass_for_precip)
+              *precip = *precip + s_top * dti * osteps;
+          }
+        ten[f][o] = tk;
+        x[f][o] = xk;
+      }
+      if (ktop != nz - 1) {  // levels ktop..nz-2 keep their state: a constant flux
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+          const I s_c = I(vt[f][ktop * kSlotTile]) * x[f][ktop * kSlotTile];
+#pragma unroll
+          for (int n = 0; n < SM; n++) hist[f][n] = s_c;
+        }
+      }
+    }
+    for (int k = ktop - 1; k >= 0; k--) {
+      const long o = (long)k * kSlotTile;
+      I fo, fr;
+      if constexpr (kMixed) {
+        fo = odz[o];
+        fr = ozr[o];
+      } else {
+        fo = 1.0 / ldi<I>(dzp + (long)k * NI);
+        fr = 1.0 / rho[o];
+      }
+#pragma unroll
+      for (int f = 0; f < NF; f++) {
+        I xk = x[f][o], tk = ten[f][o];
+        const I v = I(vt[f][o]);
+#pragma unroll
+        for (int n = 0; n < SM; n++)
+          if (n < steps) {
+            const I s_k = v * xk;
+            if constexpr (kMixed) {
+              const I dflux = hist[f][n] - s_k;
+              tk = tk + dflux * fr * osteps;
+              xk = Max(lim[f], xk + dflux * fo * cx);
+            } else {
+              tk = tk + (hist[f][n] - s_k) * fo * osteps * fr;
+              xk = Max(lim[f], xk + (hist[f][n] - s_k) * fo * dti * osteps);
+            }
+            hist[f][n] = s_k;
+            if (k == 0 && f == 0 && precip && xk > low_limit_mass_for_precip)
+              *precip = *precip + s_k * dti * osteps;
+          }
+        ten[f][o] = tk;
+        x[f][o] = xk;
+      }
+    }
+    if (ktop == 0 && nz > 1 && precip) {  // level 0 above the fall: its flux, unchanged
+      const I s0 = I(vt[0][0]) * x[0][0];
+      const bool add = x[0][0] > low_limit_mass_for_precip;
+#pragma unroll
+      for (int n = 0; n < SM; n++)
+        if (n < steps && add) *precip = *precip + s0 * dti * osteps;
+    }
+  };
+  // the substeps of one species: blocked when the warp's largest count fits the
+  // register history, else substep by substep
+  auto sweeps = [&](auto nf, const int* fx, const int* ften, const int* fv, const double* limit,
+                    int steps, int ktop, I* precip) {
+    const int wmax = BLOCK ? __reduce_max_sync(__activemask(), steps) : 1 << 30;
+    if (wmax <= 4) {
+      sweep_all(nf, std::integral_constant<int, 4>{}, fx, ften, fv, limit, steps, ktop, precip);
+    } else if (wmax <= 8) {
+      sweep_all(nf, std::integral_constant<int, 8>{}, fx, ften, fv, limit, steps, ktop, precip);
+    } else {
+      for (int n = 0; n < steps; n++) sweep(nf, fx, ften, fv, limit, steps, ktop, precip);
+    }
+  };
   using One = std::integral_constant<int, 1>;
   using Two = std::integral_constant<int, 2>;
   using Three = std::integral_constant<int, 3>;
@@ -1195,11 +1323,9 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
       }
     } else {
       sub[0] = steps;
-      for (int n = 0; n < steps; n++) {
-        const int fx[2] = {SD_XRR, SD_XNR}, ft[2] = {SD_TQR, SD_TNR}, fv[2] = {SR_VTR, SR_VTNR};
-        const double lim[2] = {r1, r2};
-        sweep(Two{}, fx, ft, fv, lim, steps, ktop, &prec_r);
-      }
+      const int fx[2] = {SD_XRR, SD_XNR}, ft[2] = {SD_TQR, SD_TNR}, fv[2] = {SR_VTR, SR_VTNR};
+      const double lim[2] = {r1, r2};
+      sweeps(Two{}, fx, ft, fv, lim, steps, ktop, &prec_r);
     }
   }
   if (any_qg && p1) {
@@ -1242,12 +1368,10 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
       }
     } else {
       sub[1] = steps;
-      for (int n = 0; n < steps; n++) {
-        const int fx[3] = {SD_XRG, SD_XNG, SD_XRB}, ft[3] = {SD_TQG, SD_TNG, SD_TQB},
-                  fv[3] = {SR_VTG, SR_VTNG, SR_VTG};
-        const double lim[3] = {r1, r2, meters3_to_liters * r1 / rho_gd(nrhg)};
-        sweep(Three{}, fx, ft, fv, lim, steps, ktop, &prec_g);
-      }
+      const int fx[3] = {SD_XRG, SD_XNG, SD_XRB}, ft[3] = {SD_TQG, SD_TNG, SD_TQB},
+                fv[3] = {SR_VTG, SR_VTNG, SR_VTG};
+      const double lim[3] = {r1, r2, meters3_to_liters * r1 / rho_gd(nrhg)};
+      sweeps(Three{}, fx, ft, fv, lim, steps, ktop, &prec_g);
     }
   }
   if (any_qs && p0) {
@@ -1256,7 +1380,7 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
     sub[2] = steps;
     const int fx[1] = {SD_XRS}, ft[1] = {SD_TQS}, fv[1] = {SR_VTSA};
     const double lim[1] = {r1};
-    for (int n = 0; n < steps; n++) sweep(One{}, fx, ft, fv, lim, steps, ktop, &prec_s);
+    sweeps(One{}, fx, ft, fv, lim, steps, ktop, &prec_s);
   }
   if (any_qi && p1) {
     fill(SR_VTI, SR_VTNI, false, false, steps, ktop);
@@ -1306,11 +1430,11 @@ template <class R>
 __host__ __device__ constexpr int sedim_min_blocks() {
   return std::is_same<R, float>::value ? 5 : 1;
 }
-template <class R, class S, int G = 1, bool SPLIT = false>
+template <class R, class S, int G = 1, bool SPLIT = false, bool BLOCK = true>
 __global__ void __launch_bounds__(128, sedim_min_blocks<R>()) tempo_sedim_kernel(const __grid_constant__ StepArgs<S> a) {
   const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= (long)*a.nact) return;
-  sedim_column<R, S, false, G>(a, nullptr, nullptr, s, SPLIT ? (int)blockIdx.y : -1);
+  sedim_column<R, S, false, G, BLOCK>(a, nullptr, nullptr, s, SPLIT ? (int)blockIdx.y : -1);
 }
 // phase B with semi-Lagrangian rain and graupel (F_SEMI), one thread per active column
 template <class R, class S>

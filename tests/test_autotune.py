@@ -26,7 +26,7 @@ def test_autotune_picks_fastest_and_keeps_state(tg):
     for k in f:
         assert torch.equal(f[k], before[k]), k
     assert 0 <= chosen < 16
-    assert len(times) == 22 and all(t > 0 for t in times)
+    assert len(times) == 28 and all(t > 0 for t in times)
     assert times[chosen] == min(times[:16])
     tun = ctx.tuning()
     assert (tun["points_variant"], tun["points_order"]) == (chosen % 8, chosen // 8)
@@ -109,12 +109,13 @@ def test_graph_replay_matches_direct_launches(tg):
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_sedim_variants_are_bit_identical(tg, precision):
     """The sedimentation variants change only how many levels' loads a sweep issues
-    together and how a column's species map to threads: two steps with each give
-    identical bits in every field."""
+    together, how a column's species map to threads and whether a species' substeps run
+    level by level or substep by substep: two steps with each give identical bits in
+    every field."""
     torch = pytest.importorskip("torch")
     from tempo_gb300 import workloads as W
     outs = []
-    for sv in range(6):
+    for sv in range(12):
         ctx = tg.TempoContext(build_tables=True, cfgs=tg.default_cfgs(hailaware_flag=0))
         f, d = _fields(W, torch)
         if precision == "mixed":
