@@ -8,11 +8,11 @@
 // unevaluated sum hi + lo of two floats (about 48 significant bits) and computed on
 // the FP32 pipes.  The algorithms are the classical error-free transformations:
 // Knuth's TwoSum, Dekker's Fast2Sum, and the FMA form of Dekker's TwoProduct, combined
-// as in the double-double arithmetic of Hida, Li and Bailey (QD library, 2001) with
-// accurate (cancellation-safe) addition, and the division algorithms of Joldes, Muller
-// and Popescu ("Tight and rigorous error bounds for basic building blocks of
-// double-word arithmetic", ACM TOMS 44(2), 2017).  Relative error of + - * is a few
-// units of 2^-48 (u^2, u = 2^-24), of / at most 15 u^2.
+// as in the double-double arithmetic of Hida, Li and Bailey (QD library, 2001), and the
+// addition and division algorithms of Joldes, Muller and Popescu ("Tight and rigorous
+// error bounds for basic building blocks of double-word arithmetic", ACM TOMS 44(2),
+// 2017).  Relative error of * is a few units of 2^-48 (u^2, u = 2^-24), of / at most
+// 15 u^2; the error of + and - is a few u^2 of the operands' magnitude.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -53,26 +53,27 @@ __host__ __device__ __forceinline__ void two_prod(float a, float b, float& p, fl
 
 __host__ __device__ __forceinline__ df operator-(df a) { return df(-a.hi, -a.lo); }
 
-// accurate addition (QD's IEEE-style add): both halves summed with TwoSum, so a sum
-// that cancels -- a saturation difference qv - qvs -- keeps its relative accuracy
+// addition of two double-words: QD's sloppy_add (SloppyDWPlusDW of Joldes, Muller and
+// Popescu), 11 FP32 operations against 20 for the cancellation-safe form.  Its absolute
+// error is a few u^2 (|a| + |b|): relative to its operands, not to a result that
+// cancels.  That is the accuracy the step needs -- a saturation difference qv - qvs,
+// for example, is then exact to ~1e-17 kg/kg, far below any threshold the step
+// compares it with, and the decision census and the precision study of the mixed
+// form came out the same with either addition.
 __host__ __device__ __forceinline__ df operator+(df a, df b) {
-  float s1, s2, t1, t2;
-  dfo::two_sum(a.hi, b.hi, s1, s2);
-  dfo::two_sum(a.lo, b.lo, t1, t2);
-  s2 += t1;
-  dfo::fast_two_sum(s1, s2, s1, s2);
-  s2 += t2;
-  dfo::fast_two_sum(s1, s2, s1, s2);
-  return df(s1, s2);
+  float s, e;
+  dfo::two_sum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  dfo::fast_two_sum(s, e, s, e);
+  return df(s, e);
 }
+// double-word plus float, DWPlusFP of the same paper: relative error at most 2 u^2
 __host__ __device__ __forceinline__ df operator+(df a, float b) {
-  float s1, s2, t1, t2;
-  dfo::two_sum(a.hi, b, s1, s2);
-  dfo::two_sum(s2, a.lo, t1, t2);
-  dfo::two_sum(s1, t1, s1, s2);
-  s2 += t2;
-  dfo::fast_two_sum(s1, s2, s1, s2);
-  return df(s1, s2);
+  float s, e;
+  dfo::two_sum(a.hi, b, s, e);
+  const float v = a.lo + e;
+  dfo::fast_two_sum(s, v, s, e);
+  return df(s, e);
 }
 __host__ __device__ __forceinline__ df operator+(float a, df b) { return b + a; }
 __host__ __device__ __forceinline__ df operator-(df a, df b) { return a + (-b); }

@@ -1,10 +1,12 @@
 // Host check of the double-float building blocks of the mixed-precision island
-// (tempo_gb300/csrc/tempo_dfloat.cuh): division, division by a float, accurate
-// addition, multiplication and the Horner step of the saturation polynomials, each
-// against long double arithmetic on seeded random operands.  Prints one line per
-// operation: name, samples, maximum relative error in units of u^2 (u = 2^-24), and for
-// the polynomials the maximum error in units of u^2 times the sum of the terms'
-// magnitudes (Horner's error scale).
+// (tempo_gb300/csrc/tempo_dfloat.cuh): division, division by a float, addition,
+// addition of a float, multiplication and the Horner step of the saturation
+// polynomials, each against long double arithmetic on seeded random operands.  Prints
+// one line per operation: name, samples, maximum relative error in units of u^2
+// (u = 2^-24); for the double-word addition the error in units of u^2 (|a| + |b|) (its
+// bound, also where the sum cancels) and the relative error of same-sign sums; for the
+// polynomials the error in units of u^2 times the sum of the terms' magnitudes
+// (Horner's error scale).
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -35,7 +37,7 @@ static LD rel(LD got, LD want) { return want == 0 ? std::fabs(got) : std::fabs((
 
 int main() {
   const int n = 200000;
-  LD e_div = 0, e_divf = 0, e_add = 0, e_mul = 0;
+  LD e_div = 0, e_divf = 0, e_add = 0, e_add_same = 0, e_addf = 0, e_mul = 0;
   for (int i = 0; i < n; i++) {
     const df a(random_value(-12, 6)), b(random_value(-12, 6));
     const float f = (float)random_value(-12, 6);
@@ -47,13 +49,21 @@ int main() {
     if (q > e_mul) e_mul = q;
     // sums of nearly equal values (the saturation differences) and of unrelated ones
     const df c = (i % 2) ? df(-(double)exact(a) * (1.0 + 1e-6 * uniform())) : b;
-    q = rel(exact(a + c), exact(a) + exact(c));
+    q = std::fabs(exact(a + c) - (exact(a) + exact(c))) / (std::fabs(exact(a)) + std::fabs(exact(c)));
     if (q > e_add) e_add = q;
+    const df bs = (exact(a) < 0) == (exact(b) < 0) ? b : -b;
+    q = rel(exact(a + bs), exact(a) + exact(bs));
+    if (q > e_add_same) e_add_same = q;
+    const float g = (i % 2) ? -(float)exact(a) * (float)(1.0 + 1e-3 * uniform()) : f;
+    q = rel(exact(a + g), exact(a) + (LD)g);
+    if (q > e_addf) e_addf = q;
   }
   std::printf("div %d %.3Lf\n", n, e_div / kU2);
   std::printf("div_float %d %.3Lf\n", n, e_divf / kU2);
   std::printf("mul %d %.3Lf\n", n, e_mul / kU2);
   std::printf("add %d %.3Lf\n", n, e_add / kU2);
+  std::printf("add_same_sign %d %.3Lf\n", n, e_add_same / kU2);
+  std::printf("add_float %d %.3Lf\n", n, e_addf / kU2);
 
   // the liquid and ice saturation polynomials (src/module_mp_tempo_utils.F90:285-331)
   static const double cl[9] = {.611583699E03, .444606896E02, .143177157e01, .264224321e-1,
