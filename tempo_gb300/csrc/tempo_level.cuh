@@ -41,6 +41,26 @@ template <class R> using Cst = typename ConstOf<R>::type;
 // ---------------------------------------------------------------------------------
 __device__ __forceinline__ double Pow(double x, double y) { return pow(x, y); }
 __device__ __forceinline__ float Pow(float x, float y) { return powf(x, y); }
+// Powers with the reference's mass exponents (bm_r = bm_i = bm_g = 3, a parameter of
+// the scheme): the size-distribution checks raise slopes to bm and form slopes as
+// (...)**(1/bm), and (...)**(1/(bm_g+1)) for the graupel intercept -- about 10 of the
+// 22 powers per level-point of a config-1 step.  The FP64 drop-in keeps the
+// reference's real-exponent pow (x**bm_r is pow(x, 3.0) there); the mixed form forms
+// them from products, cube and square roots, as accurate as powf at a fraction of its
+// code and time.  The exponent argument is the reference's constant (checked against
+// the parameter at compile time for the cube; the roots take the context's 1/bm).
+static_assert(bm_r == 3.0 && bm_i == 3.0 && bm_g == 3.0, "mass exponents of the scheme");
+__device__ __forceinline__ double PowBm(double x) { return pow(x, 3.0); }
+__device__ __forceinline__ float PowBm(float x) { return x * x * x; }
+__device__ __forceinline__ double PowObm(double x, double obm) { return pow(x, obm); }
+__device__ __forceinline__ float PowObm(float x, float) { return cbrtf(x); }
+__device__ __forceinline__ double PowOge1(double x, double oge1) { return pow(x, oge1); }
+__device__ __forceinline__ float PowOge1(float x, float) { return sqrtf(sqrtf(x)); }
+// x**y where |y log2 x| is below 1 (the diffusivity's (T/t0)**1.94 with T/t0 within
+// [0.7, 1.2]): the mixed form uses the hardware base-2 logarithm and exponential, whose
+// error there is a few ulp; the FP64 drop-in keeps pow
+__device__ __forceinline__ double PowNear1(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float PowNear1(float x, float y) { return __powf(x, y); }
 __device__ __forceinline__ double Exp(double x) { return exp(x); }
 __device__ __forceinline__ float Exp(float x) { return expf(x); }
 __device__ __forceinline__ double Log(double x) { return log(x); }
@@ -82,6 +102,25 @@ template <class T, int N, class U, class = typename std::enable_if<std::is_arith
 __device__ __forceinline__ Dual<T, N> Pow(U a, const Dual<T, N>& b) {
   const T r = Pow(T(a), b.v);
   return dual_chain(b, r, (T(a) > T(0)) ? r * Log(T(a)) : T(0));
+}
+template <class T, int N>
+__device__ __forceinline__ Dual<T, N> PowNear1(const Dual<T, N>& a, const Dual<T, N>& b) {
+  return Pow(a, b);
+}
+template <class T, int N> __device__ __forceinline__ Dual<T, N> PowBm(const Dual<T, N>& a) {
+  return Pow(a, 3.0);
+}
+template <class T, int N>
+__device__ __forceinline__ Dual<T, N> PowObm(const Dual<T, N>& a, const Dual<T, N>& obm) {
+  return Pow(a, obm);
+}
+template <class T, int N, class U, class = typename std::enable_if<std::is_arithmetic<U>::value>::type>
+__device__ __forceinline__ Dual<T, N> PowObm(const Dual<T, N>& a, U obm) {
+  return Pow(a, obm);
+}
+template <class T, int N, class U, class = typename std::enable_if<std::is_arithmetic<U>::value>::type>
+__device__ __forceinline__ Dual<T, N> PowOge1(const Dual<T, N>& a, U oge1) {
+  return Pow(a, oge1);
 }
 template <class T, int N> __device__ __forceinline__ Dual<T, N> Pow10(const Dual<T, N>& b) {
   return Pow(T(10.0), b);
@@ -402,7 +441,7 @@ __device__ void cloud_check(Lev<R>& L, R& q, R& n, bool has_nc, R ncsave, R dt, 
         L.nc = R(nt_c_max);
       }
       nu_c = get_nuc(L.nc);
-      lamc = Pow(L.nc * c.am_r * c.ccg[nu_c - 1][1] * c.ocg1[nu_c - 1] / L.rc, c.obmr);
+      lamc = PowObm(L.nc * c.am_r * c.ccg[nu_c - 1][1] * c.ocg1[nu_c - 1] / L.rc, c.obmr);
       xdc = (R(bm_r) + R(nu_c) + R(1.0)) / lamc;
       if (under_clamp(xdc, R(d0c))) {
         lamc = c.cce[nu_c - 1][1] / R(d0c);
@@ -411,16 +450,16 @@ __device__ void cloud_check(Lev<R>& L, R& q, R& n, bool has_nc, R ncsave, R dt, 
         lamc = c.cce[nu_c - 1][1] / (R(d0r) * R(2.0));
         hit_limit = true;
       }
-      L.nc = c.ccg[nu_c - 1][0] * c.ocg2[nu_c - 1] * L.rc / c.am_r * Pow(lamc, R(bm_r));
+      L.nc = c.ccg[nu_c - 1][0] * c.ocg2[nu_c - 1] * L.rc / c.am_r * PowBm(lamc);
       if (hit_limit) L.ncten = (L.nc / rho - n) * odt;
       n = Max(R(nt_c_min) / rho,
-              Min(c.ccg[nu_c - 1][0] * c.ocg2[nu_c - 1] * q / c.am_r * Pow(lamc, R(bm_r)),
+              Min(c.ccg[nu_c - 1][0] * c.ocg2[nu_c - 1] * q / c.am_r * PowBm(lamc),
                   R(nt_c_max) / rho));
     } else {
       L.nc = ncsave;
     }
     nu_c = get_nuc(L.nc);
-    lamc = Pow(L.nc * c.am_r * c.ccg[nu_c - 1][1] * c.ocg1[nu_c - 1] / L.rc, c.obmr);
+    lamc = PowObm(L.nc * c.am_r * c.ccg[nu_c - 1][1] * c.ocg1[nu_c - 1] / L.rc, c.obmr);
     L.ilamc = R(1.0) / lamc;
     L.mvd_c = Max(Min((R(3.0) + R(nu_c) + R(0.672)) * L.ilamc, R(d0r)), R(d0c));
     TG_TRACE(L, TR_CHECK + L.tpass, TB_QC | (hit_limit ? TB_QC_HIT : 0) | (nu_c << 16));
@@ -456,23 +495,23 @@ __device__ void rain_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
       hit_limit = true;
       L.mvd_r = R(1.0e-3);
       lamr = (R(3.0) + R(mu_r) + R(0.672)) / L.mvd_r;
-      L.nr = c.crg[1] * c.org3 * L.rr * Pow(lamr, R(bm_r)) / c.am_r;
+      L.nr = c.crg[1] * c.org3 * L.rr * PowBm(lamr) / c.am_r;
     }
-    lamr = Pow(c.am_r * c.crg[2] * c.org2 * L.nr / L.rr, c.obmr);
+    lamr = PowObm(c.am_r * c.crg[2] * c.org2 * L.nr / L.rr, c.obmr);
     L.mvd_r = (R(3.0) + R(mu_r) + R(0.672)) / lamr;
     if (over_clamp(L.mvd_r, R(d0r_max))) {
       hit_limit = true;
       L.mvd_r = R(d0r_max);
       lamr = (R(3.0) + R(mu_r) + R(0.672)) / L.mvd_r;
-      L.nr = c.crg[1] * c.org3 * L.rr * Pow(lamr, R(bm_r)) / c.am_r;
+      L.nr = c.crg[1] * c.org3 * L.rr * PowBm(lamr) / c.am_r;
     } else if (under_clamp(L.mvd_r, R(d0r) * R(0.75))) {
       hit_limit = true;
       L.mvd_r = R(d0r) * R(0.75);
       lamr = (R(3.0) + R(mu_r) + R(0.672)) / L.mvd_r;
-      L.nr = c.crg[1] * c.org3 * L.rr * Pow(lamr, R(bm_r)) / c.am_r;
+      L.nr = c.crg[1] * c.org3 * L.rr * PowBm(lamr) / c.am_r;
     }
     if (hit_limit) L.nrten = (L.nr / rho - n) * odt;
-    n = c.crg[1] * c.org3 * q * Pow(lamr, R(bm_r)) / c.am_r;
+    n = c.crg[1] * c.org3 * q * PowBm(lamr) / c.am_r;
     L.ilamr = R(1.0) / lamr;
     TG_TRACE(L, TR_CHECK + L.tpass, TB_QR | (hit_limit ? TB_QR_HIT : 0));
   } else {
@@ -504,21 +543,21 @@ __device__ void ice_check(Lev<R>& L, R& q, R& n, R dt, R odt) {
     if (L.ni <= R(r2)) {
       hit_limit = true;
       lami = c.cie[1] / R(5.e-6);
-      L.ni = Min(R(max_ni), c.cig[0] * c.oig2 * L.ri / c.am_i * Pow(lami, R(bm_i)));
+      L.ni = Min(R(max_ni), c.cig[0] * c.oig2 * L.ri / c.am_i * PowBm(lami));
     }
-    lami = Pow(c.am_i * c.cig[1] * c.oig1 * L.ni / L.ri, c.obmi);
+    lami = PowObm(c.am_i * c.cig[1] * c.oig1 * L.ni / L.ri, c.obmi);
     xdi = (R(bm_i) + R(mu_i) + R(1.0)) / lami;
     if (under_clamp(xdi, R(5.e-6))) {
       hit_limit = true;
       lami = c.cie[1] / R(5.e-6);
-      L.ni = Min(R(max_ni), c.cig[0] * c.oig2 * L.ri / c.am_i * Pow(lami, R(bm_i)));
+      L.ni = Min(R(max_ni), c.cig[0] * c.oig2 * L.ri / c.am_i * PowBm(lami));
     } else if (over_clamp(xdi, R(d0s))) {
       hit_limit = true;
       lami = c.cie[1] / R(d0s);
-      L.ni = c.cig[0] * c.oig2 * L.ri / c.am_i * Pow(lami, R(bm_i));
+      L.ni = c.cig[0] * c.oig2 * L.ri / c.am_i * PowBm(lami);
     }
     if (hit_limit) L.niten = (L.ni / rho - n) * odt;
-    n = Max(R(r2) / rho, Min(c.cig[0] * c.oig2 * q / c.am_i * Pow(lami, R(bm_i)), R(max_ni) / rho));
+    n = Max(R(r2) / rho, Min(c.cig[0] * c.oig2 * q / c.am_i * PowBm(lami), R(max_ni) / rho));
     L.ilami = R(1.0) / lami;
     TG_TRACE(L, TR_CHECK + L.tpass, TB_QI | (hit_limit ? TB_QI_HIT : 0));
   } else {
@@ -586,23 +625,23 @@ __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R od
         hit_limit = true;
         L.mvd_g = R(1.5e-3);
         lamg = (R(3.0) + R(mu_g) + R(0.672)) / L.mvd_g;
-        L.ng = c.cgg[0][1] * c.ogg3 * L.rg * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
+        L.ng = c.cgg[0][1] * c.ogg3 * L.rg * PowBm(lamg) / c.am_g[ig - 1];
       }
-      lamg = Pow(c.am_g[ig - 1] * c.cgg[0][2] * c.ogg2 * L.ng / L.rg, c.obmg);
+      lamg = PowObm(c.am_g[ig - 1] * c.cgg[0][2] * c.ogg2 * L.ng / L.rg, c.obmg);
       L.mvd_g = (R(3.0) + R(mu_g) + R(0.672)) / lamg;
       if (over_clamp(L.mvd_g, R(25.4e-3))) {
         hit_limit = true;
         L.mvd_g = R(25.4e-3);
         lamg = (R(3.0) + R(mu_g) + R(0.672)) / L.mvd_g;
-        L.ng = c.cgg[0][1] * c.ogg3 * L.rg * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
+        L.ng = c.cgg[0][1] * c.ogg3 * L.rg * PowBm(lamg) / c.am_g[ig - 1];
       } else if (under_clamp(L.mvd_g, R(d0r))) {
         hit_limit = true;
         L.mvd_g = R(d0r);
         lamg = (R(3.0) + R(mu_g) + R(0.672)) / L.mvd_g;
-        L.ng = c.cgg[0][1] * c.ogg3 * L.rg * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
+        L.ng = c.cgg[0][1] * c.ogg3 * L.rg * PowBm(lamg) / c.am_g[ig - 1];
       }
       if (hit_limit) L.ngten = (L.ng / rho - n) * odt;
-      n = c.cgg[0][1] * c.ogg3 * q * Pow(lamg, R(bm_g)) / c.am_g[ig - 1];
+      n = c.cgg[0][1] * c.ogg3 * q * PowBm(lamg) / c.am_g[ig - 1];
       const R b_hi = R(meters3_to_liters) * q / rho_g<R>(1);
       b = Min(Max(q * R(meters3_to_liters) / rho_g<R>(nrhg), updated(b, L.qbten, dt, L.qbmag)), b_hi);
       L.idx_bg = density_class(R(10.0) * q / b, b, b_hi);
@@ -611,9 +650,9 @@ __device__ void graupel_check(Lev<R>& L, R& q, R& n, R& b, bool hail, R dt, R od
       R ygra1 = Log10(Max(R(1.e-9), L.rg));
       R zans1 = R(3.4) + R(2.0 / 7.0) * (ygra1 + R(8.0));
       R n0_exp = Max(R(gonv_min), Min(Pow10(zans1), R(gonv_max)));
-      R lam_exp = Pow(n0_exp * c.am_g[idx_bg1 - 1] * c.cgg[0][0] / L.rg, c.oge1);
+      R lam_exp = PowOge1(n0_exp * c.am_g[idx_bg1 - 1] * c.cgg[0][0] / L.rg, c.oge1);
       lamg = lam_exp * c.graupel_lam_k;
-      L.ng = c.cgg[0][1] * c.ogg3 * L.rg * Pow(lamg, R(bm_g)) / c.am_g[idx_bg1 - 1];
+      L.ng = c.cgg[0][1] * c.ogg3 * L.rg * PowBm(lamg) / c.am_g[idx_bg1 - 1];
       L.rb = R(meters3_to_liters) * L.rg / rho_g<R>(idx_bg1);
     }
     L.ilamg = R(1.0) / lamg;
@@ -649,7 +688,7 @@ __device__ __forceinline__ void graupel_init(Lev<R>& L) {
     int idx = max(1, min(Nint(R(10.0) * rg / rb) + 1, nrhg));
     R mvd_g = R(5.e-3);
     R lamg = (R(3.0) + R(mu_g) + R(0.672)) / mvd_g;
-    R ng = c.cgg[0][1] * c.ogg3 * rg * Pow(lamg, R(bm_g)) / c.am_g[idx - 1];
+    R ng = c.cgg[0][1] * c.ogg3 * rg * PowBm(lamg) / c.am_g[idx - 1];
     L.ng1d = ng / rho;
     L.qb1d = rb / rho;
   }
@@ -676,7 +715,7 @@ __device__ bool thermo(Lev<R>& L) {
   if (Fabs(L.ssatw) < eps) L.ssatw = I(0.0);
   if (Fabs(L.ssati) < eps) L.ssati = I(0.0);
   R rtc = R(tempc);
-  L.diffu = R(2.11e-5) * Pow(R(L.temp / t0), R(1.94)) * (R(101325.0) / L.pres);
+  L.diffu = R(2.11e-5) * PowNear1(R(L.temp / t0), R(1.94)) * (R(101325.0) / L.pres);
   if (tempc >= 0.0)
     L.visco = (R(1.718) + R(0.0049) * rtc) * R(1.0e-5);
   else

@@ -133,7 +133,7 @@ __device__ void warm_rain(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, 
       TG_TRACE(L, TR_RW, 1 << 17);
       int nu_c = get_nuc(L.nc);
       R lamc = R(1.0) / L.ilamc;
-      R xdc = Max(R(d0c) * R(1.e6), (Pow(L.rc / (c.am_r * L.nc), c.obmr)) * R(1.e6));
+      R xdc = Max(R(d0c) * R(1.e6), (PowObm(L.rc / (c.am_r * L.nc), c.obmr)) * R(1.e6));
       R dc_g = (c.dc_g_k[nu_c - 1] / lamc) * R(1.e6);
       R dc_b = Pow(xdc * xdc * xdc * dc_g * dc_g * dc_g - xdc * xdc * xdc * xdc * xdc * xdc,
                    R(1.0) / R(6.0));
@@ -384,7 +384,7 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>&
     TG_RANGE(L, RG_ICE, idx_i, 1, ntb_i);
     TG_RANGE(L, RG_ICE, idx_i1, 1, ntb_i1);
     R xdi = Max(R(c.d0i), (R(bm_i) + R(mu_i) + R(1.)) * L.ilami);
-    R xmi = c.am_i * Pow(xdi, R(bm_i));
+    R xmi = c.am_i * PowBm(xdi);
     R oxmi = R(1.0) / xmi;
     t.pri_ide = R(c_cube) * t1_subl * L.diffu * ssati * rvs * c.oig1 * c.cig[4] * L.ni * L.ilami;
     const long ii = (idx_i - 1) + (long)(idx_i1 - 1) * ntb_i;
@@ -412,7 +412,7 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>&
     }
     // main:2959-2962 recompute the same xdi/xmi from ilami
     xdi = Max(R(c.d0i), (R(bm_i) + R(mu_i) + R(1.)) * L.ilami);
-    xmi = c.am_i * Pow(xdi, R(bm_i));
+    xmi = c.am_i * PowBm(xdi);
     oxmi = R(1.) / xmi;
     if (L.rs >= c.r_s1) {
       t.prs_sci = c.t1_qs_qi * L.rhof * R(ef_si) * L.ri * L.smoe;
