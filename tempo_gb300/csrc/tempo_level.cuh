@@ -56,6 +56,54 @@ __device__ __forceinline__ double PowObm(double x, double obm) { return pow(x, o
 __device__ __forceinline__ float PowObm(float x, float) { return cbrtf(x); }
 __device__ __forceinline__ double PowOge1(double x, double oge1) { return pow(x, oge1); }
 __device__ __forceinline__ float PowOge1(float x, float) { return sqrtf(sqrtf(x)); }
+// Exponents of the rain and graupel size distributions that the host puts in cre and
+// cge (params:511-523, 558-571), as constants: with the scheme's mu_r = mu_g = 0, bm = 3 and
+// bv_r = 1 all of cre and the entries of cge that do not involve the graupel fall-speed
+// exponent are integers or half-integers (negative entries: depends on bv_g).
+constexpr double kCre[13] = {bm_r + 1.0, mu_r + 1.0, bm_r + mu_r + 1.0, bm_r * 2.0 + mu_r + 1.0,
+                             mu_r + bv_r + 1.0, bm_r + mu_r + bv_r + 1.0,
+                             bm_r * 0.5 + mu_r + bv_r + 1.0, bm_r + mu_r + bv_r + 3.0,
+                             mu_r + bv_r + 3.0, mu_r + 2.0, 0.5 * (bv_r + 5.0 + 2.0 * mu_r),
+                             bm_r * 0.5 + mu_r + 1.0, bm_r * 2.0 + mu_r + bv_r + 1.0};
+constexpr double kCge[12] = {bm_g + 1.0, mu_g + 1.0, bm_g + mu_g + 1.0, bm_g * 2.0 + mu_g + 1.0,
+                             -1.0, -1.0, -1.0, -1.0, -1.0, mu_g + 2.0, -1.0,
+                             bm_g * 0.5 + mu_g + 1.0};
+// x**N and x**(TW/2) for compile-time N and TW: binary powering, one square root for a
+// half-integer, one division for a negative exponent (a few rounding errors)
+template <int N> __device__ __forceinline__ float ipow_ct(float x) {
+  if constexpr (N == 0) {
+    return 1.0f;
+  } else if constexpr (N == 1) {
+    return x;
+  } else {
+    const float h = ipow_ct<N / 2>(x);
+    if constexpr (N % 2) return h * h * x;
+    else return h * h;
+  }
+}
+template <int TW> __device__ __forceinline__ float pow_twice(float x) {
+  constexpr int A = TW < 0 ? -TW : TW;
+  float r = ipow_ct<A / 2>(x);
+  if constexpr (A % 2 != 0) r = r * sqrtf(x);
+  if constexpr (TW < 0) r = 1.0f / r;
+  return r;
+}
+// x**(S kCre[K]) and x**(S kCge[K]) (S = +1 or -1): y is the same exponent as the context
+// holds it, which the FP64 drop-in passes to pow as the reference does; the mixed form
+// multiplies
+template <double const* E, int K, int S> struct FixedExp {
+  static constexpr double e = S * E[K];
+  static constexpr int tw = (int)(2.0 * e);
+  static_assert(e * 2.0 == (double)tw && E[K] >= 0.0, "an integer or half-integer exponent");
+};
+template <int K, int S = 1> __device__ __forceinline__ double PowCre(double x, double y) { return pow(x, y); }
+template <int K, int S = 1> __device__ __forceinline__ float PowCre(float x, float) {
+  return pow_twice<FixedExp<kCre, K, S>::tw>(x);
+}
+template <int K, int S = 1> __device__ __forceinline__ double PowCge(double x, double y) { return pow(x, y); }
+template <int K, int S = 1> __device__ __forceinline__ float PowCge(float x, float) {
+  return pow_twice<FixedExp<kCge, K, S>::tw>(x);
+}
 // x**y where |y log2 x| is below 1 (the diffusivity's (T/t0)**1.94 with T/t0 within
 // [0.7, 1.2]): the mixed form uses the hardware base-2 logarithm and exponential, whose
 // error there is a few ulp; the FP64 drop-in keeps pow
@@ -121,6 +169,16 @@ __device__ __forceinline__ Dual<T, N> PowObm(const Dual<T, N>& a, U obm) {
 template <class T, int N, class U, class = typename std::enable_if<std::is_arithmetic<U>::value>::type>
 __device__ __forceinline__ Dual<T, N> PowOge1(const Dual<T, N>& a, U oge1) {
   return Pow(a, oge1);
+}
+template <int K, int S = 1, class T, int N, class U,
+          class = typename std::enable_if<std::is_arithmetic<U>::value>::type>
+__device__ __forceinline__ Dual<T, N> PowCre(const Dual<T, N>& a, U y) {
+  return Pow(a, y);
+}
+template <int K, int S = 1, class T, int N, class U,
+          class = typename std::enable_if<std::is_arithmetic<U>::value>::type>
+__device__ __forceinline__ Dual<T, N> PowCge(const Dual<T, N>& a, U y) {
+  return Pow(a, y);
 }
 template <class T, int N> __device__ __forceinline__ Dual<T, N> Pow10(const Dual<T, N>& b) {
   return Pow(T(10.0), b);
@@ -694,26 +752,32 @@ __device__ __forceinline__ void graupel_init(Lev<R>& L) {
   }
 }
 
-// thermo_vars (main:1263-1310) for one level; returns ssati > 0
-template <class R>
-__device__ bool thermo(Lev<R>& L) {
+// thermo_vars (main:1263-1310) for one level.  kIce = false leaves out the ice
+// saturation (qvsi, ssati) and delqvs: their readers -- nucleation, ice processes,
+// melting and the over-depletion limiter -- all run in the first stage of phase A, so
+// the calls before saturation adjustment and rain evaporation need them not (the
+// fields keep the first stage's values, which nothing reads again).
+template <class R, bool kIce = true>
+__device__ void thermo(Lev<R>& L) {
   using I = Isl<R>;
   I otemp = 1.0 / L.temp;
   I tempc = L.temp - t0;
   L.rhof = R(Sqrt(L.ci->rho_not / L.rho));
   L.rhof2 = Sqrt(L.rhof);
   L.qvs = calc_rslf(I(L.pres), L.temp);
-  L.delqvs = Max(I(0.0), L.qvs_t0 - L.qv);
-  if (tempc <= 0.0)
-    L.qvsi = calc_rsif(I(L.pres), L.temp);
-  else
-    L.qvsi = L.qvs;
   I satw = L.qv / L.qvs;
-  I sati = L.qv / L.qvsi;
   L.ssatw = satw - 1.0;
-  L.ssati = sati - 1.0;
   if (Fabs(L.ssatw) < eps) L.ssatw = I(0.0);
-  if (Fabs(L.ssati) < eps) L.ssati = I(0.0);
+  if constexpr (kIce) {
+    L.delqvs = Max(I(0.0), L.qvs_t0 - L.qv);
+    if (tempc <= 0.0)
+      L.qvsi = calc_rsif(I(L.pres), L.temp);
+    else
+      L.qvsi = L.qvs;
+    I sati = L.qv / L.qvsi;
+    L.ssati = sati - 1.0;
+    if (Fabs(L.ssati) < eps) L.ssati = I(0.0);
+  }
   R rtc = R(tempc);
   L.diffu = R(2.11e-5) * PowNear1(R(L.temp / t0), R(1.94)) * (R(101325.0) / L.pres);
   if (tempc >= 0.0)
@@ -728,7 +792,6 @@ __device__ bool thermo(Lev<R>& L) {
   L.lvap = lvap;
   L.tcond = (R(5.69) + R(0.0168) * rtc) * R(1.0e-5) * R(418.936);
   L.lvt2 = lvap * lvap * ocp * R(L.ci->orv) * R(otemp) * R(otemp);
-  return L.ssati > 0.0;
 }
 
 // The part of thermo_vars that the fall speeds read after the last stage of phase A

@@ -41,7 +41,7 @@ __device__ __forceinline__ void rain_index(const TempoConsts<C>& c, R rr, R ilam
   idx_r = decade_index(c, rr, c.nir2, ntb_r);
   R lamr = R(1.) / ilamr;
   R lam_exp = lamr * c.rain_n0_k;
-  R n0_exp = c.org1 * rr / c.am_r * Pow(lam_exp, c.cre[0]);
+  R n0_exp = c.org1 * rr / c.am_r * PowCre<0>(lam_exp, c.cre[0]);
   idx_r1 = decade_index(c, n0_exp, c.nir3, ntb_r1);
 }
 // graupel intercept ng ogg2 lamg**cge(2,1) and ilamg**cge(9,idx_bg) (main:2458-2462,
@@ -51,7 +51,7 @@ __device__ __forceinline__ void rain_index(const TempoConsts<C>& c, R rr, R ilam
 template <class R>
 __device__ __forceinline__ R graupel_n0(const Lev<R>& L) {
   if (!(L.psd_have & 1)) {
-    L.psd_n0g = L.ng * L.cs->ogg2 * Pow(R(1.0) / L.ilamg, L.cs->cge[0][1]);
+    L.psd_n0g = L.ng * L.cs->ogg2 * PowCge<1>(R(1.0) / L.ilamg, L.cs->cge[0][1]);
     L.psd_have |= 1;
   }
   return L.psd_n0g;
@@ -68,8 +68,8 @@ template <class R>
 __device__ __forceinline__ void rain_n0_pf9(const Lev<R>& L, R& n0_r, R& pf9) {
   if (!(L.psd_have & 4)) {
     const R lamr = R(1.0) / L.ilamr;
-    L.psd_n0r = L.nr * L.cs->org2 * Pow(lamr, L.cs->cre[1]);
-    L.psd_pf9 = Pow(lamr + R(fv_r), -L.cs->cre[8]);
+    L.psd_n0r = L.nr * L.cs->org2 * PowCre<1>(lamr, L.cs->cre[1]);
+    L.psd_pf9 = PowCre<8, -1>(lamr + R(fv_r), -L.cs->cre[8]);
     L.psd_have |= 4;
   }
   n0_r = L.psd_n0r;
@@ -88,7 +88,7 @@ __device__ __forceinline__ void graupel_index(const TempoConsts<C>& c, R rg, R i
   idx_g = decade_index(c, rg, c.nig2, ntb_g);
   R lamg = R(1.) / ilamg;
   R lam_exp = lamg * c.graupel_n0_k;
-  R n0_exp = c.ogg1 * rg / c.am_g[idx - 1] * Pow(lam_exp, c.cge[0][0]);
+  R n0_exp = c.ogg1 * rg / c.am_g[idx - 1] * PowCge<0>(lam_exp, c.cge[0][0]);
   idx_g1 = decade_index(c, n0_exp, c.nig3, ntb_g1);
 }
 // The bin of a value whose reference index is a non-decreasing function of it built on
@@ -158,10 +158,12 @@ __device__ void warm_rain(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>& T, 
       TG_RANGE(L, RG_EFRW, idx, 1, nbr);
       TG_RANGE(L, RG_EFRW, mc, 1, nbc);
       R ef_rw = ld(T.t_efrw + (idx - 1) + (long)(mc - 1) * nbr);
-      R n0_r = L.nr * c.org2 * Pow(lamr, c.cre[1]);
-      t.prr_rcw = L.rhof * c.t1_qr_qc * ef_rw * L.rc * n0_r * Pow(lamr + R(fv_r), -c.cre[8]);
+      R n0_r = L.nr * c.org2 * PowCre<1>(lamr, c.cre[1]);
+      t.prr_rcw =
+          L.rhof * c.t1_qr_qc * ef_rw * L.rc * n0_r * PowCre<8, -1>(lamr + R(fv_r), -c.cre[8]);
       t.prr_rcw = Min(L.rc * odt, t.prr_rcw);
-      t.pnc_rcw = L.rhof * c.t1_qr_qc * ef_rw * L.nc * n0_r * Pow(lamr + R(fv_r), -c.cre[8]);
+      t.pnc_rcw =
+          L.rhof * c.t1_qr_qc * ef_rw * L.nc * n0_r * PowCre<8, -1>(lamr + R(fv_r), -c.cre[8]);
       t.pnc_rcw = Min(L.nc * odt, t.pnc_rcw);
     }
   }
@@ -427,7 +429,8 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>&
       t.pnr_rci = Min(L.nr * odt, t.pnr_rci);
       t.png_rci = t.pnr_rci * Max(Min((Pow10(-(R(0.1) * w)) + R(0.1)), R(1.0)), R(0.1));
       t.pni_rci = t.pri_rci * oxmi;
-      t.prr_rci = L.rhof * c.t2_qr_qi * R(ef_ri) * L.ni * n0_r * Pow(lamr + R(fv_r), -c.cre[7]);
+      t.prr_rci = L.rhof * c.t2_qr_qi * R(ef_ri) * L.ni * n0_r *
+                  PowCre<7, -1>(lamr + R(fv_r), -c.cre[7]);
       t.prr_rci = Min(L.rr * odt, t.prr_rci);
       t.prg_rci = t.pri_rci + t.prr_rci;
       t.pbg_rci = t.prg_rci / R(rho_i);
@@ -449,7 +452,7 @@ __device__ void ice_processes(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>&
       R n0_g = graupel_n0(L);
       R t2_qg_sd = R(0.28) * c.sc3 * Sqrt(c.av_g[ig - 1]) * c.cgg[ig - 1][10];
       t.prg_gde = R(c_cube) * t1_subl * L.diffu * ssati * rvs * n0_g *
-                  (c.t1_qg_sd * Pow(L.ilamg, c.cge[0][9]) +
+                  (c.t1_qg_sd * PowCge<9>(L.ilamg, c.cge[0][9]) +
                    t2_qg_sd * L.vsc2 * L.rhof2 * Pow(L.ilamg, c.cge[ig - 1][10]));
       if (t.prg_gde < R(0.0)) {
         t.prg_gde = Max3(-L.rg * odt, t.prg_gde, rate_max);
@@ -581,11 +584,11 @@ __device__ void melting(const Lev<R>& L, Tend<R>& t, R t1_subl, uint32_t f, R dt
     R n0_melt = n0_g;
     if ((L.rg * L.ng) < R(1.e-4)) {
       R lamg = R(1.) / L.ilamg;
-      n0_melt = (R(1.e-4) / L.rg) * c.ogg2 * Pow(lamg, c.cge[0][1]);
+      n0_melt = (R(1.e-4) / L.rg) * c.ogg2 * PowCge<1>(lamg, c.cge[0][1]);
     }
     R sqav = Sqrt(c.av_g[ig - 1]);
     R t2_qg_me = R(pi) * R(4.0) * R(c_cube) * c.olfus * R(0.28) * c.sc3 * sqav * c.cgg[ig - 1][10];
-    R p10 = Pow(L.ilamg, c.cge[0][9]);
+    R p10 = PowCge<9>(L.ilamg, c.cge[0][9]);
     R p11 = Pow(L.ilamg, c.cge[ig - 1][10]);
     t.prr_gml = (tempc * L.tcond - R(lvap0) * L.diffu * delqvs) * n0_melt *
                 (c.t1_qg_me * p10 + t2_qg_me * L.rhof2 * L.vsc2 * p11);
@@ -881,6 +884,16 @@ __device__ void cloud_condensation(const Lev<R>& L, Tend<R>& t, const Tables<Cst
   if (Fabs(L.ssatw) < eps) return;
   using I = Isl<R>;
   R orho = R(1.0 / L.rho);
+  if (L.ssatw < 0.0 && L.rc <= R(r1)) {
+    // Subsaturated without cloud water: the Newton iterations below start at
+    // (qv - qvs) / (1 + lvt2 qvs) < 0 and, on a convex increasing function, approach
+    // its negative root from the right, so the condensed amount stays negative and
+    // rc + clap rho <= r1: the branch that removes the (absent) cloud, taken here
+    // without the iterations.
+    t.prw_vcd = -(L.rc * orho * odt);
+    t.pnc_wcd = -(L.nc * orho * odt);
+    return;
+  }
   I clap;
   if constexpr (std::is_same<I, df>::value) {
     // Mixed form: the cancellation sits in qv - qvs, formed once in the island type; the
@@ -974,10 +987,10 @@ __device__ void rain_evaporation(const Lev<R>& L, Tend<R>& t, R odt) {
     t.prv_rev = L.rr * orho * odt;
   } else {
     R lamr = R(1.0) / L.ilamr;
-    R n0_r = L.nr * c.org2 * Pow(lamr, c.cre[1]);
+    R n0_r = L.nr * c.org2 * PowCre<1>(lamr, c.cre[1]);
     t.prv_rev = t1_evap * L.diffu * R(-L.ssatw) * n0_r * rvs *
-                (c.t1_qr_ev * Pow(L.ilamr, c.cre[9]) +
-                 c.t2_qr_ev * L.vsc2 * L.rhof2 * Pow(lamr + R(0.5) * R(fv_r), -c.cre[10]));
+                (c.t1_qr_ev * PowCre<9>(L.ilamr, c.cre[9]) +
+                 c.t2_qr_ev * L.vsc2 * L.rhof2 * PowCre<10, -1>(lamr + R(0.5) * R(fv_r), -c.cre[10]));
     R rate_max = Min((L.rr * orho * odt), R((L.qvs - L.qv) * Isl<R>(odt)));
     t.prv_rev = Min(rate_max, t.prv_rev * orho);
     if (t.prr_gml > R(0.0)) {
@@ -1000,17 +1013,17 @@ __device__ void reflectivity_parts(const Lev<R>& L, R& ze_r, R& ze_s, R& ze_g) {
   ze_g = R(1.e-22);
   if (L.l_qr) {
     R lamr = R(1.0) / L.ilamr;
-    R n0_r = L.nr * c.org2 * Pow(lamr, c.cre[1]);
-    ze_r = n0_r * c.crg[3] * Pow(L.ilamr, c.cre[3]);
+    R n0_r = L.nr * c.org2 * PowCre<1>(lamr, c.cre[1]);
+    ze_r = n0_r * c.crg[3] * PowCre<3>(L.ilamr, c.cre[3]);
   }
   if (L.l_qs)
     ze_s = R(0.176 / 0.93) * (R(6.0) / R(pi)) * (R(6.0) / R(pi)) * (R(am_s) / R(900.0)) *
            (R(am_s) / R(900.0)) * L.smoz;
   if (L.l_qg) {
     const int ig = L.idx_bg;
-    R n0_g = L.ng * c.ogg2 * Pow(R(1.0) / L.ilamg, c.cge[0][1]);
+    R n0_g = L.ng * c.ogg2 * PowCge<1>(R(1.0) / L.ilamg, c.cge[0][1]);
     ze_g = R(0.176 / 0.93) * (R(6.0) / R(pi)) * (R(6.0) / R(pi)) * (c.am_g[ig - 1] / R(900.0)) *
-           (c.am_g[ig - 1] / R(900.0)) * n0_g * c.cgg[0][3] * Pow(L.ilamg, c.cge[0][3]);
+           (c.am_g[ig - 1] / R(900.0)) * n0_g * c.cgg[0][3] * PowCge<3>(L.ilamg, c.cge[0][3]);
   }
 }
 template <class R>
@@ -1027,7 +1040,7 @@ __device__ R max_hail_diam(const Lev<R>& L) {  // diags:398-438
   if (!(L.rg / R(L.rho) >= R(1.e-6))) return R(0.0);
   if (rho_gd(L.idx_bg) < 350.0) return R(0.0);
   R lamg = R(1.0) / L.ilamg;
-  R n0_g = L.ng * c.ogg2 * Pow(lamg, c.cge[0][1]);
+  R n0_g = L.ng * c.ogg2 * PowCge<1>(lamg, c.cge[0][1]);
   R sum_nh = R(0.0), sum_t = R(0.0), hail_max;
   int n;
   for (n = nhbins; n >= 1; n--) {

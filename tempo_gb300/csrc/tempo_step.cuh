@@ -562,8 +562,10 @@ __host__ __device__ constexpr int points_min_blocks(int v) {
 template <class R>
 __device__ __forceinline__ void rain_speeds(const Lev<R>& L, const TempoConsts<Cst<R>>& cc, R& vt, R& vtn) {
   R lamr = R(1.0) / L.ilamr;
-  vt = L.rhof * R(av_r) * cc.crg[5] * cc.org3 * Pow(lamr, cc.cre[2]) * Pow(lamr + R(fv_r), -cc.cre[5]);
-  vtn = L.rhof * R(av_r) * cc.crg[6] / cc.crg[11] * Pow(lamr, cc.cre[11]) * Pow(lamr + R(fv_r), -cc.cre[6]);
+  vt = L.rhof * R(av_r) * cc.crg[5] * cc.org3 * PowCre<2>(lamr, cc.cre[2]) *
+       PowCre<5, -1>(lamr + R(fv_r), -cc.cre[5]);
+  vtn = L.rhof * R(av_r) * cc.crg[6] / cc.crg[11] * PowCre<11>(lamr, cc.cre[11]) *
+        PowCre<6, -1>(lamr + R(fv_r), -cc.cre[6]);
 }
 // the same for graupel (graupel_fallspeed, main:1817-1833), density-dependent with qb
 template <class R>
@@ -654,13 +656,13 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   thermo(L);
   points_stage<R, kSync>(0, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in, go);
   if (do_cond) {
-    thermo(L);
+    thermo<R, false>(L);
     points_stage<R, kSync>(1, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in, go);
     block_sync<kSync>(go);
   }
   if (do_evap) {
     if (L.l_qr)
-      thermo(L);
+      thermo<R, false>(L);
     else
       thermo_tail(L);
     points_stage<R, kSync>(2, L, td, T, ci, f, w, dt, odt, dti, ncsave, ncsave_cond, nwfa_in, nifa_in, go);
