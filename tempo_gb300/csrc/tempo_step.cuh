@@ -943,7 +943,8 @@ __device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dz
 // (rain and snow -- snow's fall speed reads rain's state after rain sedimentation --
 // and graupel, ice and cloud), twice the threads for the same serial chains; v < 6
 // runs a species' substeps level by level (sweep_all) where the warp's substep counts
-// fit its register history, v >= 6 always substep by substep.
+// fit its register history, v >= 6 always substep by substep.  In the level-by-level
+// walk, v % 3 > 0 issues the next level's loads while a level runs its substeps.
 constexpr int kSedimVariants = 12;
 __host__ __device__ constexpr int sedim_group(int v) { return v % 3 + 1; }
 __host__ __device__ constexpr bool sedim_split(int v) { return (v / 3) % 2 == 1; }
@@ -1199,38 +1200,110 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
         }
       }
     }
-    for (int k = ktop - 1; k >= 0; k--) {
-      const long o = (long)k * kSlotTile;
-      I fo, fr;
-      if constexpr (kMixed) {
-        fo = odz[o];
-        fr = ozr[o];
-      } else {
-        fo = 1.0 / ldi<I>(dzp + (long)k * NI);
-        fr = 1.0 / rho[o];
-      }
-#pragma unroll
-      for (int f = 0; f < NF; f++) {
-        I xk = x[f][o], tk = ten[f][o];
-        const I v = I(vt[f][o]);
-#pragma unroll
-        for (int n = 0; n < SM; n++)
-          if (n < steps) {
-            const I s_k = v * xk;
-            if constexpr (kMixed) {
-              const I dflux = hist[f][n] - s_k;
-              tk = tk + dflux * fr * osteps;
-              xk = Max(lim[f], xk + dflux * fo * cx);
-            } else {
-              tk = tk + (hist[f][n] - s_k) * fo * osteps * fr;
-              xk = Max(lim[f], xk + (hist[f][n] - s_k) * fo * dti * osteps);
+    // Levels ktop-1 .. 0.  G >= 2: each level's loads are issued one level ahead (while
+    // the level above runs its substeps), so the column walk does not wait a memory
+    // round trip per level, at the cost of registers; G = 1: loaded when reached.
+    if constexpr (G >= 2) {
+      I cx_[NF], ct_[NF], ca = I(0.0), cb = I(0.0);
+      R cv_[NF];
+      auto load_level = [&](int k, I* xx, I* tt, R* vv, I& a, I& b) {
+        const long o = (long)k * kSlotTile;
+        if constexpr (kMixed) {
+          a = odz[o];
+          b = ozr[o];
+        } else {
+          a = ldi<I>(dzp + (long)k * NI);
+          b = rho[o];
+        }
+  #pragma unroll
+        for (int f = 0; f < NF; f++) {
+          xx[f] = x[f][o];
+          tt[f] = ten[f][o];
+          vv[f] = vt[f][o];
+        }
+      };
+      if (ktop >= 1) load_level(ktop - 1, cx_, ct_, cv_, ca, cb);
+      for (int k = ktop - 1; k >= 0; k--) {
+        I nx_[NF], nt_[NF], na = I(0.0), nb = I(0.0);
+        R nv_[NF];
+        if (k >= 1) load_level(k - 1, nx_, nt_, nv_, na, nb);
+        const long o = (long)k * kSlotTile;
+        I fo, fr;
+        if constexpr (kMixed) {
+          fo = ca;
+          fr = cb;
+        } else {
+          fo = 1.0 / ca;
+          fr = 1.0 / cb;
+        }
+  #pragma unroll
+        for (int f = 0; f < NF; f++) {
+          I xk = cx_[f], tk = ct_[f];
+          const I v = I(cv_[f]);
+  #pragma unroll
+          for (int n = 0; n < SM; n++)
+            if (n < steps) {
+              const I s_k = v * xk;
+              if constexpr (kMixed) {
+                const I dflux = hist[f][n] - s_k;
+                tk = tk + dflux * fr * osteps;
+                xk = Max(lim[f], xk + dflux * fo * cx);
+              } else {
+                tk = tk + (hist[f][n] - s_k) * fo * osteps * fr;
+                xk = Max(lim[f], xk + (hist[f][n] - s_k) * fo * dti * osteps);
+              }
+              hist[f][n] = s_k;
+              if (k == 0 && f == 0 && precip && xk > low_limit_mass_for_precip)
+                *precip = *precip + s_k * dti * osteps;
             }
-            hist[f][n] = s_k;
-            if (k == 0 && f == 0 && precip && xk > low_limit_mass_for_precip)
-              *precip = *precip + s_k * dti * osteps;
+          ten[f][o] = tk;
+          x[f][o] = xk;
+        }
+        if (k >= 1) {
+  #pragma unroll
+          for (int f = 0; f < NF; f++) {
+            cx_[f] = nx_[f];
+            ct_[f] = nt_[f];
+            cv_[f] = nv_[f];
           }
-        ten[f][o] = tk;
-        x[f][o] = xk;
+          ca = na;
+          cb = nb;
+        }
+      }
+    } else {
+      for (int k = ktop - 1; k >= 0; k--) {
+        const long o = (long)k * kSlotTile;
+        I fo, fr;
+        if constexpr (kMixed) {
+          fo = odz[o];
+          fr = ozr[o];
+        } else {
+          fo = 1.0 / ldi<I>(dzp + (long)k * NI);
+          fr = 1.0 / rho[o];
+        }
+  #pragma unroll
+        for (int f = 0; f < NF; f++) {
+          I xk = x[f][o], tk = ten[f][o];
+          const I v = I(vt[f][o]);
+  #pragma unroll
+          for (int n = 0; n < SM; n++)
+            if (n < steps) {
+              const I s_k = v * xk;
+              if constexpr (kMixed) {
+                const I dflux = hist[f][n] - s_k;
+                tk = tk + dflux * fr * osteps;
+                xk = Max(lim[f], xk + dflux * fo * cx);
+              } else {
+                tk = tk + (hist[f][n] - s_k) * fo * osteps * fr;
+                xk = Max(lim[f], xk + (hist[f][n] - s_k) * fo * dti * osteps);
+              }
+              hist[f][n] = s_k;
+              if (k == 0 && f == 0 && precip && xk > low_limit_mass_for_precip)
+                *precip = *precip + s_k * dti * osteps;
+            }
+          ten[f][o] = tk;
+          x[f][o] = xk;
+        }
       }
     }
     if (ktop == 0 && nz > 1 && precip) {  // level 0 above the fall: its flux, unchanged
