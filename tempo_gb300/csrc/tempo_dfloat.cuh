@@ -19,7 +19,8 @@
 
 namespace tg {
 
-struct df {
+// 8-byte aligned, so that a value in a scratch plane moves with one 64-bit load or store
+struct __align__(8) df {
   float hi, lo;
   df() = default;
   __host__ __device__ constexpr df(float h, float l) : hi(h), lo(l) {}
