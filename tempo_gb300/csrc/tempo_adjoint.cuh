@@ -65,6 +65,13 @@ struct AdjIO {
   template <class X> __device__ __forceinline__ void sd(X*, long idx, const X& v) const {
     contract(j.lam_sd[idx], v);
   }
+  // the bulk-type planes of the sedimenting fields (R = I in the derivative types)
+  template <class I, class R> __device__ __forceinline__ void sx(long fsd, int f, long o, const R& v) const {
+    contract(j.lam_sd[(long)f * fsd + o], v);
+  }
+  template <class O, class I> __device__ __forceinline__ O sxin(long fsd, int f, long o, int id) const {
+    return seed<O>(j.psd[(long)f * fsd + o].v, id);
+  }
   template <class X> __device__ __forceinline__ void sr(X*, long idx, const X& v) const {
     contract(j.lam_sr[idx], v);
   }

@@ -55,6 +55,14 @@ struct FwdIO {
     return reinterpret_cast<const E*>(a.sc)[idx];
   }
   template <class X> __device__ __forceinline__ void sd(X* base, long idx, const X& v) const { base[idx] = v; }
+  // the sedimenting fields and their tendencies: scratch planes (island-type slots) that
+  // hold values of the bulk type R, in the first sizeof(R) / sizeof(I) of each plane
+  template <class I, class R> __device__ __forceinline__ void sx(long fsd, int f, long o, const R& v) const {
+    reinterpret_cast<R*>(reinterpret_cast<I*>(a.sd) + (long)f * fsd)[o] = v;
+  }
+  template <class R, class I> __device__ __forceinline__ R sxin(long fsd, int f, long o, int) const {
+    return reinterpret_cast<const R*>(reinterpret_cast<const I*>(a.sd) + (long)f * fsd)[o];
+  }
   template <class X> __device__ __forceinline__ void sr(X* base, long idx, const X& v) const { base[idx] = v; }
   __device__ __forceinline__ void pmask(long o, uint8_t m) const { a.pmask[o] = m; }
   template <class V> __device__ __forceinline__ void diag3(S* p, long e3, const V& v) const {
@@ -716,26 +724,26 @@ __device__ __forceinline__ void points_point(const StepArgs<S>& a, const Tables<
   io.sd(sd, SD_TTEN * fsd + o, I(L.tten));
   io.sd(sd, SD_QV * fsd + o, I(L.qv));
   io.sd(sd, SD_RHO * fsd + o, I(L.rho));
-  io.sd(sd, SD_XRR * fsd + o, I(I(L.rr)));
-  io.sd(sd, SD_XNR * fsd + o, I(I(L.nr)));
-  io.sd(sd, SD_XRG * fsd + o, I(I(L.rg)));
-  io.sd(sd, SD_XNG * fsd + o, I(I(L.ng)));
-  io.sd(sd, SD_XRB * fsd + o, I(I(L.rb)));
-  io.sd(sd, SD_XRS * fsd + o, I(I(L.rs)));
-  io.sd(sd, SD_XRI * fsd + o, I(I(L.ri)));
-  io.sd(sd, SD_XNI * fsd + o, I(I(L.ni)));
-  io.sd(sd, SD_XRC * fsd + o, I(I(L.rc)));
-  io.sd(sd, SD_XNC * fsd + o, I(I(L.nc)));
-  io.sd(sd, SD_TQR * fsd + o, I(I(L.qrten)));
-  io.sd(sd, SD_TNR * fsd + o, I(I(L.nrten)));
-  io.sd(sd, SD_TQG * fsd + o, I(I(L.qgten)));
-  io.sd(sd, SD_TNG * fsd + o, I(I(L.ngten)));
-  io.sd(sd, SD_TQB * fsd + o, I(I(L.qbten)));
-  io.sd(sd, SD_TQS * fsd + o, I(I(L.qsten)));
-  io.sd(sd, SD_TQI * fsd + o, I(I(L.qiten)));
-  io.sd(sd, SD_TNI * fsd + o, I(I(L.niten)));
-  io.sd(sd, SD_TQC * fsd + o, I(I(L.qcten)));
-  io.sd(sd, SD_TNC * fsd + o, I(I(L.ncten)));
+  io.template sx<I>(fsd, SD_XRR, o, R(L.rr));
+  io.template sx<I>(fsd, SD_XNR, o, R(L.nr));
+  io.template sx<I>(fsd, SD_XRG, o, R(L.rg));
+  io.template sx<I>(fsd, SD_XNG, o, R(L.ng));
+  io.template sx<I>(fsd, SD_XRB, o, R(L.rb));
+  io.template sx<I>(fsd, SD_XRS, o, R(L.rs));
+  io.template sx<I>(fsd, SD_XRI, o, R(L.ri));
+  io.template sx<I>(fsd, SD_XNI, o, R(L.ni));
+  io.template sx<I>(fsd, SD_XRC, o, R(L.rc));
+  io.template sx<I>(fsd, SD_XNC, o, R(L.nc));
+  io.template sx<I>(fsd, SD_TQR, o, R(L.qrten));
+  io.template sx<I>(fsd, SD_TNR, o, R(L.nrten));
+  io.template sx<I>(fsd, SD_TQG, o, R(L.qgten));
+  io.template sx<I>(fsd, SD_TNG, o, R(L.ngten));
+  io.template sx<I>(fsd, SD_TQB, o, R(L.qbten));
+  io.template sx<I>(fsd, SD_TQS, o, R(L.qsten));
+  io.template sx<I>(fsd, SD_TQI, o, R(L.qiten));
+  io.template sx<I>(fsd, SD_TNI, o, R(L.niten));
+  io.template sx<I>(fsd, SD_TQC, o, R(L.qcten));
+  io.template sx<I>(fsd, SD_TNC, o, R(L.ncten));
   if constexpr (std::is_same<I, df>::value) {
     // the mixed form's sedimentation multiplies by these instead of dividing per sweep
     const I odz = 1.0 / ldi<I>(a.dz + e);
@@ -804,11 +812,12 @@ __global__ void __launch_bounds__(points_block(V), points_min_blocks(V)) tempo_p
 // sedim: phase B for one active column
 // ---------------------------------------------------------------------------------
 // semilagrangian_sedimentation (main:1562-1749), the scheme of Juang and Hong (2010),
-// Mon. Wea. Rev. 138, 1778-1791, on one column: x and ten are level planes (stride ls),
-// vt the filled speeds (vt(nz + 1) = 0), w the column's work rows (row stride wr, level
-// stride wl).  Indices below are the reference's, 1-based.
+// Mon. Wea. Rev. 138, 1778-1791, on one column: x and ten are level planes of the bulk
+// type (stride ls; the substep runs in the island type and stores its results), vt the
+// filled speeds (vt(nz + 1) = 0), w the column's work rows (row stride wr, level stride
+// wl).  Indices below are the reference's, 1-based.
 template <class R, class I, class S>
-__device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dzp, long NI,
+__device__ void sl_sweep(int nz, R* x, R* ten, const R* vt, long ls, const S* dzp, long NI,
                          const I* rho, I* w, long wr, long wl, int steps, double limit, I* precip,
                          I dt, I odt) {
   auto row = [&](int r, int i) -> I& { return w[(long)r * wr + (long)(i - 1) * wl]; };
@@ -822,9 +831,8 @@ __device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dz
   auto X0 = [&](int i) -> I& { return row(7, i); };
   auto VT = [&](int i) -> I { return i <= nz ? I(vt[(long)(i - 1) * ls]) : I(0.0); };
   auto DZ = [&](int i) -> I { return ldi<I>(dzp + (long)(i - 1) * NI); };
-  auto XR = [&](int i) -> I& { return x[(long)(i - 1) * ls]; };
   const I osteps = 1.0 / I(steps), fsteps = I(steps);
-  for (int k = 1; k <= nz; k++) X0(k) = XR(k);
+  for (int k = 1; k <= nz; k++) X0(k) = I(x[(long)(k - 1) * ls]);
   ZI(1) = I(0.0);
   for (int k = 1; k <= nz; k++) ZI(k + 1) = ZI(k) + DZ(k);
   // 3rd-order interpolation of the interface speeds (:1599-1611)
@@ -846,7 +854,7 @@ __device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dz
   for (int k = 1; k <= nz + 1; k++) ZA(k) = ZI(k) - WI(k) * dt * osteps;
   ZA(nz + 2) = ZI(nz + 1);
   for (int k = 1; k <= nz + 1; k++) DZA(k) = ZA(k + 1) - ZA(k);
-  for (int k = 1; k <= nz; k++) QA(k) = XR(k) * DZ(k) / DZA(k);
+  for (int k = 1; k <= nz; k++) QA(k) = X0(k) * DZ(k) / DZA(k);
   QA(nz + 1) = I(0.0);
   // interface values with the reference's monotonicity test (:1638-1659)
   for (int k = 2; k <= nz; k++) {
@@ -885,6 +893,7 @@ __device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dz
         break;
       }
     kt = kt - 1;
+    I xr = X0(k);
     if (kt == kb) {
       const I tl = (ZI(k) - ZA(kb)) / DZA(kb);
       const I th = (ZI(k + 1) - ZA(kb)) / DZA(kb);
@@ -892,7 +901,7 @@ __device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dz
       const I qqd = 0.5 * (QPI(kb) - QMI(kb));
       const I qqh = qqd * th2 + QMI(kb) * th;
       const I qql = qqd * tl2 + QMI(kb) * tl;
-      XR(k) = (qqh - qql) / (th - tl);
+      xr = (qqh - qql) / (th - tl);
     } else if (kt > kb) {
       const I tl = (ZI(k) - ZA(kb)) / DZA(kb);
       const I tl2 = tl * tl;
@@ -912,11 +921,12 @@ __device__ void sl_sweep(int nz, I* x, I* ten, const R* vt, long ls, const S* dz
       const I dqh = qqd * th2 + QMI(kt) * th;
       zsum = zsum + th * DZA(kt);
       qsum = qsum + dqh * DZA(kt);
-      XR(k) = qsum / zsum;
+      xr = qsum / zsum;
     }
     const I orho = 1.0 / rho[(long)(k - 1) * ls];
-    XR(k) = XR(k) > limit ? XR(k) : I(limit);
-    ten[(long)(k - 1) * ls] = ten[(long)(k - 1) * ls] + (XR(k) - X0(k)) * orho * odt;
+    xr = xr > limit ? xr : I(limit);
+    ten[(long)(k - 1) * ls] = R(I(ten[(long)(k - 1) * ls]) + (xr - X0(k)) * orho * odt);
+    x[(long)(k - 1) * ls] = R(xr);
   }
   // mass through the surface (:1725-1739)
   for (int k = 1; k <= nz; k++) {
@@ -963,6 +973,10 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
   const long cs = a.ncol_pad, fsd = (long)nz * cs;
   I* sd = reinterpret_cast<I*>(a.sd) + pt_base(s, nz);
   R* sr = reinterpret_cast<R*>(a.sr) + pt_base(s, nz);
+  // this slot's level 0 in the plane of a sedimenting field or its tendency: values of
+  // the bulk type R (in the mixed form FP32 in the first half of the plane); the walks
+  // below keep them in the island type between the loads and stores
+  auto xp = [&](int f) -> R* { return reinterpret_cast<R*>(reinterpret_cast<I*>(a.sd) + (long)f * fsd) + pt_base(s, nz); };
   const R dt = step_dt<R>(a);
   const I dti = step_dti<R>(a);
   const S* dzp = a.dz + g.base;
@@ -987,8 +1001,8 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
         if (A >= R(0)) {
           if (sr[SR_VTSB * fsd + o] != R(0)) {
             R vrain = any_qr ? sr[SR_VTR * fsd + o] : R(0);
-            R rsk = R(sd[SD_XRS * fsd + o]);
-            R srr = rsk / (rsk + R(sd[SD_XRR * fsd + o]));
+            R rsk = xp(SD_XRS)[o];
+            R srr = rsk / (rsk + xp(SD_XRR)[o]);
             v = A * srr + (R(1.0) - srr) * vrain;
           } else {
             v = A;
@@ -1028,14 +1042,14 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
                    int steps, int ktop, I* precip) {
     constexpr int NF = decltype(nf)::value;
     constexpr bool kMixed = std::is_same<I, df>::value;
-    I* x[NF];
-    I* ten[NF];
+    R* x[NF];
+    R* ten[NF];
     const R* vt[NF];
     I lim[NF], s_up[NF], s0[NF];
 #pragma unroll
     for (int f = 0; f < NF; f++) {
-      x[f] = sd + fx[f] * fsd;
-      ten[f] = sd + ften[f] * fsd;
+      x[f] = xp(fx[f]);
+      ten[f] = xp(ften[f]);
       vt[f] = sr + fv[f] * fsd;
       lim[f] = I(limit[f]);
     }
@@ -1058,16 +1072,17 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
       }
 #pragma unroll
       for (int f = 0; f < NF; f++) {
-        const I s_top = I(vt[f][o]) * x[f][o];
+        const I xt = I(x[f][o]), tt = I(ten[f][o]);
+        const I s_top = I(vt[f][o]) * xt;
         if constexpr (kMixed) {
-          ten[f][o] = ten[f][o] - s_top * fr * osteps;
-          x[f][o] = Max(lim[f], x[f][o] - s_top * fo * cx);
+          ten[f][o] = R(tt - s_top * fr * osteps);
+          x[f][o] = R(Max(lim[f], xt - s_top * fo * cx));
         } else {
-          ten[f][o] = ten[f][o] - s_top * fo * osteps * fr;
-          x[f][o] = Max(lim[f], x[f][o] - s_top * fo * dti * osteps);
+          ten[f][o] = R(tt - s_top * fo * osteps * fr);
+          x[f][o] = R(Max(lim[f], xt - s_top * fo * dti * osteps));
         }
-        s_up[f] = (ktop == nz - 1) ? s_top : I(vt[f][ktop * kSlotTile]) * x[f][ktop * kSlotTile];
-        s0[f] = (nz == 1) ? s_top : I(vt[f][0]) * x[f][0];
+        s_up[f] = (ktop == nz - 1) ? s_top : I(vt[f][ktop * kSlotTile]) * I(x[f][ktop * kSlotTile]);
+        s0[f] = (nz == 1) ? s_top : I(vt[f][0]) * I(x[f][0]);
       }
     }
     for (int k = ktop - 1; k >= 0; k -= G) {
@@ -1087,8 +1102,8 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
 #pragma unroll
           for (int f = 0; f < NF; f++) {
             gv[f][u] = vt[f][o];
-            gx[f][u] = x[f][o];
-            gt[f][u] = ten[f][o];
+            gx[f][u] = I(x[f][o]);
+            gt[f][u] = I(ten[f][o]);
           }
         }
 #pragma unroll
@@ -1123,12 +1138,12 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
           const long o = (long)(k - u) * kSlotTile;
 #pragma unroll
           for (int f = 0; f < NF; f++) {
-            ten[f][o] = gt[f][u];
-            x[f][o] = gx[f][u];
+            ten[f][o] = R(gt[f][u]);
+            x[f][o] = R(gx[f][u]);
           }
         }
     }
-    if (precip && x[0][0] > low_limit_mass_for_precip) *precip = *precip + s0[0] * dti * osteps;
+    if (precip && I(x[0][0]) > low_limit_mass_for_precip) *precip = *precip + s0[0] * dti * osteps;
   };
   // All substeps of NF fields, level by level (temporal blocking).  In the upwind
   // scheme level k's substep n reads only level k's state and the flux of level k + 1
@@ -1136,21 +1151,22 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
   // in order while hist[f][n] carries the flux of the level above at substep n.  Every
   // level update, and every addition to the precipitation sum, is the arithmetic of
   // the substep-by-substep sweep above in the same order; a level's fields are read
-  // and written once for all substeps instead of once per substep.  SM bounds the
-  // substeps (hist lives in registers).
+  // and written once for all substeps instead of once per substep.  One call runs
+  // nsub <= SM of the steps substeps (hist lives in registers); a column with more
+  // substeps is walked in passes, each from the state the previous pass stored.
   auto sweep_all = [&](auto nf, auto smax, const int* fx, const int* ften, const int* fv,
-                       const double* limit, int steps, int ktop, I* precip) {
+                       const double* limit, int steps, int nsub, int ktop, I* precip) {
     constexpr int NF = decltype(nf)::value;
     constexpr int SM = decltype(smax)::value;
     constexpr bool kMixed = std::is_same<I, df>::value;
-    I* x[NF];
-    I* ten[NF];
+    R* x[NF];
+    R* ten[NF];
     const R* vt[NF];
     I lim[NF], hist[NF][SM];
 #pragma unroll
     for (int f = 0; f < NF; f++) {
-      x[f] = sd + fx[f] * fsd;
-      ten[f] = sd + ften[f] * fsd;
+      x[f] = xp(fx[f]);
+      ten[f] = xp(ften[f]);
       vt[f] = sr + fv[f] * fsd;
       lim[f] = I(limit[f]);
     }
@@ -1171,11 +1187,11 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
       }
 #pragma unroll
       for (int f = 0; f < NF; f++) {
-        I xk = x[f][o], tk = ten[f][o];
+        I xk = I(x[f][o]), tk = I(ten[f][o]);
         const I v = I(vt[f][o]);
 #pragma unroll
         for (int n = 0; n < SM; n++)
-          if (n < steps) {
+          if (n < nsub) {
             const I s_top = v * xk;
             if constexpr (kMixed) {
               tk = tk - s_top * fr * osteps;
@@ -1188,13 +1204,13 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
             if (k == 0 && f == 0 && precip && xk > low_limit_mass_for_precip)
               *precip = *precip + s_top * dti * osteps;
           }
-        ten[f][o] = tk;
-        x[f][o] = xk;
+        ten[f][o] = R(tk);
+        x[f][o] = R(xk);
       }
       if (ktop != nz - 1) {  // levels ktop..nz-2 keep their state: a constant flux
 #pragma unroll
         for (int f = 0; f < NF; f++) {
-          const I s_c = I(vt[f][ktop * kSlotTile]) * x[f][ktop * kSlotTile];
+          const I s_c = I(vt[f][ktop * kSlotTile]) * I(x[f][ktop * kSlotTile]);
 #pragma unroll
           for (int n = 0; n < SM; n++) hist[f][n] = s_c;
         }
@@ -1215,10 +1231,10 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
           a = ldi<I>(dzp + (long)k * NI);
           b = rho[o];
         }
-  #pragma unroll
+#pragma unroll
         for (int f = 0; f < NF; f++) {
-          xx[f] = x[f][o];
-          tt[f] = ten[f][o];
+          xx[f] = I(x[f][o]);
+          tt[f] = I(ten[f][o]);
           vv[f] = vt[f][o];
         }
       };
@@ -1236,13 +1252,13 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
           fo = 1.0 / ca;
           fr = 1.0 / cb;
         }
-  #pragma unroll
+#pragma unroll
         for (int f = 0; f < NF; f++) {
           I xk = cx_[f], tk = ct_[f];
           const I v = I(cv_[f]);
-  #pragma unroll
+#pragma unroll
           for (int n = 0; n < SM; n++)
-            if (n < steps) {
+            if (n < nsub) {
               const I s_k = v * xk;
               if constexpr (kMixed) {
                 const I dflux = hist[f][n] - s_k;
@@ -1256,11 +1272,11 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
               if (k == 0 && f == 0 && precip && xk > low_limit_mass_for_precip)
                 *precip = *precip + s_k * dti * osteps;
             }
-          ten[f][o] = tk;
-          x[f][o] = xk;
+          ten[f][o] = R(tk);
+          x[f][o] = R(xk);
         }
         if (k >= 1) {
-  #pragma unroll
+#pragma unroll
           for (int f = 0; f < NF; f++) {
             cx_[f] = nx_[f];
             ct_[f] = nt_[f];
@@ -1281,13 +1297,13 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
           fo = 1.0 / ldi<I>(dzp + (long)k * NI);
           fr = 1.0 / rho[o];
         }
-  #pragma unroll
+#pragma unroll
         for (int f = 0; f < NF; f++) {
-          I xk = x[f][o], tk = ten[f][o];
+          I xk = I(x[f][o]), tk = I(ten[f][o]);
           const I v = I(vt[f][o]);
-  #pragma unroll
+#pragma unroll
           for (int n = 0; n < SM; n++)
-            if (n < steps) {
+            if (n < nsub) {
               const I s_k = v * xk;
               if constexpr (kMixed) {
                 const I dflux = hist[f][n] - s_k;
@@ -1301,28 +1317,36 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
               if (k == 0 && f == 0 && precip && xk > low_limit_mass_for_precip)
                 *precip = *precip + s_k * dti * osteps;
             }
-          ten[f][o] = tk;
-          x[f][o] = xk;
+          ten[f][o] = R(tk);
+          x[f][o] = R(xk);
         }
       }
     }
     if (ktop == 0 && nz > 1 && precip) {  // level 0 above the fall: its flux, unchanged
-      const I s0 = I(vt[0][0]) * x[0][0];
-      const bool add = x[0][0] > low_limit_mass_for_precip;
+      const I s0 = I(vt[0][0]) * I(x[0][0]);
+      const bool add = I(x[0][0]) > low_limit_mass_for_precip;
 #pragma unroll
       for (int n = 0; n < SM; n++)
-        if (n < steps && add) *precip = *precip + s0 * dti * osteps;
+        if (n < nsub && add) *precip = *precip + s0 * dti * osteps;
     }
   };
-  // the substeps of one species: blocked when the warp's largest count fits the
-  // register history, else substep by substep
+  // the substeps of one species: level by level when the warp's largest count fits the
+  // register history, else substep by substep.  The mixed form walks level by level
+  // always, in passes of up to 8 substeps: its planes hold FP32 values, so a pass
+  // stores FP32 and a substep-by-substep sweep would round the state after every
+  // substep where the walk keeps it in the island type.
   auto sweeps = [&](auto nf, const int* fx, const int* ften, const int* fv, const double* limit,
                     int steps, int ktop, I* precip) {
-    const int wmax = BLOCK ? __reduce_max_sync(__activemask(), steps) : 1 << 30;
+    constexpr bool kMixed = std::is_same<I, df>::value;
+    const int wmax = (BLOCK || kMixed) ? __reduce_max_sync(__activemask(), steps) : 1 << 30;
     if (wmax <= 4) {
-      sweep_all(nf, std::integral_constant<int, 4>{}, fx, ften, fv, limit, steps, ktop, precip);
+      sweep_all(nf, std::integral_constant<int, 4>{}, fx, ften, fv, limit, steps, steps, ktop, precip);
     } else if (wmax <= 8) {
-      sweep_all(nf, std::integral_constant<int, 8>{}, fx, ften, fv, limit, steps, ktop, precip);
+      sweep_all(nf, std::integral_constant<int, 8>{}, fx, ften, fv, limit, steps, steps, ktop, precip);
+    } else if constexpr (kMixed) {
+      for (int n0 = 0; n0 < steps; n0 += 8)
+        sweep_all(nf, std::integral_constant<int, 8>{}, fx, ften, fv, limit, steps, min(8, steps - n0),
+                  ktop, precip);
     } else {
       for (int n = 0; n < steps; n++) sweep(nf, fx, ften, fv, limit, steps, ktop, precip);
     }
@@ -1337,7 +1361,7 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
   [[maybe_unused]] auto sl = [&](int fx, int ften, int fv, double limit, int st, I* precip) {
     if constexpr (SEMI) {
       const long cs2 = a.ncol_pad;
-      sl_sweep<R, I, S>(nz, sd + fx * fsd, sd + ften * fsd, sr + fv * fsd, kSlotTile, dzp, NI, rho,
+      sl_sweep<R, I, S>(nz, xp(fx), xp(ften), sr + fv * fsd, kSlotTile, dzp, NI, rho,
                         reinterpret_cast<I*>(a.slw) + s, (long)(nz + 2) * cs2, cs2, st, limit,
                         precip, dti, I(a.odt));
     }
@@ -1379,15 +1403,15 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
           Lev<R> L;
           level_state(k, L);
           const long o = (long)k * kSlotTile, e = g.base + (long)k * NI;
-          const R tq = R(sd[SD_TQR * fsd + o]), tn = R(sd[SD_TNR * fsd + o]);
+          const R tq = xp(SD_TQR)[o], tn = xp(SD_TNR)[o];
           L.qrten = tq;
           L.nrten = tn;
           R q = R(a.qr[e]), nn = R(a.nr[e]);
           rain_check(L, q, nn, dt, odt_r);
-          sd[SD_XRR * fsd + o] = I(L.rr);
-          sd[SD_XNR * fsd + o] = I(L.nr);
-          if (!(L.qrten == tq)) sd[SD_TQR * fsd + o] = I(L.qrten);
-          if (!(L.nrten == tn)) sd[SD_TNR * fsd + o] = I(L.nrten);
+          xp(SD_XRR)[o] = L.rr;
+          xp(SD_XNR)[o] = L.nr;
+          if (!(L.qrten == tq)) xp(SD_TQR)[o] = L.qrten;
+          if (!(L.nrten == tn)) xp(SD_TNR)[o] = L.nrten;
           R v = vup, vn = vnup;
           if (L.rr > R(r1)) rain_speeds(L, *cst, v, vn);
           sr[SR_VTR * fsd + o] = v;
@@ -1421,18 +1445,18 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
           Lev<R> L;
           level_state(k, L);
           const long o = (long)k * kSlotTile, e = g.base + (long)k * NI;
-          const R tq = R(sd[SD_TQG * fsd + o]), tn = R(sd[SD_TNG * fsd + o]), tb = R(sd[SD_TQB * fsd + o]);
+          const R tq = xp(SD_TQG)[o], tn = xp(SD_TNG)[o], tb = xp(SD_TQB)[o];
           L.qgten = tq;
           L.ngten = tn;
           L.qbten = tb;
           R q = R(a.qg[e]), nn = hail ? R(a.ng[e]) : R(0), b = hail ? R(a.qb[e]) : R(0);
           graupel_check(L, q, nn, b, hail, dt, odt_r);
-          sd[SD_XRG * fsd + o] = I(L.rg);
-          sd[SD_XNG * fsd + o] = I(L.ng);
-          sd[SD_XRB * fsd + o] = I(L.rb);
-          if (!(L.qgten == tq)) sd[SD_TQG * fsd + o] = I(L.qgten);
-          if (!(L.ngten == tn)) sd[SD_TNG * fsd + o] = I(L.ngten);
-          if (!(L.qbten == tb)) sd[SD_TQB * fsd + o] = I(L.qbten);
+          xp(SD_XRG)[o] = L.rg;
+          xp(SD_XNG)[o] = L.ng;
+          xp(SD_XRB)[o] = L.rb;
+          if (!(L.qgten == tq)) xp(SD_TQG)[o] = L.qgten;
+          if (!(L.ngten == tn)) xp(SD_TNG)[o] = L.ngten;
+          if (!(L.qbten == tb)) xp(SD_TQB)[o] = L.qbten;
           R v = vup, vn = vnup;
           if (L.rg > R(r1)) graupel_speeds(L, *cst, a.flags, v, vn);
           sr[SR_VTG * fsd + o] = v;
@@ -1469,7 +1493,7 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
     int kt = 1;
     I hgtc = I(0.0);
     for (int k = 1; k <= nz - 1; k++) {
-      if (sd[SD_XRC * fsd + (long)(k - 1) * kSlotTile] > r2) kt = k;
+      if (xp(SD_XRC)[(long)(k - 1) * kSlotTile] > r2) kt = k;
       hgtc = hgtc + ldi<I>(dzp + (long)(k - 1) * NI);
       if (hgtc > 500.0) break;
     }
@@ -1575,16 +1599,16 @@ __device__ __forceinline__ void final_point(const StepArgs<S>& a, const TempoCon
   L.qg1d = io.template in<R>(a.qg[e], C_QG);
   L.ng1d = hail ? io.template in<R>(a.ng[e], C_NG) : R(0);
   L.qb1d = hail ? io.template in<R>(a.qb[e], C_QB) : R(0);
-  L.qrten = io.template sdin<R, I>(SD_TQR * fsd + o, C_TQR);
-  L.nrten = io.template sdin<R, I>(SD_TNR * fsd + o, C_TNR);
-  L.qgten = io.template sdin<R, I>(SD_TQG * fsd + o, C_TQG);
-  L.ngten = io.template sdin<R, I>(SD_TNG * fsd + o, C_TNG);
-  L.qbten = io.template sdin<R, I>(SD_TQB * fsd + o, C_TQB);
-  L.qsten = io.template sdin<R, I>(SD_TQS * fsd + o, C_TQS);
-  L.qiten = io.template sdin<R, I>(SD_TQI * fsd + o, C_TQI);
-  L.niten = io.template sdin<R, I>(SD_TNI * fsd + o, C_TNI);
-  L.qcten = io.template sdin<R, I>(SD_TQC * fsd + o, C_TQC);
-  L.ncten = io.template sdin<R, I>(SD_TNC * fsd + o, C_TNC);
+  L.qrten = io.template sxin<R, I>(fsd, SD_TQR, o, C_TQR);
+  L.nrten = io.template sxin<R, I>(fsd, SD_TNR, o, C_TNR);
+  L.qgten = io.template sxin<R, I>(fsd, SD_TQG, o, C_TQG);
+  L.ngten = io.template sxin<R, I>(fsd, SD_TNG, o, C_TNG);
+  L.qbten = io.template sxin<R, I>(fsd, SD_TQB, o, C_TQB);
+  L.qsten = io.template sxin<R, I>(fsd, SD_TQS, o, C_TQS);
+  L.qiten = io.template sxin<R, I>(fsd, SD_TQI, o, C_TQI);
+  L.niten = io.template sxin<R, I>(fsd, SD_TNI, o, C_TNI);
+  L.qcten = io.template sxin<R, I>(fsd, SD_TQC, o, C_TQC);
+  L.ncten = io.template sxin<R, I>(fsd, SD_TNC, o, C_TNC);
   L.smob = L.smoc = L.smo2 = L.smoz = R(0);
   if (!(f & F_NOMICRO)) {  // freeze_cloud_melt_ice (main:2124-2165)
     R xri = Max(R(0.0), L.qi1d + L.qiten * dt);
