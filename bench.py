@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--nz", type=int, default=65)
     ap.add_argument("--dt", type=float, default=30.0)
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=6)
+    ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--tuning", default=None,
                     help="points variant, point order, sedimentation variant (e.g. 5,1,5): "
                          "set instead of autotuning (for profiling a fixed configuration)")
@@ -610,9 +610,13 @@ def main():
     d2h = sum(a.nbytes for k, a in host.items() if k not in ("p", "w", "dz")) + \
         sum(a.nbytes for a in hdiag.values())
     ctx.run(host, args.dt, 1, diags=hdiag)
+    # each call returns after its last copy back, so the host clock brackets one step
+    e2e_step_ms = []
     t0 = time.perf_counter()
     for s in range(args.e2e_steps):
+        ts = time.perf_counter()
         ctx.run(host, args.dt, 2 + s, diags=hdiag)
+        e2e_step_ms.append(round((time.perf_counter() - ts) * 1e3, 2))
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
     e2e_value = world * ncol / e2e_s
 
@@ -675,7 +679,8 @@ def main():
         "autotune": {**tuning, "points_order": ("level-major", "regime")[tuning["points_order"]],
                      "points_ms_per_candidate": variant_ms[:16], "sedim_ms_per_variant": variant_ms[16:]},
         "e2e": {"value": e2e_value, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "path": "tempo_run_f32_c (host arrays)"},
+                "d2h_bytes_per_step": d2h, "path": "tempo_run_f32_c (host arrays)",
+                "step_ms": e2e_step_ms, "median_step_ms": statistics.median(e2e_step_ms)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic_from_profiles(ncol),
                      "traffic_source": "ncu dram bytes of one 65 536-column step scaled by columns",

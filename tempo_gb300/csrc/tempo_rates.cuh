@@ -279,14 +279,19 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
   R rate_max = R((L.qv - L.qvsi) * L.rho) * odt * R(0.999);
   R rho = R(L.rho);
   R xni, xnc;
-  // DeMott's number (main:2754 and :2798, the same arguments): evaluated once
-  const R xni_demott = (f & F_NIFA) ? demott_nucleation(c, tempc, rho, L.nifa) : R(0.0);
+  // DeMott's number (main:2754 and :2798, the same arguments): evaluated once, and only
+  // where a reader follows -- the freezing tables' nucleus index (rain or cloud
+  // freezing) or the deposition-nucleation branch
+  const bool fz_r = L.rr > c.r_r1, fz_c = L.rc > c.r_c1;
+  const bool nuc = (L.ssati >= demott_nuc_ssati) || (L.ssatw > eps && tempc < R(demott_nuc_tempc));
+  const R xni_demott =
+      ((f & F_NIFA) && (fz_r || fz_c || nuc)) ? demott_nucleation(c, tempc, rho, L.nifa) : R(0.0);
   if (f & F_NIFA)
     xni = xni_demott;
   else
     xni = R(1.0) * R(1000.0);
-  int idx_in = (xni > c.nt_in1) ? decade_index(c, xni, c.niin2, ntb_in) : 1;
-  if (L.rr > c.r_r1) {
+  int idx_in = ((fz_r || fz_c) && xni > c.nt_in1) ? decade_index(c, xni, c.niin2, ntb_in) : 1;
+  if (fz_r) {
     int idx_r, idx_r1;
     level_rain_index(L, idx_r, idx_r1);
     TG_TRACE(L, TR_FZR, idx_r | (idx_r1 << 6) | (idx_tc << 12) | (idx_in << 18) | (1 << 24));
@@ -310,7 +315,7 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
     t.pni_rfz = L.nr * odt;
   }
   t.pbg_rfz = R(meters3_to_liters) * t.prg_rfz / R(rho_i);
-  if (L.rc > c.r_c1) {
+  if (fz_c) {
     int idx_c, idx_n;
     cloud_index(c, T.edges, L.rc, L.nc, idx_c, idx_n);
     TG_TRACE(L, TR_FZC, idx_c | (idx_n << 8) | (1 << 16));
@@ -330,7 +335,7 @@ __device__ void ice_nucleation(const Lev<R>& L, Tend<R>& t, const Tables<Cst<R>>
     t.pri_wfz = L.rc * odt;
     t.pni_wfz = L.nc * odt;
   }
-  if ((L.ssati >= demott_nuc_ssati) || (L.ssatw > eps && tempc < R(demott_nuc_tempc))) {
+  if (nuc) {
     if (f & F_NIFA)
       xnc = xni_demott;
     else
