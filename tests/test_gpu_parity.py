@@ -112,3 +112,34 @@ def test_config1_multistep_fp64_matches_oracle(ctx_nohail, oracle_mod):
         assert e < TOL64, (step, name, e)
         state = fo
     oracle_mod.init(True)
+
+
+def test_config1_fp64_water_budget_matches_oracle(ctx_nohail, oracle_mod):
+    """Column water (vapour and condensate, times density and layer depth) plus the
+    surface precipitation, after the step minus before: the FP64 drop-in's budget
+    equals the oracle's to round-off (1e-13 of the column's water) in every column, with
+    dt = 30 s and with dt = 120 s (more than 8 sedimentation substeps near the
+    surface)."""
+    from tempo_gb300 import workloads as W
+    from tempo_gb300.workloads import RD
+    oracle_mod.init(False)
+    over = dict(hailaware_flag=0)
+    for dt in (30.0, 120.0):
+        wl = W.config1(ni=64, nj=8, steps=1, dt=dt)
+        x = wl.fields
+        rho = RD / 461.5 * x["p"] / (RD * x["t"] * (np.maximum(1e-10, x["qv"]) + RD / 461.5))
+
+        def water(F, D):
+            q = sum(np.asarray(F[n], np.float64) for n in ("qv", "qc", "qr", "qi", "qs", "qg"))
+            return (q * rho * x["dz"]).sum(axis=1) + sum(np.asarray(D[n], np.float64) for n in
+                                                         ("rain_precip", "ice_liquid_equiv_precip",
+                                                          "snow_liquid_equiv_precip",
+                                                          "graupel_liquid_equiv_precip"))
+        fo, do = run_oracle(oracle_mod, over, wl)
+        fg, dg = run_gpu(ctx_nohail, over, wl)
+        zero = {n: 0.0 for n in ("rain_precip", "ice_liquid_equiv_precip", "snow_liquid_equiv_precip",
+                                 "graupel_liquid_equiv_precip")}
+        w0 = water(x, zero)
+        diff = np.abs((water(fg, dg) - w0) - (water(fo, do) - w0)) / w0
+        assert diff.max() < 1e-13, (dt, float(diff.max()))
+    oracle_mod.init(True)
