@@ -4,7 +4,8 @@ tie (graupel density class, substep count; there the reference's own result depe
 the last bit of a libm value).
 
 Per field three measures, each against a stated bound:
-  - relative RMS, ||mixed - oracle|| / ||oracle|| (north star: 1e-5 per field);
+  - relative RMS, ||mixed - oracle|| / ||oracle||, within the benchmark spec's 1e-5 for every
+    field;
   - normwise, max |mixed - oracle| / max |oracle|;
   - pointwise, |mixed - oracle| / max(|oracle|, floor) with the floor at 1e-7 of the
     field's largest value (the FP32 resolution of the field's scale), and the fraction
@@ -13,10 +14,10 @@ The pointwise 1e-5 bound is not met everywhere with an FP32 bulk: where a value 
 small residue of large terms (a level that sedimentation nearly drains, the front of a
 falling species, a species nearly used up) its relative error is the FP32 rounding of
 the terms, and an FP32 fall speed or rate that lands on the other side of a bin edge moves
-a column.  The bounds below are the measured envelope of this build (they catch a
-regression), not the benchmark spec's pointwise bound.  Also: the column water budget
-(total water plus surface precipitation, after minus before) against the oracle's, and
-10-cm reflectivity in dBZ."""
+a column.  The normwise and pointwise bounds below are the measured envelope with a
+margin (they catch a regression), not the benchmark spec's pointwise bound.  Also: the
+column water budget (total water plus surface precipitation, after minus before)
+against the oracle's, and 10-cm reflectivity in dBZ."""
 import numpy as np
 import pytest
 
@@ -25,16 +26,16 @@ from parity_util import DIAG2, FLOOR, make_diags, run_oracle
 pytestmark = pytest.mark.gpu
 
 PROG = ("t", "qv", "qc", "qr", "qi", "qs", "qg", "ni", "nr", "nc", "ng", "qb")
-# relative RMS per field: the benchmark spec's 1e-5 where met; measured envelope otherwise
-# (nc: one droplet-evaporation bin flip in a 1024-column sample moves its relative RMS to
-# about 1e-4; on 262 144 columns it is 3e-5, bench.py precision study)
-REL_RMS = {"t": 1e-5, "qv": 1e-5, "qc": 1e-5, "qr": 1e-5, "qi": 1e-5, "qs": 1e-5, "qg": 3e-5,
-           "nr": 1e-5, "ni": 1e-4, "nc": 5e-4, "ng": 3e-5, "qb": 3e-5}
-NORMWISE = {"t": 1e-5, "qv": 1e-4}           # others: 0.05 (see the module docstring)
-SCALED_MAX = {"t": 1e-5, "qv": 1e-4}          # others: 1.0
+# relative RMS per field: the benchmark spec's 1e-5 for every field on these samples (the
+# largest measured is 1.2e-6, nc of the config-2 sample; on the 262 144 columns of the
+# bench's precision study a few columns that cross a discrete step move some fields
+# beyond it)
+REL_RMS = {n: 1e-5 for n in PROG}
+NORMWISE = {"t": 1e-5, "qv": 1e-5}           # others: 1e-4 (largest measured 4.2e-5, nc)
+SCALED_MAX = {"t": 1e-5, "qv": 1e-5}          # others: 0.05 (largest 1.7e-2, qg at clamps)
 FRAC_R1 = 0.05                               # points beyond 1e-5 with the reference floors
-BUDGET = 1e-6                                # column water budget against the oracle's
-REFL_DBZ_RMS = 0.01
+BUDGET = 1e-7                                # column water budget against the oracle's
+REFL_DBZ_RMS = 1e-3
 
 
 def _run_mixed_f32(ctx, over, wl, itimestep=1):
@@ -90,11 +91,11 @@ def _check(out):
     for n, v in out.items():
         if n in ("budget", "refl10cm_dbz"):
             continue
-        if v["rel_rms"] > REL_RMS.get(n, 1e-4):
+        if v["rel_rms"] > REL_RMS[n]:
             bad.append((n, "rel_rms", v["rel_rms"]))
-        if v["normwise"] > NORMWISE.get(n, 0.05):
+        if v["normwise"] > NORMWISE.get(n, 1e-4):
             bad.append((n, "normwise", v["normwise"]))
-        if v["scaled_max"] > SCALED_MAX.get(n, 1.0):
+        if v["scaled_max"] > SCALED_MAX.get(n, 0.05):
             bad.append((n, "scaled_max", v["scaled_max"]))
         if v["frac_r1"] > FRAC_R1:
             bad.append((n, "frac_r1", v["frac_r1"]))
