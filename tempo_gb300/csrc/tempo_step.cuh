@@ -976,7 +976,9 @@ __device__ __forceinline__ void sedim_column(const StepArgs<S>& a, const TempoCo
   // this slot's level 0 in the plane of a sedimenting field or its tendency: values of
   // the bulk type R (in the mixed form FP32 in the first half of the plane); the walks
   // below keep them in the island type between the loads and stores
-  auto xp = [&](int f) -> R* { return reinterpret_cast<R*>(reinterpret_cast<I*>(a.sd) + (long)f * fsd) + pt_base(s, nz); };
+  auto xp = [&](int f) -> R* {
+    return reinterpret_cast<R*>(reinterpret_cast<I*>(a.sd) + (long)f * fsd) + pt_base(s, nz);
+  };
   const R dt = step_dt<R>(a);
   const I dti = step_dti<R>(a);
   const S* dzp = a.dz + g.base;
