@@ -19,6 +19,7 @@
 #include "tempo_consts.h"
 #include "tempo_dfloat.cuh"
 #include "tempo_dual.cuh"
+#include "tempo_powers.h"
 #include "tempo_types.h"
 
 namespace tg {
@@ -46,8 +47,8 @@ __device__ __forceinline__ float Pow(float x, float y) { return powf(x, y); }
 // (...)**(1/bm), and (...)**(1/(bm_g+1)) for the graupel intercept -- about 10 of the
 // 22 powers per level-point of a config-1 step.  The FP64 drop-in keeps the
 // reference's real-exponent pow (x**bm_r is pow(x, 3.0) there); the mixed form forms
-// them from products, cube and square roots, as accurate as powf at a fraction of its
-// code and time.  The exponent argument is the reference's constant (checked against
+// them from products, cube and square roots, within a few rounding errors at a fraction
+// of powf's code and time.  The exponent argument is the reference's constant (checked against
 // the parameter at compile time for the cube; the roots take the context's 1/bm).
 static_assert(bm_r == 3.0 && bm_i == 3.0 && bm_g == 3.0, "mass exponents of the scheme");
 __device__ __forceinline__ double PowBm(double x) { return pow(x, 3.0); }
@@ -56,46 +57,9 @@ __device__ __forceinline__ double PowObm(double x, double obm) { return pow(x, o
 __device__ __forceinline__ float PowObm(float x, float) { return cbrtf(x); }
 __device__ __forceinline__ double PowOge1(double x, double oge1) { return pow(x, oge1); }
 __device__ __forceinline__ float PowOge1(float x, float) { return sqrtf(sqrtf(x)); }
-// Exponents of the rain and graupel size distributions that the host puts in cre and
-// cge (params:511-523, 558-571), as constants: with the scheme's mu_r = mu_g = 0, bm = 3 and
-// bv_r = 1 all of cre and the entries of cge that do not involve the graupel fall-speed
-// exponent are integers or half-integers (negative entries: depends on bv_g).
-constexpr double kCre[13] = {bm_r + 1.0, mu_r + 1.0, bm_r + mu_r + 1.0, bm_r * 2.0 + mu_r + 1.0,
-                             mu_r + bv_r + 1.0, bm_r + mu_r + bv_r + 1.0,
-                             bm_r * 0.5 + mu_r + bv_r + 1.0, bm_r + mu_r + bv_r + 3.0,
-                             mu_r + bv_r + 3.0, mu_r + 2.0, 0.5 * (bv_r + 5.0 + 2.0 * mu_r),
-                             bm_r * 0.5 + mu_r + 1.0, bm_r * 2.0 + mu_r + bv_r + 1.0};
-constexpr double kCge[12] = {bm_g + 1.0, mu_g + 1.0, bm_g + mu_g + 1.0, bm_g * 2.0 + mu_g + 1.0,
-                             -1.0, -1.0, -1.0, -1.0, -1.0, mu_g + 2.0, -1.0,
-                             bm_g * 0.5 + mu_g + 1.0};
-// x**N and x**(TW/2) for compile-time N and TW: binary powering, one square root for a
-// half-integer, one division for a negative exponent (a few rounding errors)
-template <int N> __device__ __forceinline__ float ipow_ct(float x) {
-  if constexpr (N == 0) {
-    return 1.0f;
-  } else if constexpr (N == 1) {
-    return x;
-  } else {
-    const float h = ipow_ct<N / 2>(x);
-    if constexpr (N % 2) return h * h * x;
-    else return h * h;
-  }
-}
-template <int TW> __device__ __forceinline__ float pow_twice(float x) {
-  constexpr int A = TW < 0 ? -TW : TW;
-  float r = ipow_ct<A / 2>(x);
-  if constexpr (A % 2 != 0) r = r * sqrtf(x);
-  if constexpr (TW < 0) r = 1.0f / r;
-  return r;
-}
-// x**(S kCre[K]) and x**(S kCge[K]) (S = +1 or -1): y is the same exponent as the context
-// holds it, which the FP64 drop-in passes to pow as the reference does; the mixed form
-// multiplies
-template <double const* E, int K, int S> struct FixedExp {
-  static constexpr double e = S * E[K];
-  static constexpr int tw = (int)(2.0 * e);
-  static_assert(e * 2.0 == (double)tw && E[K] >= 0.0, "an integer or half-integer exponent");
-};
+// x**(S kCre[K]) and x**(S kCge[K]) (S = +1 or -1, tempo_powers.h): y is the same
+// exponent as the context holds it, which the FP64 drop-in passes to pow as the
+// reference does; the mixed form multiplies
 template <int K, int S = 1> __device__ __forceinline__ double PowCre(double x, double y) { return pow(x, y); }
 template <int K, int S = 1> __device__ __forceinline__ float PowCre(float x, float) {
   return pow_twice<FixedExp<kCre, K, S>::tw>(x);
