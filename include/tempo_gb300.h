@@ -27,9 +27,9 @@ extern "C" {
 typedef enum {
   TEMPO_OK = 0,
   TEMPO_ERR_ARG = -1,         /* NULL required pointer, bad bounds, dt <= 0, ... */
-  TEMPO_ERR_UNSUPPORTED = -2, /* optional path outside this build (the ML boundary-layer
-                                 cloud path; derivatives of the semi-Lagrangian, melting-layer
-                                 and ML cloud-number paths) */
+  TEMPO_ERR_UNSUPPORTED = -2, /* optional path this library does not implement (the ML
+                                 boundary-layer cloud path; derivatives of the
+                                 semi-Lagrangian, melting-layer and ML cloud-number paths) */
   TEMPO_ERR_TABLE = -3,       /* missing, truncated or malformed lookup table */
   TEMPO_ERR_CUDA = -4,        /* CUDA runtime failure (message has the CUDA error string) */
   TEMPO_ERR_NOMEM = -5,       /* host or device allocation failed */

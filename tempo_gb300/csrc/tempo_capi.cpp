@@ -1744,7 +1744,7 @@ int tl_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, temp
   if (int rc = build_args(c, cfg, dt, itimestep, X, b, dgs, ap)) return rc;
   if (ap.flags & (F_SEMI | F_MELT | F_MLNC))
     return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation, the "
-                "melting-layer reflectivity and the ML cloud number are not part of this build");
+                "melting-layer reflectivity and the ML cloud number are not implemented by this library");
   if (cfg->max_hail_diameter_flag) ap.mhd_sfc = ap.mhd_col = nullptr;  // not differentiable
   CUDA_TRY(cudaSetDevice(c->device));
   DevBufs B;
@@ -1784,7 +1784,7 @@ int adjoint_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep,
   if (int rc = build_args(c, cfg, dt, itimestep, X, b, nullptr, ap)) return rc;
   if (ap.flags & (F_SEMI | F_MELT | F_MLNC))
     return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation, the "
-                "melting-layer reflectivity and the ML cloud number are not part of this build");
+                "melting-layer reflectivity and the ML cloud number are not implemented by this library");
   CUDA_TRY(cudaSetDevice(c->device));
   DevBufs B;
   using D1 = Dual<T, 1>;

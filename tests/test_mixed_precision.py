@@ -4,8 +4,8 @@ tie (graupel density class, substep count; there the reference's own result depe
 the last bit of a libm value).
 
 Per field three measures, each against a stated bound:
-  - relative RMS, ||mixed - oracle|| / ||oracle||, within the benchmark spec's 1e-5 for every
-    field;
+  - relative RMS, ||mixed - oracle|| / ||oracle||, within the 1e-5 per-field target for
+    every field;
   - normwise, max |mixed - oracle| / max |oracle|;
   - pointwise, |mixed - oracle| / max(|oracle|, floor) with the floor at 1e-7 of the
     field's largest value (the FP32 resolution of the field's scale), and the fraction
@@ -15,7 +15,7 @@ small residue of large terms (a level that sedimentation nearly drains, the fron
 falling species, a species nearly used up) its relative error is the FP32 rounding of
 the terms, and an FP32 fall speed or rate that lands on the other side of a bin edge moves
 a column.  The normwise and pointwise bounds below are the measured envelope with a
-margin (they catch a regression), not the benchmark spec's pointwise bound.  Also: the
+margin (they catch a regression), not the 1e-5 pointwise target.  Also: the
 column water budget (total water plus surface precipitation, after minus before)
 against the oracle's, and 10-cm reflectivity in dBZ."""
 import numpy as np
@@ -26,7 +26,7 @@ from parity_util import DIAG2, FLOOR, make_diags, run_oracle
 pytestmark = pytest.mark.gpu
 
 PROG = ("t", "qv", "qc", "qr", "qi", "qs", "qg", "ni", "nr", "nc", "ng", "qb")
-# relative RMS per field: the benchmark spec's 1e-5 for every field on these samples (the
+# relative RMS per field: the 1e-5 target for every field on these samples (the
 # largest measured is 1.2e-6, nc of the config-2 sample; on the 262 144 columns of the
 # bench's precision study a few columns that cross a discrete step move some fields
 # beyond it)
