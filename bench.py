@@ -154,7 +154,7 @@ def cpu_baseline(seconds: float, nz: int, dt: float, sample_cols: int = 16384):
     oracle.build()
     oracle.init(False, REPO / "tables" / "ccn_activate.bin")
     oracle.build_big_tables()
-    wl = W.config1(seed=11, ni=sample_cols, nj=1, nz=nz, steps=1, dt=dt)
+    wl = W.stretched_grid(seed=11, ni=sample_cols, nj=1, nz=nz, steps=1, dt=dt)
     cfg = oracle.default_cfgs(hailaware_flag=0)
     f = {k: v.copy() for k, v in wl.fields.items()}
     nj, nk, ni = f["p"].shape
@@ -232,7 +232,7 @@ def adjoint_timing(ctx, tg, W, torch, device, reps=3):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    base = W.config1_torch(seed=7, ni=256, nj=256, nz=65, device=device, dtype=torch.float64)
+    base = W.stretched_grid_torch(seed=7, ni=256, nj=256, nz=65, device=device, dtype=torch.float64)
     out = {"workload": "65536 columns x 65 levels, dt=60s, J = sum precip + 1e-3 sum Ze dz",
            "reps": reps}
     for name, dtype in (("fp64", torch.float64), ("fp32", torch.float32)):
@@ -278,11 +278,11 @@ def multi_domain(ctx, tg, W, torch, device, steps=3):
     over all domains); the same domains stepped one call each are timed beside it.  ms
     from CUDA events; value = all domains' columns x steps / time; the level-point rate
     and the rate in 65-level column equivalents compare it with the single-domain run."""
-    doms = W.config4_domains(seed=0)
+    doms = W.domain_set(seed=0)
     table_ms = ctx.build_tables()
     data = []
     for d, (ncol, nz, dt, seed) in enumerate(doms):
-        f = W.config1_torch(seed=100 + d, ni=ncol, nj=1, nz=nz, device=device, dtype=torch.float32)
+        f = W.stretched_grid_torch(seed=100 + d, ni=ncol, nj=1, nz=nz, device=device, dtype=torch.float32)
         dg = {n: torch.zeros((1, ncol), device=device) for n in tg.DIAG2}
         dg.update({n: torch.zeros((1, nz, ncol), device=device)
                    for n in ("refl10cm", "re_cloud", "re_ice", "re_snow")})
@@ -339,7 +339,7 @@ def multi_domain(ctx, tg, W, torch, device, steps=3):
 
 
 def precision_study(tg, W, torch, device, ncol_side=512):
-    """The config-2 precision study: 262 144 hail-aware deep-convective columns x 65
+    """The precision study on hail-aware deep convection: 262 144 hail-aware deep-convective columns x 65
     levels (qg lognormal, median 2 g/kg clipped at 8, ng log-uniform 1e2..1e5, graupel
     density 300..900 kg m-3, supercooled cloud water; the seeded generator on the
     device), on a hail-aware context: one step of the mixed form (FP32 bulk, FP64-grade
@@ -357,7 +357,7 @@ def precision_study(tg, W, torch, device, ncol_side=512):
     import oracle
     dt = 30.0
     ctx = tg.TempoContext(build_tables=True, cfgs=tg.default_cfgs(hailaware_flag=1))
-    gen = W.config1_torch(seed=3, ni=ncol_side, nj=ncol_side, nz=65, device=device,
+    gen = W.stretched_grid_torch(seed=3, ni=ncol_side, nj=ncol_side, nz=65, device=device,
                           dtype=torch.float32, hail=True, deep=True)
     fields = {k: v.cpu().numpy() for k, v in gen.items()}
     del gen
@@ -440,7 +440,7 @@ def precision_study(tg, W, torch, device, ncol_side=512):
     ro = budget(fo, do) - w0
     cons = {name: float(np.max((np.abs(budget(F, D) - w0 - ro) / w0)[clean]))
             for name, F, D in (("mixed", fm, dm), ("fp64_gpu", f64, d64))}
-    return {"workload": f"config2: {ncols} hail-aware deep-convective columns x {nk} levels, dt={dt}s "
+    return {"workload": f"{ncols} hail-aware deep-convective columns x {nk} levels, dt={dt}s "
                         "(seeded generator on the device)",
             "oracle_columns": ncols, "oracle_tie_columns": int((~clean).sum()),
             "oracle_seconds": oracle_s,
@@ -461,7 +461,7 @@ def run_reference(args, rank, world):
     oracle.init(False, REPO / "tables" / "ccn_activate.bin")
     oracle.build_big_tables()
     ncol = args.ref_columns
-    wl = W.config1(seed=11, ni=ncol, nj=1, nz=args.nz, steps=1, dt=args.dt)
+    wl = W.stretched_grid(seed=11, ni=ncol, nj=1, nz=args.nz, steps=1, dt=args.dt)
     cfg = oracle.default_cfgs(hailaware_flag=0)
     f = {k: v.copy() for k, v in wl.fields.items()}
     nj, nk, ni = f["p"].shape
@@ -486,8 +486,8 @@ def run_reference(args, rank, world):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded config1 generator)",
-            "config": {"workload": f"config1: {args.ni * args.nj} columns x {args.nz} levels, "
+            "data": "synthetic (seeded stretched-grid column generator)",
+            "config": {"workload": f"{args.ni * args.nj} columns x {args.nz} levels, stretched 20 km grid, "
                                    f"dt={args.dt}s; each timed step is a bounded sample of "
                                    f"{ncol} of its columns (ms_per_step is the sample's)",
                        "parallelism": "cpu-openmp"},
@@ -519,7 +519,7 @@ def main():
     ctx.set_precision(tg.PREC_MIXED)
     ni, nj, nz = args.ni, args.nj, args.nz
     ncol = ni * nj
-    f32 = W.config1_torch(seed=rank, ni=ni, nj=nj, nz=nz, device=f"cuda:{local}",
+    f32 = W.stretched_grid_torch(seed=rank, ni=ni, nj=nj, nz=nz, device=f"cuda:{local}",
                           dtype=torch.float32)
     diag = {n: torch.zeros((nj, ni), device=f"cuda:{local}", dtype=torch.float32) for n in tg.DIAG2}
     diag.update({n: torch.zeros((nj, nz, ni), device=f"cuda:{local}", dtype=torch.float32)
@@ -667,8 +667,8 @@ def main():
         "metric": METRIC, "value": value, "unit": "column-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-        "data": "synthetic (seeded config1 generator on device)",
-        "config": {"workload": f"config1: {ncol} columns x {nz} levels, stretched 20 km grid, "
+        "data": "synthetic (seeded stretched-grid column generator on device)",
+        "config": {"workload": f"{ncol} columns x {nz} levels, stretched 20 km grid, "
                                f"40% clear, dt={args.dt}s, mixed precision (FP32 bulk, FP64 "
                                f"islands), aerosol-aware, hail-aware off",
                    "columns_per_gpu": ncol, "levels": nz, "dt": args.dt,
@@ -691,7 +691,7 @@ def main():
         "fp32_roofline": fp32_roof,
         "adjoint": adjoint,
         "multi_domain": multi,
-        "precision_study_config2": prec,
+        "precision_study_hail": prec,
         "gpu_launches": args.steps * stats.get("launches", 1),
         "clocks": clocks,
         "step_stats": stats,

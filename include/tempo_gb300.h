@@ -141,7 +141,7 @@ int tempo_check_table_c(const char *name, const char *path);
  * present mass, number, aerosol and volume array must be finite; t (or th and pii), p and
  * dz must be > 0.  A failed scan returns TEMPO_ERR_NONFINITE naming the first bad field
  * and (i, k, j) index, before any array is modified.  Host-array runs scan on the host
- * before the copy; device-array runs scan with one kernel and wait for its verdict (the
+ * before the copy; device-array runs scan with one kernel and wait for its result (the
  * call then synchronises with its stream).  Off by default. */
 int tempo_set_validation(tempo_ctx_t *ctx, int on);
 

@@ -1,6 +1,6 @@
 """CPU FP64 restatement of NCAR/TEMPO's column step -- test infrastructure only.
 
-This package is the CHECKER.  Only ``tests/``, ``__graft_entry__.smoke()`` and
+This package is the oracle, not the product.  Only ``tests/``, ``__graft_entry__.smoke()`` and
 ``bench.py`` (its ``cpu_baseline`` leg and ``--impl reference``) may import it, and
 only to compare against or time beside the CUDA product.  The product
 (``tempo_gb300``) never loads it.

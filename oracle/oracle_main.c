@@ -17,7 +17,7 @@
 #include "oracle_common.h"
 #include "tempo_oracle.h"
 
-/* Rounding-tie detection (checker-only instrumentation, no effect on results).
+/* Rounding-tie detection (oracle-only instrumentation, no effect on results).
  * nint(x) and int(y) are discontinuous at half-integers and integers; where the
  * reference's arithmetic puts an argument there up to one rounding (e.g. the graupel
  * density class 10*rg/rb = 0.5 when rb sits at its clamp rg*1000/rho_g(1)), any
@@ -32,7 +32,7 @@ static inline int nint_tie(double x) {
   if (fabs(f - 0.5) <= 1e-12 * fmax2(1.0, fabs(x))) t_tie |= t_tie_bit;
   return nint(x);
 }
-/* Decision trace (checker-only instrumentation, no effect on results): every table index
+/* Decision trace (oracle-only instrumentation, no effect on results): every table index
  * and branch decision of a step, per (tile column, level) point TRP ints and per column
  * TRC ints, in the layout the GPU library's test build records (TraceSlot and
  * TraceCheckBit in tempo_gb300/csrc/tempo_types.h), so a test compares them exactly. */

@@ -1,7 +1,7 @@
 /*
  * tempo_oracle.h -- CPU FP64 restatement of NCAR/TEMPO v3.1.1 (test infrastructure).
  *
- * This is the CHECKER, not the product.  Only tests/, __graft_entry__.smoke() and
+ * This is the oracle, not the product.  Only tests/, __graft_entry__.smoke() and
  * bench.py's cpu_baseline / --impl reference legs may load it.  It restates, in
  * plain C with Fortran semantics (-fdefault-real-8: every real is a double, every
  * unsuffixed literal is a double; nint rounds half away from zero; real**integer is
@@ -145,7 +145,7 @@ int oracle_run(const ocfg_t *cfg, double dt, int itimestep,
  * [2..6] max substeps rain/graupel/snow/ice/cloud(=1). */
 void oracle_last_stats(long out[8]);
 
-/* Checker instrumentation: when flags != NULL, oracle_run writes per tile column
+/* Oracle-only instrumentation: when flags != NULL, oracle_run writes per tile column
  * (2-D diagnostic layout) the bits of the index computations that the column's step
  * passed within one rounding of their discontinuity (nint at a half-integer, int at
  * an integer): 1 = before or in sedimentation (graupel density class, substep

@@ -124,7 +124,7 @@ struct tempo_ctx {
   bool times_valid = false;  // the last run recorded the kernel-timing events
   bool validate = false;     // input scan before each run (tempo_set_validation)
   bool in_host_run = false;  // run_dev called by run_host (inputs scanned on the host)
-  unsigned long long* d_first_bad = nullptr;  // verdict of the device input scan
+  unsigned long long* d_first_bad = nullptr;  // result of the device input scan
 #ifdef TEMPO_TRACE
   int* trace = nullptr;  // decision-trace buffer of a test build (tempo_set_trace_c)
 #endif
@@ -607,7 +607,7 @@ int validate_host(const RunArrays<S>& A, const Bounds& b) {
   return validation_failure(v, b, names, code, x);
 }
 
-// The validation scan on device arrays: one kernel on stream s, then a wait for its verdict.
+// The validation scan on device arrays: one kernel on stream s, then a wait for its result.
 template <class S>
 int validate_dev(tempo_ctx* c, const RunArrays<S>& A, const Bounds& b, cudaStream_t s) {
   const char* names[kValidateFields];

@@ -45,7 +45,7 @@ __device__ __forceinline__ float Pow(float x, float y) { return powf(x, y); }
 // Powers with the reference's mass exponents (bm_r = bm_i = bm_g = 3, a parameter of
 // the scheme): the size-distribution checks raise slopes to bm and form slopes as
 // (...)**(1/bm), and (...)**(1/(bm_g+1)) for the graupel intercept -- about 10 of the
-// 22 powers per level-point of a config-1 step.  The FP64 drop-in keeps the
+// 22 powers per level-point of a stretched-grid step.  The FP64 drop-in keeps the
 // reference's real-exponent pow (x**bm_r is pow(x, 3.0) there); the mixed form forms
 // them from products, cube and square roots, within a few rounding errors at a fraction
 // of powf's code and time.  The exponent argument is the reference's constant (checked against

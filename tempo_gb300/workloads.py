@@ -4,15 +4,15 @@ The reference measures on no public dataset; these generators stand in for real
 model columns with the shapes, sizes and value distributions of the five benchmark
 configurations:
 
-* ``config0``: 256 columns x 60 levels, uniform dz = 250 m, dt = 20 s,
+* ``uniform_grid``: 256 columns x 60 levels, uniform dz = 250 m, dt = 20 s,
   aerosol-aware, no hail prognostics (ng/qb not passed).
-* ``config1``: 1024 x 1024 columns x 65 levels on a stretched grid (dz 50 m at the
+* ``stretched_grid``: 1024 x 1024 columns x 65 levels on a stretched grid (dz 50 m at the
   surface to 500 m at 20 km), 40 % clear columns, random cloud base/depth,
   w ~ N(0, 3) with 5 % convective columns, dt = 30 s.
-* ``config2``: 262144 deep-convective columns x 65 levels with hail-aware
+* ``hail_convection``: 262144 deep-convective columns x 65 levels with hail-aware
   2-moment graupel (ng, qb passed), dt = 30 s.
-* ``config3``: 65536 columns from the config1 generator, dt = 60 s.
-* ``config4``: 24 domains, column counts log-uniform in 1e3..5e5, nz in
+* ``stretched_grid_dt60``: 65536 columns from the stretched-grid generator, dt = 60 s.
+* ``domain_set``: 24 domains, column counts log-uniform in 1e3..5e5, nz in
   {50, 65, 90, 128}, dt in {10, 20, 30, 60}.
 
 Fields are returned as float64 arrays shaped ``(nj, nk, ni)`` -- the Fortran
@@ -178,15 +178,15 @@ def _to3d(cols: dict, ni: int, nj: int, hail: bool) -> dict:
     return out
 
 
-def config0(seed: int = 0, ncol: int = 256, nz: int = 60) -> Workload:
+def uniform_grid(seed: int = 0, ncol: int = 256, nz: int = 60) -> Workload:
     rng = np.random.default_rng(np.random.PCG64(1000 + seed))
     dz = np.full(nz, 250.0)
     cols = _profiles(rng, ncol, dz)
-    return Workload("config0", 20.0, _to3d(cols, ncol, 1, hail=False), hail=False,
+    return Workload("uniform_grid", 20.0, _to3d(cols, ncol, 1, hail=False), hail=False,
                     meta=dict(ncol=ncol, nz=nz, seed=seed))
 
 
-def _config1_cols(rng, ncol, nz, hail=False, deep=False):
+def _stretched_cols(rng, ncol, nz, hail=False, deep=False):
     dz = stretched_dz(nz)
     clear = rng.uniform(size=ncol) < (0.0 if deep else 0.4)
     base = rng.uniform(300.0, 3000.0, ncol)
@@ -198,28 +198,28 @@ def _config1_cols(rng, ncol, nz, hail=False, deep=False):
                      hail=hail, deep=deep)
 
 
-def config1(seed: int = 0, ni: int = 1024, nj: int = 1024, nz: int = 65,
+def stretched_grid(seed: int = 0, ni: int = 1024, nj: int = 1024, nz: int = 65,
             steps: int = 10, dt: float = 30.0) -> Workload:
     rng = np.random.default_rng(np.random.PCG64(2000 + seed))
-    cols = _config1_cols(rng, ni * nj, nz)
-    return Workload("config1", dt, _to3d(cols, ni, nj, hail=False), hail=False, steps=steps,
+    cols = _stretched_cols(rng, ni * nj, nz)
+    return Workload("stretched_grid", dt, _to3d(cols, ni, nj, hail=False), hail=False, steps=steps,
                     meta=dict(ncol=ni * nj, nz=nz, seed=seed))
 
 
-def config2(seed: int = 0, ni: int = 512, nj: int = 512, nz: int = 65, dt: float = 30.0) -> Workload:
+def hail_convection(seed: int = 0, ni: int = 512, nj: int = 512, nz: int = 65, dt: float = 30.0) -> Workload:
     rng = np.random.default_rng(np.random.PCG64(3000 + seed))
-    cols = _config1_cols(rng, ni * nj, nz, hail=True, deep=True)
-    return Workload("config2", dt, _to3d(cols, ni, nj, hail=True), hail=True,
+    cols = _stretched_cols(rng, ni * nj, nz, hail=True, deep=True)
+    return Workload("hail_convection", dt, _to3d(cols, ni, nj, hail=True), hail=True,
                     meta=dict(ncol=ni * nj, nz=nz, seed=seed))
 
 
-def config3(seed: int = 0, ni: int = 256, nj: int = 256, nz: int = 65) -> Workload:
-    wl = config1(seed=seed + 7, ni=ni, nj=nj, nz=nz, steps=1, dt=60.0)
-    wl.name = "config3"
+def stretched_grid_dt60(seed: int = 0, ni: int = 256, nj: int = 256, nz: int = 65) -> Workload:
+    wl = stretched_grid(seed=seed + 7, ni=ni, nj=nj, nz=nz, steps=1, dt=60.0)
+    wl.name = "stretched_grid_dt60"
     return wl
 
 
-def config4_domains(seed: int = 0, ndom: int = 24, scale: float = 1.0):
+def domain_set(seed: int = 0, ndom: int = 24, scale: float = 1.0):
     """Domain descriptors (ncol, nz, dt, seed) of the uneven multi-domain batch."""
     rng = np.random.default_rng(np.random.PCG64(5000 + seed))
     out = []
@@ -231,10 +231,10 @@ def config4_domains(seed: int = 0, ndom: int = 24, scale: float = 1.0):
     return out
 
 
-def config4_domain(ncol: int, nz: int, dt: float, seed: int) -> Workload:
+def domain_set_member(ncol: int, nz: int, dt: float, seed: int) -> Workload:
     rng = np.random.default_rng(np.random.PCG64(seed))
-    cols = _config1_cols(rng, ncol, nz)
-    return Workload("config4", dt, _to3d(cols, ncol, 1, hail=False), hail=False,
+    cols = _stretched_cols(rng, ncol, nz)
+    return Workload("domain_set", dt, _to3d(cols, ncol, 1, hail=False), hail=False,
                     meta=dict(ncol=ncol, nz=nz, seed=seed))
 
 
@@ -248,12 +248,12 @@ def column_water(fields: dict) -> np.ndarray:
     return np.sum(q * rho * dz, axis=1)
 
 
-def config1_torch(seed: int = 0, ni: int = 1024, nj: int = 1024, nz: int = 65,
+def stretched_grid_torch(seed: int = 0, ni: int = 1024, nj: int = 1024, nz: int = 65,
                   device: str = "cuda", dtype=None, hail: bool = False, deep: bool = False,
                   clear_frac: float = 0.4):
-    """The config1 generator evaluated with torch on the GPU (for the 10^6-column
+    """The stretched-grid generator evaluated with torch on the GPU (for the 10^6-column
     benchmark, where the NumPy version would spend minutes on the host).  Same recipe
-    and distributions as :func:`_profiles` via :func:`_config1_cols`, drawn from a
+    and distributions as :func:`_profiles` via :func:`_stretched_cols`, drawn from a
     torch generator seeded with 2000 + seed, so the values differ from the NumPy
     stream.  Returns a dict of (nj, nz, ni) tensors."""
     import torch

@@ -8,7 +8,7 @@
   (point, field) pairs whose difference quotients are stable (eps and eps/2 agree), i.e.
   away from thresholds;
 * the FP32 gradient against the FP64 gradient.
-Workload: the stretched-grid generator (config-1), dt = 60 s.
+Workload: the stretched-grid generator, dt = 60 s.
 """
 import numpy as np
 import pytest
@@ -19,7 +19,7 @@ DIFF = ("t", "qv", "qc", "nc", "qr", "nr", "qi", "ni", "qs", "qg")
 
 
 def _setup(W, torch, dtype, ni=48, nj=8, seed=4):
-    wl = W.config1(seed=seed, ni=ni, nj=nj, steps=1, dt=60.0)
+    wl = W.stretched_grid(seed=seed, ni=ni, nj=nj, steps=1, dt=60.0)
     f = {k: torch.tensor(v, dtype=dtype, device="cuda") for k, v in wl.fields.items()}
     return wl, f
 

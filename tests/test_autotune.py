@@ -8,7 +8,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _fields(W, torch):
-    f = W.config1_torch(seed=3, ni=128, nj=64, nz=65, device="cuda", dtype=torch.float32)
+    f = W.stretched_grid_torch(seed=3, ni=128, nj=64, nz=65, device="cuda", dtype=torch.float32)
     d = {n: torch.zeros((64, 128), device="cuda") for n in ("rain_precip", "snow_liquid_equiv_precip")}
     d["refl10cm"] = torch.zeros((64, 65, 128), device="cuda")
     return f, d

@@ -15,7 +15,7 @@ OUT = ("t", "qv", "qc", "qr", "qi", "qs", "qg", "ni", "nr", "nc", "nwfa", "nifa"
 
 def _domain(torch, tg, ncol, nz, dt, seed):
     from tempo_gb300 import workloads as W
-    wl = W.config4_domain(ncol, nz, dt, seed)
+    wl = W.domain_set_member(ncol, nz, dt, seed)
     f = {k: torch.tensor(v.astype(np.float32), device="cuda") for k, v in wl.fields.items()}
     nj, nk, ni = f["p"].shape
     d = {n: torch.zeros((nj, ni), device="cuda") for n in tg.DIAG2}

@@ -68,9 +68,9 @@ def _workloads():
     diag = dict(rain_med_vol_diam_flag=1, graupel_med_vol_diam_flag=1,
                 cloud_number_mixing_ratio_flag=1)
     return [
-        ("config0", W.config0(ncol=256), dict(diag, hailaware_flag=0), False),
-        ("config1", W.config1(ni=64, nj=16, steps=1), dict(diag, hailaware_flag=0), False),
-        ("config2", W.config2(ni=32, nj=16), dict(diag, hailaware_flag=1), True),
+        ("uniform_grid", W.uniform_grid(ncol=256), dict(diag, hailaware_flag=0), False),
+        ("stretched_grid", W.stretched_grid(ni=64, nj=16, steps=1), dict(diag, hailaware_flag=0), False),
+        ("hail_convection", W.hail_convection(ni=32, nj=16), dict(diag, hailaware_flag=1), True),
     ]
 
 
@@ -99,7 +99,7 @@ def _run(tg, oracle_mod, oracle_tables, case, mixed):
     return name, ref, got, clean, ni * nj, nz
 
 
-@pytest.mark.parametrize("case", [0, 1, 2], ids=["config0", "config1", "config2"])
+@pytest.mark.parametrize("case", [0, 1, 2], ids=["uniform_grid", "stretched_grid", "hail_convection"])
 def test_fp64_decisions_equal_the_oracle(tg, oracle_mod, oracle_tables, case):
     name, ref, got, clean, ncol, nz = _run(tg, oracle_mod, oracle_tables, case, mixed=False)
     assert clean.mean() > 0.5
@@ -118,7 +118,7 @@ def _assert_indices_in_range(got, ncol, nz):
     assert not rng.any(), ("table index out of range", int(np.count_nonzero(rng)), hex(sites))
 
 
-@pytest.mark.parametrize("case", [1, 2], ids=["config1", "config2"])
+@pytest.mark.parametrize("case", [1, 2], ids=["stretched_grid", "hail_convection"])
 def test_mixed_decision_census(tg, oracle_mod, oracle_tables, case):
     """The mixed form against the oracle on the same FP32-rounded inputs: per slot, the
     number of points (columns) where an FP32 value took another table bin or branch.

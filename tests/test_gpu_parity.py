@@ -56,10 +56,10 @@ def test_gpu_table_build_matches_oracle(tg, oracle_tables, oracle_mod):
 
 
 @pytest.mark.parametrize("seed", [0, 1])
-def test_config0_fp64_matches_oracle(ctx_nohail, oracle_mod, seed):
+def test_uniform_grid_fp64_matches_oracle(ctx_nohail, oracle_mod, seed):
     from tempo_gb300 import workloads as W
     oracle_mod.init(False)
-    wl = W.config0(seed=seed)
+    wl = W.uniform_grid(seed=seed)
     over = dict(hailaware_flag=0)
     fo, do = run_oracle(oracle_mod, over, wl)
     fg, dg = run_gpu(ctx_nohail, over, wl)
@@ -69,10 +69,10 @@ def test_config0_fp64_matches_oracle(ctx_nohail, oracle_mod, seed):
     oracle_mod.init(True)
 
 
-def test_config2_hail_fp64_matches_oracle(ctx_hail, oracle_mod):
+def test_hail_convection_fp64_matches_oracle(ctx_hail, oracle_mod):
     from tempo_gb300 import workloads as W
     oracle_mod.init(True)
-    wl = W.config2(ni=32, nj=16)
+    wl = W.hail_convection(ni=32, nj=16)
     over = dict(hailaware_flag=1, rain_med_vol_diam_flag=1, graupel_med_vol_diam_flag=1,
                 cloud_number_mixing_ratio_flag=1)
     ties = np.zeros(wl.fields["p"].shape[::2], np.int32)
@@ -94,14 +94,14 @@ def test_config2_hail_fp64_matches_oracle(ctx_hail, oracle_mod):
     assert moved <= max(1, ties.size // 100), (moved, int((ties & 1).astype(bool).sum()))
 
 
-def test_config1_multistep_fp64_matches_oracle(ctx_nohail, oracle_mod):
+def test_stretched_grid_multistep_fp64_matches_oracle(ctx_nohail, oracle_mod):
     """Three consecutive steps on the stretched grid (dt = 30 s).  Each step starts
     both implementations from the same state (the oracle's previous output), so
     the comparison measures one step's round-off, not the divergence of two chaotic
     trajectories."""
     from tempo_gb300 import workloads as W
     oracle_mod.init(False)
-    wl = W.config1(ni=64, nj=8, steps=3)
+    wl = W.stretched_grid(ni=64, nj=8, steps=3)
     over = dict(hailaware_flag=0)
     state = {k: v.copy() for k, v in wl.fields.items()}
     for step in range(1, 4):
@@ -114,7 +114,7 @@ def test_config1_multistep_fp64_matches_oracle(ctx_nohail, oracle_mod):
     oracle_mod.init(True)
 
 
-def test_config1_fp64_water_budget_matches_oracle(ctx_nohail, oracle_mod):
+def test_stretched_grid_fp64_water_budget_matches_oracle(ctx_nohail, oracle_mod):
     """Column water (vapour and condensate, times density and layer depth) plus the
     surface precipitation, after the step minus before: the FP64 drop-in's budget
     equals the oracle's to round-off (1e-13 of the column's water) in every column, with
@@ -125,7 +125,7 @@ def test_config1_fp64_water_budget_matches_oracle(ctx_nohail, oracle_mod):
     oracle_mod.init(False)
     over = dict(hailaware_flag=0)
     for dt in (30.0, 120.0):
-        wl = W.config1(ni=64, nj=8, steps=1, dt=dt)
+        wl = W.stretched_grid(ni=64, nj=8, steps=1, dt=dt)
         x = wl.fields
         rho = RD / 461.5 * x["p"] / (RD * x["t"] * (np.maximum(1e-10, x["qv"]) + RD / 461.5))
 

@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 def _fields(dtype=np.float64):
     from tempo_gb300 import workloads as W
-    wl = W.config0(ncol=48)
+    wl = W.uniform_grid(ncol=48)
     return wl, {k: np.ascontiguousarray(v.astype(dtype)) for k, v in wl.fields.items()}
 
 

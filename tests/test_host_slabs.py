@@ -11,7 +11,7 @@ def test_slabbed_host_run_matches_device_run(tg):
     torch = pytest.importorskip("torch")
     from tempo_gb300 import workloads as W
     ni, nj, nz = 1024, 520, 65
-    f = W.config1_torch(seed=11, ni=ni, nj=nj, nz=nz, device="cuda", dtype=torch.float32)
+    f = W.stretched_grid_torch(seed=11, ni=ni, nj=nj, nz=nz, device="cuda", dtype=torch.float32)
     # tile rows 5..516 (512 rows = 2 slabs of 262 144 columns) inside memory rows 1..520
     b = [1, ni, 1, nj, 1, nz, 1, ni, 1, nj, 1, nz, 1, ni, 5, 516, 1, nz]
     tj = 516 - 5 + 1

@@ -20,7 +20,7 @@ MELT = dict(hailaware_flag=1, refl10cm_from_melting_flag=1)
 def test_oracle_melting_changes_only_reflectivity(oracle_mod):
     from tempo_gb300 import workloads as W
     oracle_mod.init(True)
-    wl = W.config2(ni=16, nj=8)
+    wl = W.hail_convection(ni=16, nj=8)
     fa, da = run_oracle(oracle_mod, dict(hailaware_flag=1), wl)
     fb, db = run_oracle(oracle_mod, MELT, wl)
     for k in fa:
@@ -47,7 +47,7 @@ def test_oracle_melting_changes_only_reflectivity(oracle_mod):
 def test_melting_fp64_matches_oracle(ctx_hail, oracle_mod):
     from tempo_gb300 import workloads as W
     oracle_mod.init(True)
-    wl = W.config2(ni=32, nj=16)
+    wl = W.hail_convection(ni=32, nj=16)
     over = dict(MELT, rain_med_vol_diam_flag=1, graupel_med_vol_diam_flag=1)
     ties = np.zeros(wl.fields["p"].shape[::2], np.int32)
     fo, do = run_oracle(oracle_mod, over, wl, ties=ties)
@@ -68,7 +68,7 @@ def test_melting_fp64_matches_oracle(ctx_hail, oracle_mod):
 @pytest.mark.gpu
 def test_melting_mixed_close_to_fp64(tg, ctx_hail):
     from tempo_gb300 import workloads as W
-    wl = W.config2(ni=32, nj=16)
+    wl = W.hail_convection(ni=32, nj=16)
     wl.fields = {k: v.astype(np.float32).astype(np.float64) for k, v in wl.fields.items()}
     f64, d64 = run_gpu(ctx_hail, MELT, wl)
     ctx_hail.set_precision(tg.PREC_MIXED)
@@ -86,7 +86,7 @@ def test_melting_mixed_close_to_fp64(tg, ctx_hail):
 def test_melting_rejected_where_unsupported(tg, ctx_hail):
     torch = pytest.importorskip("torch")
     from tempo_gb300 import workloads as W
-    wl = W.config2(ni=8, nj=4)
+    wl = W.hail_convection(ni=8, nj=4)
     f = {k: torch.tensor(v, device="cuda") for k, v in wl.fields.items()}
     cfg = tg.default_cfgs(**MELT)
     refl = torch.zeros(f["p"].shape, dtype=torch.float64, device="cuda")

@@ -27,7 +27,7 @@ pytestmark = pytest.mark.gpu
 
 PROG = ("t", "qv", "qc", "qr", "qi", "qs", "qg", "ni", "nr", "nc", "ng", "qb")
 # relative RMS per field: the 1e-5 target for every field on these samples (the
-# largest measured is 1.2e-6, nc of the config-2 sample; on the 262 144 columns of the
+# largest measured is 1.2e-6, nc of the hail-convection sample; on the 262 144 columns of the
 # bench's precision study a few columns that cross a discrete step move some fields
 # beyond it)
 REL_RMS = {n: 1e-5 for n in PROG}
@@ -106,19 +106,19 @@ def _check(out):
     return bad
 
 
-@pytest.mark.parametrize("case", ["config1", "config2", "config1_dt120"])
+@pytest.mark.parametrize("case", ["stretched_grid", "hail_convection", "stretched_grid_dt120"])
 def test_mixed_against_oracle(ctx_nohail, ctx_hail, oracle_mod, case):
-    """config1_dt120: the config-1 columns with a 120 s step, where rain near the
+    """stretched_grid_dt120: the stretched-grid columns with a 120 s step, where rain near the
     surface needs more than 8 sedimentation substeps, so the mixed form's level-by-level
     walk runs in several passes with the state stored in FP32 between them."""
     from tempo_gb300 import workloads as W
-    hail = case == "config2"
+    hail = case == "hail_convection"
     if hail:
-        wl = _rounded(W.config2(ni=32, nj=16))
-    elif case == "config1_dt120":
-        wl = _rounded(W.config1(ni=64, nj=16, steps=1, dt=120.0))
+        wl = _rounded(W.hail_convection(ni=32, nj=16))
+    elif case == "stretched_grid_dt120":
+        wl = _rounded(W.stretched_grid(ni=64, nj=16, steps=1, dt=120.0))
     else:
-        wl = _rounded(W.config1(ni=64, nj=16, steps=1))
+        wl = _rounded(W.stretched_grid(ni=64, nj=16, steps=1))
     ctx = ctx_hail if hail else ctx_nohail
     over = dict(hailaware_flag=int(hail), rain_med_vol_diam_flag=1, graupel_med_vol_diam_flag=1,
                 cloud_number_mixing_ratio_flag=1)

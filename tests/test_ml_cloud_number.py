@@ -21,7 +21,7 @@ WEIGHTS = Path(__file__).resolve().parent / "golden" / "ml_cloud_number.npz"
 
 def _workload():
     from tempo_gb300 import workloads as W
-    wl = copy(W.config1(ni=32, nj=8, steps=1))
+    wl = copy(W.stretched_grid(ni=32, nj=8, steps=1))
     wl.fields = {k: v for k, v in wl.fields.items() if k != "nc"}  # single-moment cloud
     return wl
 
@@ -114,7 +114,7 @@ def test_oracle_bl_changes_only_re_cloud(oracle_mod):
     oracle_mod.init(False)
     oracle_mod.set_ml(dict(np.load(WEIGHTS)))
     from tempo_gb300 import workloads as W
-    wl = W.config1(ni=32, nj=8, steps=1)
+    wl = W.stretched_grid(ni=32, nj=8, steps=1)
     fa, da = run_oracle(oracle_mod, dict(hailaware_flag=0), wl)
     fb, db = run_oracle(oracle_mod, dict(hailaware_flag=0), _with_bl(wl))
     for k in fa:
@@ -138,7 +138,7 @@ def test_bl_fp64_matches_oracle(tg, oracle_mod, oracle_tables):
                           cfgs=tg.default_cfgs(hailaware_flag=0))
     try:
         ctx.set_ml_cloud_number(weights)
-        wl = _with_bl(W.config1(ni=32, nj=8, steps=1))
+        wl = _with_bl(W.stretched_grid(ni=32, nj=8, steps=1))
         fo, do = run_oracle(oracle_mod, dict(hailaware_flag=0), wl)
         fg, dg = run_gpu(ctx, dict(hailaware_flag=0), wl)
         name, e = worst(compare(fg, dg, fo, do, inputs=wl.fields))

@@ -17,7 +17,7 @@ SEMI = dict(hailaware_flag=0, semi_sedi_flag=1)
 def test_oracle_semi_changes_only_rain_and_graupel_columns(oracle_mod):
     from tempo_gb300 import workloads as W
     oracle_mod.init(False)
-    wl = W.config1(ni=32, nj=8, steps=1, dt=60.0)
+    wl = W.stretched_grid(ni=32, nj=8, steps=1, dt=60.0)
     fe, de = run_oracle(oracle_mod, dict(hailaware_flag=0), wl)
     fs, ds = run_oracle(oracle_mod, SEMI, wl)
     moving = np.zeros(wl.fields["p"].shape[::2], bool)
@@ -77,7 +77,7 @@ def _check_calibrated(frac, calib):
 def test_semi_fp64_matches_oracle(ctx_nohail, oracle_mod):
     from tempo_gb300 import workloads as W
     oracle_mod.init(False)
-    wl = W.config1(ni=64, nj=8, steps=2, dt=60.0)
+    wl = W.stretched_grid(ni=64, nj=8, steps=2, dt=60.0)
     state = {k: v.copy() for k, v in wl.fields.items()}
     for step in (1, 2):
         calib = _self_fraction(oracle_mod, SEMI, wl, state, step)
@@ -92,7 +92,7 @@ def test_semi_fp64_matches_oracle(ctx_nohail, oracle_mod):
 def test_semi_hail_fp64_matches_oracle(ctx_hail, oracle_mod):
     from tempo_gb300 import workloads as W
     oracle_mod.init(True)
-    wl = W.config2(ni=32, nj=16, dt=60.0)
+    wl = W.hail_convection(ni=32, nj=16, dt=60.0)
     over = dict(hailaware_flag=1, semi_sedi_flag=1, rain_med_vol_diam_flag=1,
                 graupel_med_vol_diam_flag=1)
     calib = _self_fraction(oracle_mod, over, wl)
@@ -114,7 +114,7 @@ def test_semi_mixed_close_to_fp64(tg, ctx_nohail):
     path's, but by a bounded factor; column precipitation agrees to 1e-4."""
     from copy import copy
     from tempo_gb300 import workloads as W
-    wl = copy(W.config1(ni=64, nj=8, steps=1, dt=60.0))
+    wl = copy(W.stretched_grid(ni=64, nj=8, steps=1, dt=60.0))
     wl.fields = {k: v.astype(np.float32).astype(np.float64) for k, v in wl.fields.items()}
 
     def fractions(over):
@@ -144,7 +144,7 @@ def test_semi_mixed_close_to_fp64(tg, ctx_nohail):
 def test_semi_rejected_where_unsupported(tg, ctx_nohail):
     torch = pytest.importorskip("torch")
     from tempo_gb300 import workloads as W
-    wl = W.config1(ni=8, nj=4, steps=1, dt=60.0)
+    wl = W.stretched_grid(ni=8, nj=4, steps=1, dt=60.0)
     f = {k: torch.tensor(v, device="cuda") for k, v in wl.fields.items()}
     cfg = tg.default_cfgs(hailaware_flag=0, semi_sedi_flag=1)
     with pytest.raises(tg.TempoError) as e:

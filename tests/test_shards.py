@@ -59,7 +59,7 @@ def _rank_main(rank, world, port, outdir):
     oracle.build()
     oracle.init(False, REPO / "tables" / "ccn_activate.bin")
     oracle.build_big_tables(nthreads=2)
-    wl = W.config1(seed=3, ni=12, nj=7, steps=1)
+    wl = W.stretched_grid(seed=3, ni=12, nj=7, steps=1)
     f = {k: v.copy() for k, v in wl.fields.items()}
     nj, nk, ni = f["p"].shape
     full = [1, ni, 1, nj, 1, nk] * 3
@@ -98,7 +98,7 @@ def test_two_gloo_ranks_match_whole_domain(tmp_path, oracle_mod):
     o = oracle_mod
     o.init(False, REPO / "tables" / "ccn_activate.bin")
     o.build_big_tables(nthreads=2)
-    wl = W.config1(seed=3, ni=12, nj=7, steps=1)
+    wl = W.stretched_grid(seed=3, ni=12, nj=7, steps=1)
     f = {k: v.copy() for k, v in wl.fields.items()}
     d = make_diags(f["p"].shape)
     assert o.run(o.default_cfgs(hailaware_flag=0), wl.dt, 1, f, d, nthreads=1) == 0

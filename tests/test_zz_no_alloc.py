@@ -22,7 +22,7 @@ def test_noalloc_step_matches_allocating_step(tg, ctx_nohail):
     torch = pytest.importorskip("torch")
     from tempo_gb300 import workloads as W
     ctx = ctx_nohail
-    wl = W.config1(seed=5, ni=40, nj=25, steps=2, dt=30.0)      # 1000 columns x 65 levels
+    wl = W.stretched_grid(seed=5, ni=40, nj=25, steps=2, dt=30.0)      # 1000 columns x 65 levels
     f = {k: torch.tensor(v.astype(np.float32), device="cuda") for k, v in wl.fields.items()}
     nj, nk, ni = f["p"].shape
     a = {k: v.clone() for k, v in f.items()}
@@ -46,7 +46,7 @@ def test_noalloc_rejects_tiles_beyond_its_scratch(tg, ctx_nohail):
     torch = pytest.importorskip("torch")
     from tempo_gb300 import workloads as W
     ctx = ctx_nohail
-    wl = W.config1(seed=6, ni=128, nj=64, steps=1, dt=30.0)     # 8192 columns > ~4200
+    wl = W.stretched_grid(seed=6, ni=128, nj=64, steps=1, dt=30.0)     # 8192 columns > ~4200
     f = {k: torch.tensor(v.astype(np.float32), device="cuda") for k, v in wl.fields.items()}
     before = {k: v.clone() for k, v in f.items()}
     ctx.set_precision(tg.PREC_MIXED)
@@ -68,7 +68,7 @@ def test_noalloc_allocates_nothing_and_records_no_kernel_times(tg, ctx_nohail):
     torch = pytest.importorskip("torch")
     from tempo_gb300 import workloads as W
     ctx = ctx_nohail
-    wl = W.config1(seed=7, ni=32, nj=20, steps=4, dt=30.0)       # 640 columns
+    wl = W.stretched_grid(seed=7, ni=32, nj=20, steps=4, dt=30.0)       # 640 columns
     f = {k: torch.tensor(v.astype(np.float32), device="cuda") for k, v in wl.fields.items()}
     nj, nk, ni = f["p"].shape
     d = _diags(torch, nj, nk, ni, tg)
