@@ -262,7 +262,8 @@ int tempo_run_batch_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, 
                               const tempo_domain_t *domains, void *stream);
 
 /* tempo_aerosol_surface_emissions (src/module_mp_tempo_driver.F90:516-529) on device
- * arrays: nwfa(i,kts,j) += nwfa2d(i,j)*dt over the memory range. */
+ * arrays: nwfa(i,kts,j) += nwfa2d(i,j)*dt over the memory range.  The calling thread's
+ * current device must be the context's (otherwise TEMPO_ERR_STATE, nothing enqueued). */
 int tempo_aerosol_surface_emissions_dev_c(tempo_ctx_t *ctx, double dt, double *nwfa,
                                           const double *nwfa2d, int ims, int ime, int jms,
                                           int jme, int kms, int kme, int kts, void *stream);
@@ -325,7 +326,8 @@ int tempo_autotune_dev_f32_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, f
  * qv, qc, nc, qr, nr, qi, ni, qs, qg and, hail-aware, ng and qb; NULL entries = zero),
  * is replaced by the tangent of the outputs.  ddiags receives the tangents of the
  * requested diagnostics.  Branches, clips and table bins are those of the trajectory
- * from x.  Returns after the step has finished. */
+ * from x.  Returns after the step has finished.  The calling thread's current device
+ * must be the context's (otherwise TEMPO_ERR_STATE before any work). */
 int tempo_tl_dev_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double dt, int itimestep,
                    int fp64, tempo_state_t *x, tempo_state_t *dx, tempo_diags_t *tempo_diags,
                    tempo_diags_t *tangent_diags, int ims, int ime, int jms, int jme, int kms,
@@ -337,7 +339,8 @@ int tempo_tl_dev_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double dt, 
  * its inputs; lam_diags (optional) gives the adjoints of the surface precipitation
  * (rain, ice, snow, graupel) and of refl10cm (dBZ).  Needs device memory for the
  * recomputed trajectory and checkpoints (about 10x the state).  Returns after the
- * adjoint has finished. */
+ * adjoint has finished.  As for tempo_tl_dev_c, the calling thread's current device must
+ * be the context's. */
 int tempo_adjoint_dev_c(tempo_ctx_t *ctx, const tempo_cfgs_t *tempo_cfgs, double dt,
                         int itimestep, int fp64, const tempo_state_t *x, tempo_state_t *lam,
                         const tempo_diags_t *lam_diags, int ims, int ime, int jms, int jme,

@@ -1746,7 +1746,7 @@ int tl_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep, temp
     return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation, the "
                 "melting-layer reflectivity and the ML cloud number are not implemented by this library");
   if (cfg->max_hail_diameter_flag) ap.mhd_sfc = ap.mhd_col = nullptr;  // not differentiable
-  CUDA_TRY(cudaSetDevice(c->device));
+  if (int rc = check_current_device(c)) return rc;
   DevBufs B;
   DualStep<T> st;
   const RunArrays<T> DX = dx ? arrays_of<T>(dx) : RunArrays<T>{};
@@ -1785,7 +1785,7 @@ int adjoint_dev(tempo_ctx* c, const tempo_cfgs_t* cfg, double dt, int itimestep,
   if (ap.flags & (F_SEMI | F_MELT | F_MLNC))
     return fail(TEMPO_ERR_UNSUPPORTED, "derivatives of the semi-Lagrangian sedimentation, the "
                 "melting-layer reflectivity and the ML cloud number are not implemented by this library");
-  CUDA_TRY(cudaSetDevice(c->device));
+  if (int rc = check_current_device(c)) return rc;
   DevBufs B;
   using D1 = Dual<T, 1>;
   // 1. forward trajectory on packed copies (zero tangents): prep and phase A
@@ -1939,6 +1939,7 @@ int tempo_aerosol_surface_emissions_dev_c(tempo_ctx_t* c, double dt, double* nwf
   if (!nwfa || !nwfa2d) return fail(TEMPO_ERR_ARG, "NULL array");
   if (ime < ims || jme < jms || kme < kms || kts < kms || kts > kme)
     return fail(TEMPO_ERR_ARG, "bad bounds");
+  if (int rc = check_current_device(c)) return rc;
   cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
   CUDA_TRY(launch_surface_emissions(nwfa, nwfa2d, ime - ims + 1, kme - kms + 1, jme - jms + 1,
                                     kts - kms, dt, s));
