@@ -84,3 +84,36 @@ def test_one_fp32_ulp_of_input_moves_outputs_beyond_1e5(oracle_mod, oracle_table
     assert r["qc"]["frac"] > 0.05, r["qc"]
     assert r["qg"]["frac"] > 1e-3, r["qg"]
     assert r["nc"]["frac"] > 1e-3 and r["nc"]["rel_rms"] > 1e-5, r["nc"]
+
+
+def test_one_fp32_ulp_of_input_flips_decisions(oracle_mod, oracle_tables):
+    """The same change flips table bins and branches of the FP64 step itself: 9.0e-5 of
+    the stretched-grid sample's points (droplet-evaporation bins, condensation and final
+    existence checks), 1.9e-4 on 65 536 hail-convection columns -- the yardstick for
+    the mixed form's decision flips against the oracle."""
+    from parity_util import make_diags
+    from tempo_gb300 import workloads as W
+    from trace_util import mismatches
+    wl = W.stretched_grid(ni=64, nj=16, steps=1)
+    over = dict(rain_med_vol_diam_flag=1, graupel_med_vol_diam_flag=1,
+                cloud_number_mixing_ratio_flag=1, hailaware_flag=0)
+    nj, nz, ni = wl.fields["p"].shape
+
+    def trace(w):
+        f = {k: v.copy() for k, v in w.fields.items()}
+        tr = np.zeros(oracle_mod.trace_size(ni * nj, nz), np.int32)
+        ties = np.zeros((nj, ni), np.int32)
+        rc = oracle_mod.run(oracle_mod.default_cfgs(**over), w.dt, 1, f, make_diags(f["p"].shape),
+                            ties=ties, trace=tr)
+        assert rc == 0
+        return tr, ties
+
+    oracle_mod.init(False)
+    try:
+        a, ta = trace(_fp32(wl))
+        b, tb = trace(_one_ulp(wl, 1))
+    finally:
+        oracle_mod.init(True)
+    clean = ((ta.ravel() | tb.ravel()) & 1) == 0
+    flips = sum(mismatches(b, a, ni * nj, nz, clean).values()) / (int(clean.sum()) * nz)
+    assert 1e-5 < flips < 1e-3, flips
